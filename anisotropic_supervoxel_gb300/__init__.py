@@ -1,0 +1,9 @@
+"""GB300-native supervoxel engine: the JFA + Lloyd hot path of
+dongxiao0401/anisotropic_supervoxel behind a C ABI (include/asv.h).
+
+Python here is a thin host mirror over libasv.so (ctypes); the compute runs
+in the CUDA kernels of csrc/.
+"""
+from ._lib import AsvError, load  # noqa: F401
+from .image import (Image, config, preprocess_frame, synth_clip, write_labels_txt,  # noqa: F401
+                    write_render_ppm)

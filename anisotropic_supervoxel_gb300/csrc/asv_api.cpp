@@ -1,0 +1,853 @@
+// asv_api.cpp -- host side of the C ABI (include/asv.h): context, device
+// memory layout, host seed grid, stage sequencing and CUDA-graph replay.
+//
+// The stage functions follow the reference's Image methods; the reference
+// line ranges are in include/asv.h next to each declaration.
+#include "asv.h"
+#include "asv_common.cuh"
+#include "asv_internal.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace asv {
+
+// ---------------------------------------------------------------------------
+// Seed grid (GPU-AS/Image.cpp:20-92; streamGPU-AS/Image.cpp:26-103), host.
+// ---------------------------------------------------------------------------
+int grid_seeds(int W, int H, int D, int K, int middlebury, GridInfo *g, std::vector<float> *seeds4)
+{
+    if (W < 1 || H < 1 || D < 1 || K < 1) return -1;
+    long long N = (long long)W * H * D;
+    double voxel_size = (double)(N / K);
+    int s = middlebury ? (int)std::floor(std::pow(1.0 * W * H / K, 0.5))
+                       : (int)std::floor(std::pow(voxel_size, 1.0 / 3));
+    long long kdd = (long long)K * D * D / W / H;
+    int dNum = (int)std::pow((double)(float)kdd, 1.0 / 3.0);
+    if (dNum == 0) dNum = 1;
+    int fsn = K / dNum;
+    int wNum = (int)std::sqrt((float)((long long)fsn * W / H));
+    if (wNum == 0) return -2;
+    int hNum = fsn / wNum;
+    if (hNum == 0) return -2;
+    g->s = s; g->dNum = dNum; g->hNum = hNum; g->wNum = wNum; g->Kp = dNum * hNum * wNum;
+    if (!seeds4) return g->Kp;
+    seeds4->clear();
+    int stepD = D / dNum, stepH = H / hNum, stepW = W / wNum;
+    int d_rem = D - stepD * dNum, h_rem = H - stepH * hNum, w_rem = W - stepW * wNum;
+    int td = d_rem < 1 ? 0 : 1;
+    int count = 0;
+    for (int k = 0; k < dNum; k++) {
+        int th = 1;
+        for (int i = 0; i < hNum; i++) {
+            int tw = 1;
+            for (int j = 0; j < wNum; j++) {
+                int sx = (int)(j * stepW + 0.5 * stepW + tw);
+                int sy = (int)(i * stepH + 0.5 * stepH + th);
+                int sz = (int)(k * stepD + 0.5 * stepD + td);
+                sx = std::min(sx, W - 1); sy = std::min(sy, H - 1); sz = std::min(sz, D - 1);
+                if (tw < w_rem) tw++;
+                seeds4->push_back((float)(sx + 0.5));
+                seeds4->push_back((float)(sy + 0.5));
+                seeds4->push_back((float)(sz + 0.5));
+                seeds4->push_back((float)count++);
+            }
+            if (th < h_rem) th++;
+        }
+        if (td < d_rem) td++;
+    }
+    return g->Kp;
+}
+
+// cell tables of the density placement (Image.cpp:360-468): per x (y, z)
+// the largest grid column (row, layer) whose range holds it, then the x
+// ranges of the columns.
+void cell_tables(int W, int H, int D, const GridInfo &g, const std::vector<float> &grid,
+                 std::vector<int> *cells)
+{
+    auto mid = [](float a, float b) { return (int)std::floor(0.5 * (double)(a + b)); };
+    std::vector<int> xl(g.wNum), xr(g.wNum), yl(g.hNum), yr(g.hNum), zl(g.dNum), zr(g.dNum);
+    for (int i = 0; i < g.wNum; i++) {
+        float c = grid[4 * i];
+        xl[i] = i > 0 ? mid(grid[4 * (i - 1)], c) : 0;
+        xr[i] = i < g.wNum - 1 ? mid(grid[4 * (i + 1)], c) : W - 1;
+    }
+    for (int j = 0; j < g.hNum; j++) {
+        float c = grid[4 * (j * g.wNum) + 1];
+        yl[j] = j > 0 ? mid(grid[4 * ((j - 1) * g.wNum) + 1], c) : 0;
+        yr[j] = j < g.hNum - 1 ? mid(grid[4 * ((j + 1) * g.wNum) + 1], c) : H - 1;
+    }
+    for (int t = 0; t < g.dNum; t++) {
+        float c = grid[4 * (t * g.wNum * g.hNum) + 2];
+        zl[t] = t > 0 ? mid(grid[4 * ((t - 1) * g.wNum * g.hNum) + 2], c) : 0;
+        zr[t] = t < g.dNum - 1 ? mid(grid[4 * ((t + 1) * g.wNum * g.hNum) + 2], c) : D - 1;
+    }
+    cells->assign((size_t)W + H + D + 2 * g.wNum, -1);
+    for (int x = 0; x < W; x++) for (int i = 0; i < g.wNum; i++) if (xl[i] <= x && x <= xr[i]) (*cells)[x] = i;
+    for (int y = 0; y < H; y++) for (int j = 0; j < g.hNum; j++) if (yl[j] <= y && y <= yr[j]) (*cells)[W + y] = j;
+    for (int z = 0; z < D; z++) for (int t = 0; t < g.dNum; t++) if (zl[t] <= z && z <= zr[t]) (*cells)[W + H + z] = t;
+    for (int i = 0; i < g.wNum; i++) { (*cells)[W + H + D + i] = xl[i]; (*cells)[W + H + D + g.wNum + i] = xr[i]; }
+}
+
+float ratio_of(int s, float compactness)
+{
+    float q = compactness / (float)s;
+    return q * q;
+}
+
+// JFA ladder (GPU-AS/Image.cpp:1055-1190): [1] + [floor(s/2) halving with
+// floor(x/2+0.5) down to 1] + [2, 1] (last two at 2x ratio).
+int ladder(int s, int full, int maxdim, int *steps, float *rmul, int cap)
+{
+    int n = 0;
+    auto push = [&](int st, float rm) { if (n < cap) { steps[n] = st; rmul[n] = rm; } n++; };
+    push(1, 1.0f);
+    if (!full) {
+        float st = (float)std::floor(0.5 * s);
+        while (st > 0) {
+            push((int)st, 1.0f);
+            if ((int)st == 1) st = 0;
+            st = (float)std::floor(0.5 * st + 0.5);
+        }
+    } else {
+        int p = 1;
+        while (p * 2 <= maxdim) p *= 2;
+        for (; p >= 1; p /= 2) push(p, 1.0f);
+    }
+    push(2, 2.0f);
+    push(1, 2.0f);
+    return n;
+}
+
+} // namespace asv
+
+using namespace asv;
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+struct asv_ctx {
+    asv_config cfg;
+    cudaStream_t st = nullptr;
+    bool own_st = false;
+    std::string err;
+    // layout
+    std::vector<SegHost> seg;
+    std::vector<SegDesc> sd;
+    AsvDev d{};
+    std::vector<void *> allocs;
+    size_t bytes = 0;
+    int jfa_blocks = 0;
+    int maxpass = 0;
+    // state
+    bool have_rgb = false, have_flow = false, have_pos0 = false, have_M0 = false, have_lab = false;
+    bool seeded = false, ran = false;
+    int post_host[ASV_POST_WORDS];
+    // graph
+    cudaGraphExec_t gexec = nullptr;
+    // instrumentation
+    asv_stats stats{};
+    std::vector<cudaEvent_t> ev;
+    int launches = 0;
+};
+
+static asv_status fail(asv_ctx *c, asv_status s, const std::string &m)
+{
+    if (c) c->err = m;
+    return s;
+}
+
+static asv_status cuda_fail(asv_ctx *c, cudaError_t e, const char *where)
+{
+    return fail(c, ASV_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                                     \
+    do {                                                             \
+        cudaError_t e_ = (call);                                     \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call);     \
+    } while (0)
+
+static void free_layout(asv_ctx *ctx)
+{
+    if (ctx->gexec) { cudaGraphExecDestroy(ctx->gexec); ctx->gexec = nullptr; }
+    for (void *p : ctx->allocs) cudaFree(p);
+    ctx->allocs.clear();
+    ctx->bytes = 0;
+    ctx->d = AsvDev{};
+    ctx->have_rgb = ctx->have_flow = ctx->have_pos0 = ctx->have_M0 = ctx->have_lab = false;
+    ctx->seeded = ctx->ran = false;
+}
+
+template <typename T>
+static asv_status dalloc(asv_ctx *ctx, T **p, size_t n)
+{
+    size_t b = std::max<size_t>(n, 1) * sizeof(T);
+    b = (b + 255) & ~(size_t)255;
+    if (ctx->cfg.hbm_budget && ctx->bytes + b > ctx->cfg.hbm_budget)
+        return fail(ctx, ASV_ERR_OVER_BUDGET, "allocation exceeds the configured HBM budget");
+    void *q = nullptr;
+    cudaError_t e = cudaMalloc(&q, b);
+    if (e != cudaSuccess) { cudaGetLastError(); return fail(ctx, ASV_ERR_OOM, std::string("cudaMalloc: ") + cudaGetErrorString(e)); }
+    ctx->allocs.push_back(q);
+    ctx->bytes += b;
+    *p = (T *)q;
+    return ASV_OK;
+}
+
+#define AL(ptr, n)                                              \
+    do {                                                        \
+        asv_status s_ = dalloc(ctx, &(ptr), (n));               \
+        if (s_ != ASV_OK) { free_layout(ctx); return s_; }      \
+    } while (0)
+
+// Prepares one segment's host description (grid, ladder, cells).
+asv_status asv_prepare_segment(asv_ctx *ctx, int W, int H, int D, int K, SegHost *sh)
+{
+    if (W < 1 || H < 1 || D < 2 || W > 4096 || H > 4096 || D > 4096 || K < 1)
+        return fail(ctx, ASV_ERR_BAD_ARG, "need 1 <= W,H <= 4096, 2 <= D <= 4096, K >= 1");
+    sh->W = W; sh->H = H; sh->D = D; sh->K = K;
+    if (grid_seeds(W, H, D, K, ctx->cfg.middlebury, &sh->g, &sh->grid) <= 0)
+        return fail(ctx, ASV_ERR_BAD_ARG, "K too small for the seed grid (no column or row)");
+    if (sh->g.Kp >= 32768) return fail(ctx, ASV_ERR_BAD_ARG, "more than 32767 seeds");
+    if (sh->g.s < 1) return fail(ctx, ASV_ERR_BAD_ARG, "K larger than the voxel count");
+    sh->Kp = sh->g.Kp;
+    float compact = ctx->cfg.variant == ASV_VARIANT_STREAM ? 6.0f : 8.0f;
+    sh->ratio = ratio_of(sh->g.s, compact);
+    int maxdim = std::max(W, std::max(H, D));
+    sh->npass = ladder(sh->g.s, ctx->cfg.full_ladder, maxdim, sh->steps, sh->rmul, ASV_MAXP);
+    if (sh->npass > ASV_MAXP) return fail(ctx, ASV_ERR_BAD_ARG, "JFA ladder longer than 32 passes");
+    cell_tables(W, H, D, sh->g, sh->grid, &sh->cells);
+    return ASV_OK;
+}
+
+size_t asv_layout_bytes(const std::vector<SegHost> &seg)
+{
+    size_t vox = 0, seeds = 0, cells = 0, chunks = 0;
+    for (auto &s : seg) {
+        long long n = (long long)s.W * s.H * s.D;
+        vox += (size_t)((n + ASV_CHUNK - 1) / ASV_CHUNK) * ASV_CHUNK;
+        chunks += (size_t)((n + ASV_CHUNK - 1) / ASV_CHUNK);
+        seeds += (size_t)((s.Kp + 64 + 31) / 32) * 32;
+        cells += s.W + s.H + s.D + 2 * s.g.wNum;
+    }
+    size_t per_vox = 3 + 4 + 8 + 8 + 4 + 4;
+    size_t per_seed = 16 * 4 + 4 * 8 * 2 + 3 * 16 + 8 * 8 + 8 * 4 + 4 + ASV_RING * (32 + 4) + 16 + 8 + 4;
+    return vox * per_vox + seeds * per_seed + cells * 4 + chunks * 4 + 4096 + seg.size() * 1024;
+}
+
+// Allocates the packed device arrays for the segments in ctx->seg.
+asv_status asv_build_layout(asv_ctx *ctx)
+{
+    free_layout(ctx);
+    const int nseg = (int)ctx->seg.size();
+    std::vector<int> tile_p(nseg + 1), chunk_p(nseg + 1), seed_p(nseg + 1);
+    long long vox = 0;
+    int tiles = 0, chunks = 0, seeds = 0, cells = 0;
+    ctx->sd.assign(nseg, SegDesc{});
+    ctx->maxpass = 0;
+    for (int i = 0; i < nseg; i++) {
+        SegHost &h = ctx->seg[i];
+        SegDesc &s = ctx->sd[i];
+        long long n = (long long)h.W * h.H * h.D;
+        s.W = h.W; s.H = h.H; s.D = h.D; s.Kp = h.Kp;
+        s.vox_off = vox; s.nvox = n;
+        s.seed_off = seeds;
+        s.npass = h.npass;
+        for (int p = 0; p < h.npass; p++) { s.steps[p] = h.steps[p]; s.ratio[p] = h.rmul[p] * h.ratio; }
+        s.tiles_x = (h.W + ASV_TILE_X - 1) / ASV_TILE_X;
+        s.tiles_y = (h.H + ASV_TILE_Y - 1) / ASV_TILE_Y;
+        s.angle_filter = ctx->cfg.variant == ASV_VARIANT_PLAIN ? 1 : 0;
+        s.wNum = h.g.wNum; s.hNum = h.g.hNum; s.dNum = h.g.dNum;
+        s.cell_off = cells;
+        s.final_buf = h.npass & 1;
+        h.vox_off = vox; h.seed_off = seeds;
+        tile_p[i] = tiles; chunk_p[i] = chunks; seed_p[i] = seeds;
+        int nchunk = (int)((n + ASV_CHUNK - 1) / ASV_CHUNK);
+        vox += (long long)nchunk * ASV_CHUNK;
+        chunks += nchunk;
+        tiles += s.tiles_x * s.tiles_y * h.D;
+        seeds += ((h.Kp + 64 + 31) / 32) * 32;
+        cells += h.W + h.H + h.D + 2 * h.g.wNum;
+        ctx->maxpass = std::max(ctx->maxpass, h.npass);
+    }
+    tile_p[nseg] = tiles; chunk_p[nseg] = chunks; seed_p[nseg] = seeds;
+    AsvDev &d = ctx->d;
+    d.nseg = nseg;
+    d.total_tiles = tiles; d.total_chunks = chunks; d.total_seeds = seeds;
+    SegDesc *segs; int *tp, *cp, *sp;
+    AL(segs, nseg); AL(tp, nseg + 1); AL(cp, nseg + 1); AL(sp, nseg + 1);
+    d.segs = segs; d.tile_prefix = tp; d.chunk_prefix = cp; d.seed_prefix = sp;
+    AL(d.rgb, (size_t)vox * 3);
+    AL(d.lab, (size_t)vox);
+    AL(d.fwd, (size_t)vox);
+    AL(d.bwd, (size_t)vox);
+    AL(d.labA, (size_t)vox);
+    AL(d.labB, (size_t)vox);
+    AL(d.pos0, seeds); AL(d.M0, (size_t)seeds * 8);
+    AL(d.pos, seeds); AL(d.slab, seeds); AL(d.M, (size_t)seeds * 8);
+    AL(d.jtab, (size_t)seeds * 3);
+    AL(d.sums, (size_t)seeds * 8);
+    AL(d.Mself, (size_t)seeds * 8); AL(d.neg, seeds);
+    AL(d.Mring, (size_t)seeds * ASV_RING * 8); AL(d.ringok, (size_t)seeds * ASV_RING);
+    AL(d.grid, seeds);
+    AL(d.dacc, seeds);
+    AL(d.cells, std::max(cells, 1));
+    AL(d.post, (size_t)nseg * ASV_POST_WORDS);
+    AL(d.rank, seeds);
+    AL(d.scan, std::max(chunks, 1));
+    AL(d.srgb, 256);
+    AL(d.err, 4);
+    CK(cudaMemcpyAsync(segs, ctx->sd.data(), sizeof(SegDesc) * nseg, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(tp, tile_p.data(), sizeof(int) * (nseg + 1), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(cp, chunk_p.data(), sizeof(int) * (nseg + 1), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(sp, seed_p.data(), sizeof(int) * (nseg + 1), cudaMemcpyHostToDevice, ctx->st));
+    std::vector<int> allcells((size_t)std::max(cells, 1), -1);
+    std::vector<float4> grid((size_t)seeds, make_float4(0, 0, 0, -1));
+    for (int i = 0; i < nseg; i++) {
+        SegHost &h = ctx->seg[i];
+        std::copy(h.cells.begin(), h.cells.end(), allcells.begin() + ctx->sd[i].cell_off);
+        for (int k = 0; k < h.Kp; k++)
+            grid[h.seed_off + k] = make_float4(h.grid[4 * k], h.grid[4 * k + 1], h.grid[4 * k + 2], h.grid[4 * k + 3]);
+    }
+    CK(cudaMemcpyAsync(d.cells, allcells.data(), sizeof(int) * allcells.size(), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(d.grid, grid.data(), sizeof(float4) * grid.size(), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemsetAsync(d.post, 0, sizeof(int) * nseg * ASV_POST_WORDS, ctx->st));
+    CK(cudaMemsetAsync(d.err, 0, 16, ctx->st));
+    CK(cudaMemsetAsync(d.pos0, 0, sizeof(float4) * seeds, ctx->st));
+    CK(cudaMemsetAsync(d.pos, 0, sizeof(float4) * seeds, ctx->st));
+    CK(cudaMemsetAsync(d.slab, 0, sizeof(float4) * seeds, ctx->st));
+    CK(cudaMemsetAsync(d.M0, 0, sizeof(float) * 8 * seeds, ctx->st));
+    CK(cudaMemsetAsync(d.M, 0, sizeof(float) * 8 * seeds, ctx->st));
+    asv_launch_srgb_table(d, ctx->st);
+    CK(cudaGetLastError());
+    ctx->jfa_blocks = asv_jfa_grid_blocks(std::max(tiles, 1));
+    return ASV_OK;
+}
+
+// ---------------------------------------------------------------------------
+// stage sequencing
+// ---------------------------------------------------------------------------
+static void rec_begin(asv_ctx *ctx, int idx)
+{
+    if (ctx->cfg.instrument && !ctx->gexec) cudaEventRecord(ctx->ev[idx], ctx->st);
+}
+
+static asv_status ensure_events(asv_ctx *ctx, size_t n)
+{
+    while (ctx->ev.size() < n) {
+        cudaEvent_t e;
+        CK(cudaEventCreate(&e));
+        ctx->ev.push_back(e);
+    }
+    return ASV_OK;
+}
+
+static void do_first_init(asv_ctx *ctx)
+{
+    asv_launch_first_init(ctx->d, ctx->st);
+    cudaMemsetAsync(ctx->d.labA, 0xff, sizeof(int32_t) * (size_t)ctx->d.total_chunks * ASV_CHUNK, ctx->st);
+    asv_launch_draw(ctx->d, ctx->st);
+    ctx->launches += 2;
+}
+
+static void do_flood(asv_ctx *ctx, int evbase)
+{
+    for (int p = 0; p < ctx->maxpass; p++) {
+        if (evbase >= 0) rec_begin(ctx, evbase + 2 * p);
+        asv_launch_jfa(ctx->d, p, ctx->jfa_blocks, ctx->st);
+        if (evbase >= 0) rec_begin(ctx, evbase + 2 * p + 1);
+        ctx->launches++;
+    }
+}
+
+static void do_centroids(asv_ctx *ctx, bool reseed)
+{
+    cudaMemsetAsync(ctx->d.sums, 0, sizeof(unsigned long long) * 8 * (size_t)ctx->d.total_seeds, ctx->st);
+    asv_launch_centroids(ctx->d, ctx->st);
+    ctx->launches++;
+    if (reseed) { asv_launch_finalize(ctx->d, ctx->st); ctx->launches++; }
+}
+
+static void do_next_seeds(asv_ctx *ctx)
+{
+    asv_launch_metric(ctx->d, 1, ctx->st);
+    cudaMemsetAsync(ctx->d.labA, 0xff, sizeof(int32_t) * (size_t)ctx->d.total_chunks * ASV_CHUNK, ctx->st);
+    asv_launch_draw(ctx->d, ctx->st);
+    ctx->launches += 4;
+}
+
+static void do_post(asv_ctx *ctx)
+{
+    asv_launch_post(ctx->d, ctx->st);
+    ctx->launches += 4;
+}
+
+// the Lloyd loop of Render::run (GPU-AS/Render.cpp:277-303)
+static void enqueue_lloyd(asv_ctx *ctx, bool instrument)
+{
+    const int I = ctx->cfg.lloyd_iters;
+    const int per_it = 2 * ctx->maxpass;
+    do_first_init(ctx);
+    for (int it = 1; it <= I; it++) {
+        if (it > 1) do_next_seeds(ctx);
+        do_flood(ctx, instrument ? (it - 1) * per_it : -1);
+        do_centroids(ctx, it != I);
+    }
+    do_post(ctx);
+}
+
+static asv_status check_ready(asv_ctx *ctx)
+{
+    if (ctx->seg.empty()) return fail(ctx, ASV_ERR_STATE, "no clip: call asv_init_gpu first");
+    if (!ctx->have_flow) return fail(ctx, ASV_ERR_STATE, "no flow: call asv_upload_flow first");
+    if (!ctx->have_pos0) return fail(ctx, ASV_ERR_STATE, "no seeds: call asv_initialization first");
+    if (!ctx->have_M0) return fail(ctx, ASV_ERR_STATE, "no metric: call asv_seed_matrix first");
+    if (!ctx->have_lab) return fail(ctx, ASV_ERR_STATE, "no LAB volume: call asv_rgb2lab first");
+    return ASV_OK;
+}
+
+static asv_status read_post(asv_ctx *ctx)
+{
+    std::vector<int> rec(ctx->seg.size() * ASV_POST_WORDS);
+    CK(cudaMemcpyAsync(rec.data(), ctx->d.post, sizeof(int) * rec.size(), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    for (size_t i = 0; i < ctx->seg.size(); i++) {
+        ctx->seg[i].dead = rec[i * ASV_POST_WORDS + POST_DEAD];
+        ctx->seg[i].neg = rec[i * ASV_POST_WORDS + POST_NEG];
+        ctx->seg[i].valid = rec[i * ASV_POST_WORDS + POST_VALID];
+    }
+    return ASV_OK;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+void asv_config_default(asv_config *cfg)
+{
+    if (!cfg) return;
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->variant = ASV_VARIANT_PLAIN;
+    cfg->lloyd_iters = 20;
+    cfg->density_adjust = 1;
+    cfg->use_graph = 1;
+}
+
+int asv_version(void) { return 100; }
+
+const char *asv_status_string(asv_status st)
+{
+    switch (st) {
+    case ASV_OK: return "ok";
+    case ASV_ERR_BAD_ARG: return "bad argument";
+    case ASV_ERR_OOM: return "out of device memory";
+    case ASV_ERR_OVER_BUDGET: return "over HBM budget";
+    case ASV_ERR_TIMEOUT: return "device wait timed out";
+    case ASV_ERR_CUDA: return "CUDA error";
+    case ASV_ERR_STATE: return "call out of order";
+    case ASV_ERR_NO_DEVICE: return "no CUDA device";
+    default: return "unknown status";
+    }
+}
+
+asv_status asv_create(const asv_config *cfg, asv_ctx **out)
+{
+    if (!out) return ASV_ERR_BAD_ARG;
+    *out = nullptr;
+    asv_config c;
+    if (cfg) c = *cfg; else asv_config_default(&c);
+    if (c.lloyd_iters < 1 || c.lloyd_iters > 1000) return ASV_ERR_BAD_ARG;
+    if (c.variant != ASV_VARIANT_PLAIN && c.variant != ASV_VARIANT_STREAM) return ASV_ERR_BAD_ARG;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) { cudaGetLastError(); return ASV_ERR_NO_DEVICE; }
+    if (c.device < 0 || c.device >= n) return ASV_ERR_BAD_ARG;
+    if (cudaSetDevice(c.device) != cudaSuccess) return ASV_ERR_CUDA;
+    asv_ctx *ctx = new asv_ctx();
+    ctx->cfg = c;
+    if (c.stream) ctx->st = (cudaStream_t)c.stream;
+    else {
+        if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess) { delete ctx; return ASV_ERR_CUDA; }
+        ctx->own_st = true;
+    }
+    *out = ctx;
+    return ASV_OK;
+}
+
+asv_status asv_destroy(asv_ctx *ctx)
+{
+    if (!ctx) return ASV_OK;
+    cudaSetDevice(ctx->cfg.device);
+    cudaStreamSynchronize(ctx->st);
+    free_layout(ctx);
+    for (auto e : ctx->ev) cudaEventDestroy(e);
+    if (ctx->own_st) cudaStreamDestroy(ctx->st);
+    delete ctx;
+    return ASV_OK;
+}
+
+const char *asv_last_error(const asv_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+size_t asv_clip_bytes(int W, int H, int D, int K)
+{
+    asv_config c;
+    asv_config_default(&c);
+    asv_ctx tmp;
+    tmp.cfg = c;
+    SegHost h;
+    if (asv_prepare_segment(&tmp, W, H, D, K, &h) != ASV_OK) return 0;
+    std::vector<SegHost> v(1, h);
+    return asv_layout_bytes(v);
+}
+
+asv_status asv_init_gpu(asv_ctx *ctx, const uint8_t *rgb, int W, int H, int D, int K)
+{
+    if (!ctx) return ASV_ERR_BAD_ARG;
+    if (!rgb) return fail(ctx, ASV_ERR_BAD_ARG, "rgb is NULL");
+    cudaSetDevice(ctx->cfg.device);
+    SegHost h;
+    asv_status s = asv_prepare_segment(ctx, W, H, D, K, &h);
+    if (s != ASV_OK) return s;
+    std::vector<SegHost> v(1, h);
+    if (ctx->cfg.hbm_budget && asv_layout_bytes(v) > ctx->cfg.hbm_budget)
+        return fail(ctx, ASV_ERR_OVER_BUDGET, "clip exceeds the configured HBM budget");
+    ctx->seg = v;
+    s = asv_build_layout(ctx);
+    if (s != ASV_OK) return s;
+    CK(cudaMemcpyAsync(ctx->d.rgb, rgb, (size_t)W * H * D * 3, cudaMemcpyHostToDevice, ctx->st));
+    ctx->have_rgb = true;
+    return ASV_OK;
+}
+
+asv_status asv_upload_flow(asv_ctx *ctx, const float *fwd, const float *bwd)
+{
+    if (!ctx) return ASV_ERR_BAD_ARG;
+    if (ctx->seg.size() != 1) return fail(ctx, ASV_ERR_STATE, "no clip: call asv_init_gpu first");
+    if (!fwd || !bwd) return fail(ctx, ASV_ERR_BAD_ARG, "flow pointer is NULL");
+    size_t n = (size_t)ctx->seg[0].W * ctx->seg[0].H * ctx->seg[0].D;
+    CK(cudaMemcpyAsync(ctx->d.fwd, fwd, n * 8, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ctx->d.bwd, bwd, n * 8, cudaMemcpyHostToDevice, ctx->st));
+    ctx->have_flow = true;
+    return ASV_OK;
+}
+
+asv_status asv_initialization(asv_ctx *ctx)
+{
+    if (!ctx) return ASV_ERR_BAD_ARG;
+    if (!ctx->have_rgb) return fail(ctx, ASV_ERR_STATE, "no clip: call asv_init_gpu first");
+    AsvDev &d = ctx->d;
+    if (ctx->cfg.density_adjust) {
+        CK(cudaMemsetAsync(d.dacc, 0, sizeof(unsigned long long) * d.total_seeds, ctx->st));
+        asv_launch_density(d, ctx->st);
+        asv_launch_density_adjust(d, ctx->st);
+        CK(cudaGetLastError());
+        asv_status s = read_post(ctx);
+        if (s != ASV_OK) return s;
+        for (auto &h : ctx->seg)
+            if (h.valid != h.Kp) return fail(ctx, ASV_ERR_CUDA, "density placement produced fewer seeds than the grid");
+    } else {
+        CK(cudaMemcpyAsync(d.pos0, d.grid, sizeof(float4) * d.total_seeds, cudaMemcpyDeviceToDevice, ctx->st));
+    }
+    ctx->have_pos0 = true;
+    ctx->have_M0 = false;
+    return ASV_OK;
+}
+
+asv_status asv_seed_matrix(asv_ctx *ctx)
+{
+    if (!ctx) return ASV_ERR_BAD_ARG;
+    if (!ctx->have_pos0) return fail(ctx, ASV_ERR_STATE, "no seeds: call asv_initialization first");
+    if (!ctx->have_flow) return fail(ctx, ASV_ERR_STATE, "no flow: call asv_upload_flow first");
+    asv_launch_metric(ctx->d, 0, ctx->st);
+    CK(cudaGetLastError());
+    ctx->have_M0 = true;
+    return ASV_OK;
+}
+
+asv_status asv_rgb2lab(asv_ctx *ctx)
+{
+    if (!ctx) return ASV_ERR_BAD_ARG;
+    if (!ctx->have_rgb) return fail(ctx, ASV_ERR_STATE, "no clip: call asv_init_gpu first");
+    asv_launch_rgb2lab(ctx->d, ctx->st);
+    CK(cudaGetLastError());
+    ctx->have_lab = true;
+    return ASV_OK;
+}
+
+asv_status asv_ld_first_init(asv_ctx *ctx)
+{
+    if (!ctx) return ASV_ERR_BAD_ARG;
+    asv_status s = check_ready(ctx);
+    if (s != ASV_OK) return s;
+    do_first_init(ctx);
+    CK(cudaGetLastError());
+    ctx->seeded = true;
+    return ASV_OK;
+}
+
+asv_status asv_flood(asv_ctx *ctx, int lloyd_iter)
+{
+    if (!ctx) return ASV_ERR_BAD_ARG;
+    (void)lloyd_iter;
+    if (!ctx->seeded) return fail(ctx, ASV_ERR_STATE, "no seeds drawn: call asv_ld_first_init first");
+    do_flood(ctx, -1);
+    CK(cudaGetLastError());
+    return ASV_OK;
+}
+
+asv_status asv_centroids_next_seeds(asv_ctx *ctx, int lloyd_iter)
+{
+    if (!ctx) return ASV_ERR_BAD_ARG;
+    if (!ctx->seeded) return fail(ctx, ASV_ERR_STATE, "no seeds drawn: call asv_ld_first_init first");
+    do_centroids(ctx, lloyd_iter != ctx->cfg.lloyd_iters);
+    CK(cudaGetLastError());
+    return ASV_OK;
+}
+
+asv_status asv_ld_next_seeds_matrix(asv_ctx *ctx, int lloyd_iter)
+{
+    if (!ctx) return ASV_ERR_BAD_ARG;
+    (void)lloyd_iter;
+    if (!ctx->seeded) return fail(ctx, ASV_ERR_STATE, "no seeds drawn: call asv_ld_first_init first");
+    do_next_seeds(ctx);
+    CK(cudaGetLastError());
+    return ASV_OK;
+}
+
+asv_status asv_check_dead_seeds(asv_ctx *ctx, int32_t *labels_out)
+{
+    if (!ctx) return ASV_ERR_BAD_ARG;
+    if (!ctx->seeded) return fail(ctx, ASV_ERR_STATE, "no labels: run the Lloyd loop first");
+    do_post(ctx);
+    CK(cudaGetLastError());
+    ctx->ran = true;
+    asv_status s = read_post(ctx);
+    if (s != ASV_OK) return s;
+    if (labels_out) return asv_get_labels(ctx, labels_out);
+    return ASV_OK;
+}
+
+asv_status asv_run_lloyd(asv_ctx *ctx)
+{
+    if (!ctx) return ASV_ERR_BAD_ARG;
+    asv_status s = check_ready(ctx);
+    if (s != ASV_OK) return s;
+    cudaSetDevice(ctx->cfg.device);
+    ctx->launches = 0;
+    if (ctx->cfg.instrument) {
+        s = ensure_events(ctx, (size_t)2 * ctx->maxpass * ctx->cfg.lloyd_iters + 2);
+        if (s != ASV_OK) return s;
+        size_t tot = (size_t)2 * ctx->maxpass * ctx->cfg.lloyd_iters;
+        CK(cudaEventRecord(ctx->ev[tot], ctx->st));
+        enqueue_lloyd(ctx, true);
+        CK(cudaEventRecord(ctx->ev[tot + 1], ctx->st));
+        CK(cudaGetLastError());
+        CK(cudaEventSynchronize(ctx->ev[tot + 1]));
+        double jfa = 0.0;
+        for (size_t k = 0; k < tot; k += 2) {
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, ctx->ev[k], ctx->ev[k + 1]));
+            jfa += ms;
+        }
+        float all = 0.f;
+        CK(cudaEventElapsedTime(&all, ctx->ev[tot], ctx->ev[tot + 1]));
+        ctx->stats.jfa_ms = jfa;
+        ctx->stats.jfa_launches = (int)(tot / 2);
+        ctx->stats.total_ms = all;
+        ctx->stats.launches = ctx->launches;
+    } else if (ctx->cfg.use_graph) {
+        if (!ctx->gexec) {
+            cudaGraph_t g;
+            CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
+            enqueue_lloyd(ctx, false);
+            cudaError_t e = cudaStreamEndCapture(ctx->st, &g);
+            if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaStreamEndCapture");
+            e = cudaGraphInstantiate(&ctx->gexec, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) { ctx->gexec = nullptr; return cuda_fail(ctx, e, "cudaGraphInstantiate"); }
+            ctx->stats.launches = ctx->launches;
+        }
+        CK(cudaGraphLaunch(ctx->gexec, ctx->st));
+    } else {
+        enqueue_lloyd(ctx, false);
+        CK(cudaGetLastError());
+        ctx->stats.launches = ctx->launches;
+    }
+    ctx->seeded = true;
+    ctx->ran = true;
+    return ASV_OK;
+}
+
+asv_status asv_segment_clip(asv_ctx *ctx, const uint8_t *rgb, const float *fwd, const float *bwd,
+                            int W, int H, int D, int K, int32_t *labels_out)
+{
+    asv_status s;
+    if ((s = asv_init_gpu(ctx, rgb, W, H, D, K)) != ASV_OK) return s;
+    if ((s = asv_upload_flow(ctx, fwd, bwd)) != ASV_OK) return s;
+    if ((s = asv_initialization(ctx)) != ASV_OK) return s;
+    if ((s = asv_seed_matrix(ctx)) != ASV_OK) return s;
+    if ((s = asv_rgb2lab(ctx)) != ASV_OK) return s;
+    if ((s = asv_run_lloyd(ctx)) != ASV_OK) return s;
+    if (labels_out) return asv_get_labels(ctx, labels_out);
+    return asv_synchronize(ctx);
+}
+
+asv_status asv_get_info(asv_ctx *ctx, asv_info *info)
+{
+    if (!ctx || !info) return ASV_ERR_BAD_ARG;
+    if (ctx->seg.empty()) return fail(ctx, ASV_ERR_STATE, "no clip");
+    std::memset(info, 0, sizeof(*info));
+    const SegHost &h = ctx->seg[0];
+    if (ctx->ran) { asv_status s = read_post(ctx); if (s != ASV_OK) return s; }
+    info->W = h.W; info->H = h.H; info->D = h.D; info->K = h.K; info->Kp = h.Kp; info->s = h.g.s;
+    info->ratio = h.ratio; info->passes = h.npass;
+    for (int p = 0; p < h.npass && p < 32; p++) info->steps[p] = h.steps[p];
+    info->dead = h.dead; info->neg_count = h.neg; info->final_label_num = h.valid;
+    return ASV_OK;
+}
+
+static asv_status copy_labels(asv_ctx *ctx, int32_t *out, bool raw)
+{
+    if (!ctx || !out) return ASV_ERR_BAD_ARG;
+    if (!ctx->ran) return fail(ctx, ASV_ERR_STATE, "no labels: run the Lloyd loop first");
+    const SegDesc &s = ctx->sd[0];
+    const int32_t *src = ((s.final_buf == 1) == raw ? ctx->d.labB : ctx->d.labA) + s.vox_off;
+    CK(cudaMemcpyAsync(out, src, sizeof(int32_t) * (size_t)s.nvox, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return ASV_OK;
+}
+
+asv_status asv_get_labels(asv_ctx *ctx, int32_t *out) { return copy_labels(ctx, out, false); }
+asv_status asv_get_raw_labels(asv_ctx *ctx, int32_t *out) { return copy_labels(ctx, out, true); }
+
+asv_status asv_get_seeds(asv_ctx *ctx, float *out)
+{
+    if (!ctx || !out) return ASV_ERR_BAD_ARG;
+    if (ctx->seg.empty()) return fail(ctx, ASV_ERR_STATE, "no clip");
+    int Kp = ctx->seg[0].Kp, off = ctx->seg[0].seed_off;
+    std::vector<float4> p(Kp), c(Kp);
+    std::vector<float> m((size_t)Kp * 8);
+    bool work = ctx->seeded;
+    CK(cudaMemcpyAsync(p.data(), (work ? ctx->d.pos : ctx->d.pos0) + off, sizeof(float4) * Kp, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(c.data(), ctx->d.slab + off, sizeof(float4) * Kp, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(m.data(), (work ? ctx->d.M : ctx->d.M0) + 8 * (size_t)off, sizeof(float) * 8 * Kp, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    for (int i = 0; i < Kp; i++) {
+        float *o = out + 12 * (size_t)i;
+        o[0] = p[i].x; o[1] = p[i].y; o[2] = p[i].z;
+        o[3] = c[i].x; o[4] = c[i].y; o[5] = c[i].z;
+        for (int e = 0; e < 6; e++) o[6 + e] = m[8 * (size_t)i + e];
+    }
+    return ASV_OK;
+}
+
+asv_status asv_set_seeds(asv_ctx *ctx, const float *in, int Kp)
+{
+    if (!ctx || !in) return ASV_ERR_BAD_ARG;
+    if (ctx->seg.size() != 1) return fail(ctx, ASV_ERR_STATE, "no clip");
+    if (Kp != ctx->seg[0].Kp) return fail(ctx, ASV_ERR_BAD_ARG, "seed count differs from the clip's");
+    int off = ctx->seg[0].seed_off;
+    std::vector<float4> p(Kp), c(Kp);
+    std::vector<float> m((size_t)Kp * 8, 0.f);
+    for (int i = 0; i < Kp; i++) {
+        const float *o = in + 12 * (size_t)i;
+        p[i] = make_float4(o[0], o[1], o[2], (float)i);
+        c[i] = make_float4(o[3], o[4], o[5], 0.f);
+        for (int e = 0; e < 6; e++) m[8 * (size_t)i + e] = o[6 + e];
+    }
+    CK(cudaMemcpyAsync(ctx->d.pos + off, p.data(), sizeof(float4) * Kp, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ctx->d.slab + off, c.data(), sizeof(float4) * Kp, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ctx->d.M + 8 * (size_t)off, m.data(), sizeof(float) * 8 * Kp, cudaMemcpyHostToDevice, ctx->st));
+    asv_launch_draw(ctx->d, ctx->st);   // packs the JFA table (the label write is ignored here)
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->seeded = true;
+    return ASV_OK;
+}
+
+asv_status asv_get_lab(asv_ctx *ctx, uint8_t *out)
+{
+    if (!ctx || !out) return ASV_ERR_BAD_ARG;
+    if (!ctx->have_lab) return fail(ctx, ASV_ERR_STATE, "no LAB volume: call asv_rgb2lab first");
+    const SegDesc &s = ctx->sd[0];
+    CK(cudaMemcpyAsync(out, ctx->d.lab + s.vox_off, 4 * (size_t)s.nvox, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return ASV_OK;
+}
+
+asv_status asv_get_sums(asv_ctx *ctx, int64_t *out)
+{
+    if (!ctx || !out) return ASV_ERR_BAD_ARG;
+    if (ctx->seg.empty()) return fail(ctx, ASV_ERR_STATE, "no clip");
+    int Kp = ctx->seg[0].Kp, off = ctx->seg[0].seed_off;
+    std::vector<unsigned long long> s((size_t)(Kp + 1) * 8);
+    CK(cudaMemcpyAsync(s.data(), ctx->d.sums + 8 * (size_t)off, sizeof(unsigned long long) * s.size(), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    for (int i = 0; i <= Kp; i++)
+        for (int k = 0; k < 7; k++) out[7 * (size_t)i + k] = (int64_t)s[8 * (size_t)i + k];
+    return ASV_OK;
+}
+
+asv_status asv_check_dead_seeds_host(asv_ctx *ctx, const int32_t *raw_in, int32_t *out)
+{
+    if (!ctx || !raw_in || !out) return ASV_ERR_BAD_ARG;
+    if (ctx->seg.size() != 1 || !ctx->have_lab)
+        return fail(ctx, ASV_ERR_STATE, "need a clip and its LAB volume");
+    const SegDesc &s = ctx->sd[0];
+    int32_t *fin = (s.final_buf ? ctx->d.labB : ctx->d.labA) + s.vox_off;
+    CK(cudaMemcpyAsync(fin, raw_in, 4 * (size_t)s.nvox, cudaMemcpyHostToDevice, ctx->st));
+    do_centroids(ctx, false);
+    do_post(ctx);
+    CK(cudaGetLastError());
+    ctx->ran = true;
+    asv_status st = read_post(ctx);
+    if (st != ASV_OK) return st;
+    return asv_get_labels(ctx, out);
+}
+
+asv_status asv_jfa_pass_host(asv_ctx *ctx, int step, float ratio, const int32_t *in, int32_t *out)
+{
+    if (!ctx || !in || !out || step < 1) return ASV_ERR_BAD_ARG;
+    if (ctx->seg.size() != 1 || !ctx->have_lab || !ctx->seeded)
+        return fail(ctx, ASV_ERR_STATE, "need a clip, its LAB volume and a seed table");
+    const SegDesc &s = ctx->sd[0];
+    size_t n = (size_t)s.nvox;
+    int32_t *din = ctx->d.labA + s.vox_off, *dout = ctx->d.labB + s.vox_off;
+    CK(cudaMemcpyAsync(din, in, 4 * n, cudaMemcpyHostToDevice, ctx->st));
+    asv_launch_jfa_single(ctx->d, din, dout, step, ratio, ctx->st);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, dout, 4 * n, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return ASV_OK;
+}
+
+asv_status asv_get_stats(asv_ctx *ctx, asv_stats *st)
+{
+    if (!ctx || !st) return ASV_ERR_BAD_ARG;
+    *st = ctx->stats;
+    return ASV_OK;
+}
+
+asv_status asv_get_stream(asv_ctx *ctx, void **stream)
+{
+    if (!ctx || !stream) return ASV_ERR_BAD_ARG;
+    *stream = (void *)ctx->st;
+    return ASV_OK;
+}
+
+asv_status asv_synchronize(asv_ctx *ctx)
+{
+    if (!ctx) return ASV_ERR_BAD_ARG;
+    CK(cudaStreamSynchronize(ctx->st));
+    CK(cudaGetLastError());
+    return ASV_OK;
+}
+
+} // extern "C"

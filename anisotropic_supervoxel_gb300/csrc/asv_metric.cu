@@ -1,0 +1,297 @@
+// asv_metric.cu -- per-seed anisotropic metric tensor from the flow field.
+//
+// Replaces the reference's CPU solve (GPU-AS/Image.cpp:689-1009 seed_matrix /
+// matrix_slover, :1300-1534 Ld_next_seeds_matrix) and its GPU->CPU->GPU
+// round trip every Lloyd iteration.  For each seed, the 3x3 neighbourhood of
+// its voxel gives up to 18 rows d^T M d = b (forward rows d = (dx, dy, 1),
+// backward rows d = (dx, dy, -1), b = n^2 + m^2 + 1); M is the min-norm
+// least-squares solution (FP64 one-sided Jacobi SVD, rank rule of Eigen's
+// SVD solve: keep sigma >= max(sigma_max * min(rows,6) * FLT_EPSILON,
+// FLT_MIN)).  A non-PSD M falls back to the mean of the PSD metrics of the
+// 1-ring, then 2-ring neighbours, then to the nearest PSD matrix.
+//
+// Three launches per solve: k_metric_self (one thread per seed),
+// k_metric_ring (one thread per seed and neighbour, only for non-PSD seeds),
+// k_metric_combine (one thread per seed).  Compiled with -fmad=false.
+#include "asv_common.cuh"
+
+#include <float.h>
+
+#define SVD_SWEEPS 40
+
+__device__ void asv_lsq_minnorm(int m, double (*U)[6], const double *b, double x[6])
+{
+    double V[6][6];
+    for (int r = 0; r < 6; r++)
+        for (int c = 0; c < 6; c++) V[r][c] = r == c ? 1.0 : 0.0;
+    for (int sw = 0; sw < SVD_SWEEPS; sw++) {
+        int rot = 0;
+        for (int p = 0; p < 5; p++)
+            for (int q = p + 1; q < 6; q++) {
+                double al = 0.0, be = 0.0, ga = 0.0;
+                for (int i = 0; i < m; i++) {
+                    al = al + U[i][p] * U[i][p];
+                    be = be + U[i][q] * U[i][q];
+                    ga = ga + U[i][p] * U[i][q];
+                }
+                if (ga == 0.0) continue;
+                if (fabs(ga) <= 1e-15 * sqrt(al * be)) continue;
+                double zeta = (be - al) / (2.0 * ga);
+                double t = 1.0 / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+                if (zeta < 0.0) t = -t;
+                double c = 1.0 / sqrt(1.0 + t * t);
+                double s = c * t;
+                for (int i = 0; i < m; i++) {
+                    double up = U[i][p], uq = U[i][q];
+                    U[i][p] = c * up - s * uq;
+                    U[i][q] = s * up + c * uq;
+                }
+                for (int i = 0; i < 6; i++) {
+                    double vp = V[i][p], vq = V[i][q];
+                    V[i][p] = c * vp - s * vq;
+                    V[i][q] = s * vp + c * vq;
+                }
+                rot++;
+            }
+        if (!rot) break;
+    }
+    double sig[6], smax = 0.0;
+    for (int j = 0; j < 6; j++) {
+        double a = 0.0;
+        for (int i = 0; i < m; i++) a = a + U[i][j] * U[i][j];
+        sig[j] = sqrt(a);
+        if (sig[j] > smax) smax = sig[j];
+    }
+    double thr = smax * ((double)(m < 6 ? m : 6) * (double)FLT_EPSILON);
+    if (thr < (double)FLT_MIN) thr = (double)FLT_MIN;
+    for (int r = 0; r < 6; r++) x[r] = 0.0;
+    for (int j = 0; j < 6; j++) {
+        if (!(sig[j] >= thr)) continue;
+        double ub = 0.0;
+        for (int i = 0; i < m; i++) ub = ub + U[i][j] * b[i];
+        double coef = ub / (sig[j] * sig[j]);
+        for (int r = 0; r < 6; r++) x[r] = x[r] + V[r][j] * coef;
+    }
+}
+
+// symmetric 3x3 eigen-decomposition, cyclic Jacobi
+__device__ void asv_sym3_eig(const float M[6], double w[3], double V[3][3])
+{
+    double a[3][3] = { { M[0], M[1], M[2] }, { M[1], M[3], M[4] }, { M[2], M[4], M[5] } };
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) V[r][c] = r == c ? 1.0 : 0.0;
+    const int P[3] = { 0, 0, 1 }, Q[3] = { 1, 2, 2 };
+    for (int sw = 0; sw < 50; sw++) {
+        int rot = 0;
+        for (int k = 0; k < 3; k++) {
+            int p = P[k], q = Q[k];
+            double apq = a[p][q];
+            if (apq == 0.0) continue;
+            if (fabs(apq) <= 1e-18 * (fabs(a[p][p]) + fabs(a[q][q]))) continue;
+            double th = (a[q][q] - a[p][p]) / (2.0 * apq);
+            double t = 1.0 / (fabs(th) + sqrt(th * th + 1.0));
+            if (th < 0.0) t = -t;
+            double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+            for (int r = 0; r < 3; r++) {
+                double ap = a[r][p], aq = a[r][q];
+                a[r][p] = c * ap - s * aq;
+                a[r][q] = s * ap + c * aq;
+            }
+            for (int r = 0; r < 3; r++) {
+                double ap = a[p][r], aq = a[q][r];
+                a[p][r] = c * ap - s * aq;
+                a[q][r] = s * ap + c * aq;
+            }
+            for (int r = 0; r < 3; r++) {
+                double vp = V[r][p], vq = V[r][q];
+                V[r][p] = c * vp - s * vq;
+                V[r][q] = s * vp + c * vq;
+            }
+            rot++;
+        }
+        if (!rot) break;
+    }
+    for (int k = 0; k < 3; k++) w[k] = a[k][k];
+}
+
+__device__ int asv_m6_negative(const float M[6])
+{
+    double w[3], V[3][3];
+    asv_sym3_eig(M, w, V);
+    return (w[0] < 0.0 || w[1] < 0.0 || w[2] < 0.0) ? 1 : 0;
+}
+
+__device__ void asv_m6_nearest_psd(const float M[6], float out[6])
+{
+    double w[3], V[3][3];
+    asv_sym3_eig(M, w, V);
+    for (int k = 0; k < 3; k++) if (w[k] < 0.0) w[k] = 0.0;
+    const int R[6] = { 0, 0, 0, 1, 1, 2 }, C[6] = { 0, 1, 2, 1, 2, 2 };
+    for (int e = 0; e < 6; e++) {
+        int i = R[e], j = C[e];
+        double acc = (V[i][0] * w[0]) * V[j][0];
+        acc = acc + (V[i][1] * w[1]) * V[j][1];
+        acc = acc + (V[i][2] * w[2]) * V[j][2];
+        out[e] = (float)acc;
+    }
+}
+
+__device__ __forceinline__ float asv_round_half_up(float f) { return (float)floor((double)f + 0.5); }
+
+// matrix_slover (GPU-AS/Image.cpp:874-1009); returns the non-PSD flag
+__device__ int asv_metric_solve(const float2 *__restrict__ fwd, const float2 *__restrict__ bwd, int W,
+                                int H, int D, float sx, float sy, int frame, float M[6])
+{
+    const float expected_b[9] = { 3, 2, 3, 2, 1, 2, 3, 2, 3 };
+    double A[18][6], b[18];
+    int m = 0, id_b = 0;
+    for (int oy = -1; oy < 2; oy++)
+        for (int ox = -1; ox < 2; ox++, id_b++) {
+            int nx = (int)sx + ox, ny = (int)sy + oy;
+            if (!(nx >= 0 && nx < W && ny >= 0 && ny < H)) continue;
+            long long o = ((long long)frame * H + ny) * W + nx;
+            if (frame != D - 1) {
+                float2 f = __ldg(fwd + o);
+                float dx = (float)ox + asv_round_half_up(f.x);
+                float dy = (float)oy + asv_round_half_up(f.y);
+                A[m][0] = (double)(dx * dx); A[m][1] = (double)(2.0f * dx * dy);
+                A[m][2] = (double)(2.0f * dx); A[m][3] = (double)(dy * dy);
+                A[m][4] = (double)(2.0f * dy); A[m][5] = 1.0;
+                b[m++] = expected_b[id_b];
+            }
+            if (frame != 0) {
+                float2 f = __ldg(bwd + o);
+                float dx = asv_round_half_up(f.x) + (float)ox;
+                float dy = asv_round_half_up(f.y) + (float)oy;
+                A[m][0] = (double)(dx * dx); A[m][1] = (double)(2.0f * dx * dy);
+                A[m][2] = (double)(-2.0f * dx); A[m][3] = (double)(dy * dy);
+                A[m][4] = (double)(-2.0f * dy); A[m][5] = 1.0;
+                b[m++] = expected_b[id_b];
+            }
+        }
+    double x[6];
+    if (m == 0) { for (int k = 0; k < 6; k++) x[k] = 0.0; }
+    else asv_lsq_minnorm(m, A, b, x);
+    for (int k = 0; k < 6; k++) M[k] = (float)x[k];
+    return asv_m6_negative(M);
+}
+
+// plain reseed flow-angle filter (GPU-AS/Image.cpp:1406-1409): accept iff
+// the float cosine c satisfies T <= c <= 1, T the smallest float with
+// float(double(acosf(T)) * (180 / 3.141592653)) < 90 (bits 0x328885a3).
+// The last frame's flow is the reference's 4x4 zero Mat: read as zero.
+__device__ int asv_angle_ok(const float2 *__restrict__ fwd, int W, int H, int D, int frame, int sx,
+                            int sy, int nx, int ny)
+{
+    float sfx = 0.0f, sfy = 0.0f, nfx = 0.0f, nfy = 0.0f;
+    if (frame != D - 1) {
+        float2 a = __ldg(fwd + ((long long)frame * H + sy) * W + sx);
+        float2 c = __ldg(fwd + ((long long)frame * H + ny) * W + nx);
+        sfx = a.x; sfy = a.y; nfx = c.x; nfy = c.y;
+    }
+    float num = sfx * nfx + sfy * nfy;
+    double den = sqrt((double)sfx * (double)sfx + (double)sfy * (double)sfy) *
+                 sqrt((double)nfx * (double)nfx + (double)nfy * (double)nfy);
+    float c = (float)((double)num / den);
+    return (c >= 1.5893254712295857e-08f && c <= 1.0f) ? 1 : 0;
+}
+
+__constant__ int c_ringx[ASV_RING] = { -1, 0, 1, -1, 1, -1, 0, 1,
+                                       -2, -1, 0, 1, 2, -2, 2, -2, 2, -2, 2, -2, -1, 0, 1, 2 };
+__constant__ int c_ringy[ASV_RING] = { -1, -1, -1, 0, 0, 1, 1, 1,
+                                       -2, -2, -2, -2, -2, -1, -1, 0, 0, 1, 1, 2, 2, 2, 2, 2 };
+
+struct SeedRef { int si, i, g; };
+
+__device__ __forceinline__ bool asv_seed_ref(const AsvDev &d, int g, SeedRef &r)
+{
+    if (g >= d.total_seeds) return false;
+    r.g = g;
+    r.si = asv_find_seg(d.seed_prefix, d.nseg, g);
+    r.i = g - d.seed_prefix[r.si];
+    return r.i < d.segs[r.si].Kp;
+}
+
+// which seed positions: reseed 0 -> pos0 (seed_matrix), 1 -> pos (reseed)
+__global__ void k_metric_self(AsvDev d, int reseed)
+{
+    SeedRef r;
+    if (!asv_seed_ref(d, blockIdx.x * blockDim.x + threadIdx.x, r)) return;
+    const SegDesc &S = d.segs[r.si];
+    float4 p = reseed ? d.pos[r.g] : d.pos0[r.g];
+    float fx = floorf(p.x), fy = floorf(p.y);
+    int frame = (int)p.z;
+    float M[6];
+    int neg = asv_metric_solve(d.fwd + S.vox_off, d.bwd + S.vox_off, S.W, S.H, S.D, fx, fy, frame, M);
+    for (int e = 0; e < 6; e++) d.Mself[8 * r.g + e] = M[e];
+    d.neg[r.g] = neg;
+}
+
+__global__ void k_metric_ring(AsvDev d, int reseed)
+{
+    int gid = blockIdx.x * blockDim.x + threadIdx.x;
+    int g = gid / ASV_RING, t = gid - g * ASV_RING;
+    SeedRef r;
+    if (!asv_seed_ref(d, g, r)) return;
+    int *ok = d.ringok + ASV_RING * g + t;
+    if (!d.neg[g]) { *ok = 0; return; }
+    const SegDesc &S = d.segs[r.si];
+    float4 p = reseed ? d.pos[g] : d.pos0[g];
+    float fx = floorf(p.x), fy = floorf(p.y);
+    int frame = (int)p.z;
+    float nx = fx + (float)c_ringx[t], ny = fy + (float)c_ringy[t];
+    if (!(nx >= 0 && nx < S.W && ny >= 0 && ny < S.H)) { *ok = 0; return; }
+    const float2 *fwd = d.fwd + S.vox_off, *bwd = d.bwd + S.vox_off;
+    if (reseed && S.angle_filter &&
+        !asv_angle_ok(fwd, S.W, S.H, S.D, frame, (int)fx, (int)fy, (int)nx, (int)ny)) {
+        *ok = 0;
+        return;
+    }
+    float M[6];
+    int neg = asv_metric_solve(fwd, bwd, S.W, S.H, S.D, nx, ny, frame, M);
+    float *dst = d.Mring + 8 * (ASV_RING * g + t);
+    for (int e = 0; e < 6; e++) dst[e] = M[e];
+    *ok = neg ? 0 : 1;
+}
+
+// writes M0 (reseed 0) or M (reseed 1)
+__global__ void k_metric_combine(AsvDev d, int reseed)
+{
+    SeedRef r;
+    if (!asv_seed_ref(d, blockIdx.x * blockDim.x + threadIdx.x, r)) return;
+    const int g = r.g;
+    float *out = (reseed ? d.M : d.M0) + 8 * g;
+    float self[6];
+    for (int e = 0; e < 6; e++) self[e] = d.Mself[8 * g + e];
+    if (!d.neg[g]) {
+        for (int e = 0; e < 6; e++) out[e] = self[e];
+        return;
+    }
+    for (int ring = 0; ring < 2; ring++) {
+        int t0 = ring == 0 ? 0 : 8, t1 = ring == 0 ? 8 : ASV_RING;
+        float sum[6] = { 0, 0, 0, 0, 0, 0 };
+        int n = 0;
+        for (int t = t0; t < t1; t++) {
+            if (!d.ringok[ASV_RING * g + t]) continue;
+            const float *m = d.Mring + 8 * (ASV_RING * g + t);
+            n++;
+            for (int e = 0; e < 6; e++) sum[e] = sum[e] + m[e];
+        }
+        if (n > 0) {
+            for (int e = 0; e < 6; e++) out[e] = sum[e] / (float)n;
+            return;
+        }
+    }
+    float o[6];
+    asv_m6_nearest_psd(self, o);
+    for (int e = 0; e < 6; e++) out[e] = o[e];
+}
+
+void asv_launch_metric(const AsvDev &d, int reseed, cudaStream_t st)
+{
+    int nb = (d.total_seeds + 63) / 64;
+    k_metric_self<<<nb, 64, 0, st>>>(d, reseed);
+    long long nr = (long long)d.total_seeds * ASV_RING;
+    k_metric_ring<<<(int)((nr + 63) / 64), 64, 0, st>>>(d, reseed);
+    k_metric_combine<<<nb, 64, 0, st>>>(d, reseed);
+}

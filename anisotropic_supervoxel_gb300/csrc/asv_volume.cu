@@ -1,0 +1,710 @@
+// asv_volume.cu -- per-voxel and per-seed kernels of the supervoxel path.
+//
+// Compiled with -fmad=false: every float operation is one IEEE operation in
+// the order written, so the labels match the CPU restatement bit for bit.
+// Reference files (in dongxiao0401/anisotropic_supervoxel): GPU-AS/shaders/*,
+// GPU-AS/Image.cpp.
+#include "asv_common.cuh"
+
+#include <cuda_fp16.h>
+
+#define FULL 0xffffffffu
+
+// ---------------------------------------------------------------------------
+// RGB -> LAB (GPU-AS/shaders/RGB2LAB.fs:11-79).  Output bytes are the
+// integers the shader writes to its RGB16F target (exact in 8 bits).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float asv_pow_cr(float x, float y)
+{
+    return (float)pow((double)x, (double)y);
+}
+
+__global__ void k_srgb_table(float *__restrict__ tab)
+{
+    int c = threadIdx.x;
+    if (c >= 256) return;
+    float v = (float)c / 255.0f;                      // unorm8 texel
+    float t;
+    if (v <= 0.04045f) t = v / 12.92f;                 // RGB2LAB.fs:27-40
+    else t = asv_pow_cr((v + 0.055f) / 1.055f, 2.4f);
+    tab[c] = t;
+}
+
+__device__ __forceinline__ uchar4 asv_lab_of(const float *__restrict__ tab, unsigned r, unsigned g,
+                                             unsigned b)
+{
+    float t0 = tab[r], t1 = tab[g], t2 = tab[b];
+    float X = (t0 * 0.412453f + t1 * 0.357580f) + t2 * 0.180423f;   // fs:19-21, 42-44
+    float Y = (t0 * 0.212671f + t1 * 0.715160f) + t2 * 0.072169f;
+    float Z = (t0 * 0.019334f + t1 * 0.119193f) + t2 * 0.950227f;
+    float rr[3] = { X / 0.950456f, Y / 1.0f, Z / 1.088754f };        // fs:54-55
+    float f[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        if (rr[k] > 0.008856f) f[k] = asv_pow_cr(rr[k], 1.0f / 3.0f); // fs:57-70
+        else f[k] = (903.3f * rr[k] + 16.0f) / 116.0f;
+    }
+    float L = 116.0f * f[1] - 16.0f;                                  // fs:72
+    float A = 500.0f * (f[0] - f[1]);
+    float B = 200.0f * (f[1] - f[2]);
+    L = L * 2.55f; A = A + 128.0f; B = B + 128.0f;                    // fs:74-76
+    float v0 = floorf(L + 0.5f), v1 = floorf(A + 0.5f), v2 = floorf(B + 0.5f);
+    v0 = fminf(fmaxf(v0, 0.0f), 255.0f);
+    v1 = fminf(fmaxf(v1, 0.0f), 255.0f);
+    v2 = fminf(fmaxf(v2, 0.0f), 255.0f);
+    return make_uchar4((unsigned char)v0, (unsigned char)v1, (unsigned char)v2, 0);
+}
+
+__global__ void __launch_bounds__(256) k_rgb2lab(AsvDev d)
+{
+    __shared__ float tab[256];
+    tab[threadIdx.x] = d.srgb[threadIdx.x];
+    __syncthreads();
+    int si = asv_find_seg(d.chunk_prefix, d.nseg, blockIdx.x);
+    const SegDesc &S = d.segs[si];
+    long long base = (long long)(blockIdx.x - d.chunk_prefix[si]) * ASV_CHUNK;
+    long long n = S.nvox;
+    for (int i = 0; i < ASV_CHUNK / 256; i++) {
+        long long v = base + i * 256 + threadIdx.x;
+        if (v >= n) break;
+        const uint8_t *p = d.rgb + 3 * (S.vox_off + v);
+        d.lab[S.vox_off + v] = asv_lab_of(tab, p[0], p[1], p[2]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Gradient density per grid cell (GPU-AS/Image.cpp:350-620,
+// derivative_t.gs:24-49, density_grid.vs:17-43).  Each voxel's gradient is
+// rounded to half (RGB16F target) and summed exactly, in units of 2^-24.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float asv_gradient(const uint8_t *__restrict__ rgb, int W, int H, int x,
+                                              int y, int z)
+{
+    long long row = (long long)W;
+    long long sl = (long long)W * H;
+    long long v = z * sl + y * row + x;
+    const uint8_t *c = rgb + 3 * v;
+    const uint8_t *nb0 = rgb + 3 * (v - (x > 0 ? 1 : 0));
+    const uint8_t *nb1 = rgb + 3 * (v - (y > 0 ? row : 0));
+    const uint8_t *nb2 = rgb + 3 * (v - (z > 0 ? sl : 0));
+    const uint8_t *nbs[3] = { nb0, nb1, nb2 };
+    float g = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const uint8_t *q = nbs[k];
+        float s = (float)abs((int)q[0] - (int)c[0]);
+        s = s + (float)abs((int)q[1] - (int)c[1]);
+        s = s + (float)abs((int)q[2] - (int)c[2]);
+        g = g + 0.33f * s;                                            // gs:36, 43, 49
+    }
+    return g;
+}
+
+// value of a non-negative half in units of 2^-24
+__device__ __forceinline__ unsigned long long asv_half_units(__half h)
+{
+    unsigned short b = __half_as_ushort(h);
+    unsigned e = (b >> 10) & 0x1fu, m = b & 0x3ffu;
+    if (e == 0) return m;
+    return (unsigned long long)(1024u + m) << (e - 1);
+}
+
+__global__ void __launch_bounds__(256) k_density(AsvDev d)
+{
+    int si = asv_find_seg(d.chunk_prefix, d.nseg, blockIdx.x);
+    const SegDesc &S = d.segs[si];
+    const int W = S.W, H = S.H;
+    const int *xc = d.cells + S.cell_off, *yc = xc + W, *zc = yc + H;
+    const uint8_t *rgb = d.rgb + 3 * S.vox_off;
+    unsigned long long *acc = d.dacc + S.seed_off;
+    const int cap = d.seed_prefix[si + 1] - S.seed_off;
+    long long base = (long long)(blockIdx.x - d.chunk_prefix[si]) * ASV_CHUNK;
+    for (int i = 0; i < ASV_CHUNK / 256; i++) {
+        long long v = base + i * 256 + threadIdx.x;
+        int key = -1;
+        unsigned u32 = 0;
+        if (v < S.nvox) {
+            int x = (int)(v % W);
+            long long r = v / W;
+            int y = (int)(r % H), z = (int)(r / H);
+            int cx = xc[x], cy = yc[y], cz = zc[z];
+            if (cx >= 0 && cy >= 0 && cz >= 0) {
+                int k = (cz * S.hNum + cy) * S.wNum + cx;
+                // cell id stored in an R16F texture (Image.cpp:474)
+                int slot = (int)__half2float(__float2half_rn((float)k));
+                unsigned long long units = asv_half_units(__float2half_rn(asv_gradient(rgb, W, H, x, y, z)));
+                if (slot < cap) {
+                    if ((units & 0xfffull) == 0 && (units >> 12) < (1ull << 26)) {
+                        key = slot;
+                        u32 = (unsigned)(units >> 12);
+                    } else {
+                        atomicAdd(acc + slot, units);
+                    }
+                }
+            }
+        }
+        unsigned grp = __match_any_sync(FULL, key);
+        unsigned sum = __reduce_add_sync(grp, u32);
+        if (key >= 0 && (threadIdx.x & 31) == __ffs(grp) - 1)
+            atomicAdd(acc + key, (unsigned long long)sum << 12);
+    }
+}
+
+// 1-D redistribution of the seeds along the cells (Image.cpp:549-616).  One
+// thread per segment: the prefix sums are sequential float sums in the
+// reference.  `scratch` holds Kp floats per segment.
+__global__ void k_density_adjust(AsvDev d, float *scratch)
+{
+    int si = blockIdx.x;
+    if (threadIdx.x != 0 || si >= d.nseg) return;
+    const SegDesc &S = d.segs[si];
+    const int Kp = S.Kp;
+    const unsigned long long *acc = d.dacc + S.seed_off;
+    const int *xl = d.cells + S.cell_off + S.W + S.H + S.D, *xr = xl + S.wNum;
+    const float4 *grid = d.grid + S.seed_off;
+    float *len = scratch + S.seed_off;
+    for (int i = 0; i < Kp; i++) {
+        unsigned long long tot = acc[i] + (3ull << 24);               // cleared to 3.0 (:506-507)
+        float res = __ull2float_rn(tot) * 0x1p-24f;
+        float dens = (float)(0.001 * (double)res);                    // :554
+        len[i] = i == 0 ? dens : dens + len[i - 1];                   // :558-569
+    }
+    float interval = len[Kp - 1] / (float)(Kp + 1);                   // :570
+    int i = 0, j1 = 0, n = 0;
+    while (i < Kp) {                                                  // :586-616
+        float seed_in = (float)(i + 1) * interval;
+        if (seed_in < len[j1]) {
+            int c = j1 % S.wNum;
+            int x1 = xl[c], x2 = xr[c];
+            float frac = j1 == 0 ? seed_in / len[j1] : (seed_in - len[j1 - 1]) / (len[j1] - len[j1 - 1]);
+            float ax = floorf((float)x1 + (float)(x2 - x1) * frac);
+            float4 g = grid[j1];
+            d.pos0[S.seed_off + n] = make_float4((float)((double)ax + 0.5), g.y, g.z, (float)i);
+            n++; i++;
+        } else {
+            j1++;
+            if (j1 == Kp) break;
+        }
+    }
+    d.post[si * ASV_POST_WORDS + POST_VALID] = n;   // seeds placed (checked by the host)
+}
+
+// ---------------------------------------------------------------------------
+// Seeds: first-iteration init (draw_seeds.vs:20-35) and the per-iteration
+// draw (draw_next_seeds.vs): seed record at the seed voxel, the later seed
+// winning a shared voxel; JFA table packed for the passes.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int asv_seed_seg(const AsvDev &d, int g, int &local)
+{
+    int si = asv_find_seg(d.seed_prefix, d.nseg, g);
+    local = g - d.seed_prefix[si];
+    return si;
+}
+
+__global__ void k_first_init(AsvDev d)
+{
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= d.total_seeds) return;
+    int i;
+    int si = asv_seed_seg(d, g, i);
+    const SegDesc &S = d.segs[si];
+    if (i >= S.Kp) return;
+    float4 p = d.pos0[g];
+    d.pos[g] = p;
+#pragma unroll
+    for (int e = 0; e < 8; e++) d.M[8 * g + e] = d.M0[8 * g + e];
+    int x = min(max((int)floorf(p.x), 0), S.W - 1);
+    int y = min(max((int)floorf(p.y), 0), S.H - 1);
+    int z = min(max((int)floorf(p.z), 0), S.D - 1);
+    uchar4 l = d.lab[S.vox_off + ((long long)z * S.H + y) * S.W + x];
+    d.slab[g] = make_float4((float)l.x, (float)l.y, (float)l.z, 0.0f);
+}
+
+__global__ void k_draw(AsvDev d)
+{
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= d.total_seeds) return;
+    int i;
+    int si = asv_seed_seg(d, g, i);
+    const SegDesc &S = d.segs[si];
+    if (i >= S.Kp) return;
+    float4 p = d.pos[g], c = d.slab[g];
+    const float *m = d.M + 8 * g;
+    // table: (x, y, z, L) (a, b, M00, 2M01) (2M02, M11, 2M12, M22); doubling
+    // is exact, so (dx*dy)*(2*M01) == ((2*dx)*dy)*M01 (flood.gs:85).
+    d.jtab[3 * g + 0] = make_float4(p.x, p.y, p.z, c.x);
+    d.jtab[3 * g + 1] = make_float4(c.y, c.z, m[0], 2.0f * m[1]);
+    d.jtab[3 * g + 2] = make_float4(2.0f * m[2], m[3], 2.0f * m[4], m[5]);
+    if (!(p.x >= 0.0f && p.y >= 0.0f && p.z >= 0.0f)) return;
+    int x = (int)p.x, y = (int)p.y, z = (int)p.z;
+    if (x >= S.W || y >= S.H || z >= S.D) return;
+    atomicMax(d.labA + S.vox_off + ((long long)z * S.H + y) * S.W + x, i);
+}
+
+// ---------------------------------------------------------------------------
+// One JFA pass (GPU-AS/shaders/flood.gs:26-182).  One thread per voxel,
+// 32x8-voxel tiles of one slice, persistent grid-stride over the tiles of
+// all segments (z-major, so the resident tiles share their +-step slices in
+// L2).  27 candidates in the shader's order: slices z, z-step, z+step; rows
+// y-step..y+step; columns x-step..x+step; clamp to edge.  A candidate whose
+// seed id equals the current best or the previously evaluated id is skipped:
+// its distance is identical and the test is strict `<`.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void asv_jfa_voxel(const int32_t *__restrict__ in, int32_t *__restrict__ out,
+                                              const uchar4 *__restrict__ lab,
+                                              const float4 *__restrict__ tab, int W, int H, int D,
+                                              int x, int y, int z, int step, float ratio)
+{
+    const long long sl = (long long)W * H;
+    const float vx = (float)x + 0.5f, vy = (float)y + 0.5f, vz = (float)z + 0.5f;
+    uchar4 c = __ldg(lab + z * sl + (long long)y * W + x);
+    const float cL = (float)c.x, ca = (float)c.y, cb = (float)c.z;
+    const int xs0 = max(x - step, 0), xs2 = min(x + step, W - 1);
+    const int ys0 = max(y - step, 0), ys2 = min(y + step, H - 1);
+    const int zs[3] = { z, max(z - step, 0), min(z + step, D - 1) };
+    const int xs[3] = { xs0, x, xs2 };
+    const int ys[3] = { ys0, y, ys2 };
+    int32_t cand[27];
+#pragma unroll
+    for (int s = 0; s < 3; s++)
+#pragma unroll
+        for (int oy = 0; oy < 3; oy++) {
+            const int32_t *row = in + zs[s] * sl + (long long)ys[oy] * W;
+#pragma unroll
+            for (int ox = 0; ox < 3; ox++) cand[(s * 3 + oy) * 3 + ox] = __ldg(row + xs[ox]);
+        }
+    float mind = 100000000.0f;                                        // flood.gs:63
+    int32_t best = -1, last = -1;
+#pragma unroll
+    for (int k = 0; k < 27; k++) {
+        const int32_t l = cand[k];
+        if (l < 0 || l == best || l == last) continue;
+        last = l;
+        const float4 t0 = __ldg(tab + 3 * l), t1 = __ldg(tab + 3 * l + 1), t2 = __ldg(tab + 3 * l + 2);
+        const float dx = vx - t0.x, dy = vy - t0.y, dz = vz - t0.z;
+        float p1 = (dx * dx) * t1.z + (dx * dy) * t1.w;              // flood.gs:85
+        p1 = p1 + (dx * dz) * t2.x;
+        float p2 = (dy * dy) * t2.y + (dy * dz) * t2.z;
+        p2 = p2 + (dz * dz) * t2.w;
+        float pos = p1 + p2;
+        const float eL = cL - t0.w, ea = ca - t1.x, eb = cb - t1.y;
+        float col = eL * eL + ea * ea;                                 // flood.gs:89
+        col = col + eb * eb;
+        pos = (pos < 0.0f) ? 0.0f : pos;                               // flood.gs:90-93
+        const float dist = ratio * pos + col;                          // flood.gs:94
+        if (dist < mind) { mind = dist; best = l; }                    // flood.gs:95-99
+    }
+    out[z * sl + (long long)y * W + x] = best;
+}
+
+__global__ void __launch_bounds__(256) k_jfa(AsvDev d, int pass, const int32_t *__restrict__ in,
+                                             int32_t *__restrict__ out)
+{
+    const int lx = threadIdx.x & (ASV_TILE_X - 1), ly = threadIdx.x >> 5;
+    for (int t = blockIdx.x; t < d.total_tiles; t += gridDim.x) {
+        const int si = asv_find_seg(d.tile_prefix, d.nseg, t);
+        const SegDesc &S = d.segs[si];
+        if (pass >= S.npass) continue;
+        const int lt = t - d.tile_prefix[si];
+        const int tx = lt % S.tiles_x, rest = lt / S.tiles_x;
+        const int ty = rest % S.tiles_y, z = rest / S.tiles_y;
+        const int x = tx * ASV_TILE_X + lx, y = ty * ASV_TILE_Y + ly;
+        if (x >= S.W || y >= S.H) continue;
+        asv_jfa_voxel(in + S.vox_off, out + S.vox_off, d.lab + S.vox_off, d.jtab + 3 * S.seed_off,
+                      S.W, S.H, S.D, x, y, z, S.steps[pass], S.ratio[pass]);
+    }
+}
+
+// single-segment pass with explicit step and ratio (test entry point)
+__global__ void __launch_bounds__(256) k_jfa_single(AsvDev d, const int32_t *__restrict__ in,
+                                                    int32_t *__restrict__ out, int step, float ratio)
+{
+    const SegDesc &S = d.segs[0];
+    const int lx = threadIdx.x & (ASV_TILE_X - 1), ly = threadIdx.x >> 5;
+    const int ntiles = S.tiles_x * S.tiles_y * S.D;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int tx = t % S.tiles_x, rest = t / S.tiles_x;
+        const int ty = rest % S.tiles_y, z = rest / S.tiles_y;
+        const int x = tx * ASV_TILE_X + lx, y = ty * ASV_TILE_Y + ly;
+        if (x >= S.W || y >= S.H) continue;
+        asv_jfa_voxel(in, out, d.lab + S.vox_off, d.jtab + 3 * S.seed_off, S.W, S.H, S.D, x, y, z,
+                      step, ratio);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Centroid sums (centroids.vs:19-54): per label slot (label -1 -> slot Kp)
+// sum(2x+1), sum(2y+1), sum(2z+1), count, sum L, a, b -- exact integers.
+// Lanes with the same label are reduced in the warp, then one u64 atomic per
+// group and component.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_centroids(AsvDev d)
+{
+    int si = asv_find_seg(d.chunk_prefix, d.nseg, blockIdx.x);
+    const SegDesc &S = d.segs[si];
+    const int W = S.W, H = S.H;
+    const int32_t *lbl = (S.final_buf ? d.labB : d.labA) + S.vox_off;
+    const uchar4 *lab = d.lab + S.vox_off;
+    unsigned long long *sums = d.sums + 8ull * S.seed_off;
+    long long base = (long long)(blockIdx.x - d.chunk_prefix[si]) * ASV_CHUNK;
+    const int lane = threadIdx.x & 31;
+    for (int i = 0; i < ASV_CHUNK / 256; i++) {
+        long long v = base + i * 256 + threadIdx.x;
+        int key = -1;
+        unsigned q[7] = { 0, 0, 0, 0, 0, 0, 0 };
+        if (v < S.nvox) {
+            int l = __ldg(lbl + v);
+            key = l < 0 ? S.Kp : l;
+            int x = (int)(v % W);
+            long long r = v / W;
+            int y = (int)(r % H), z = (int)(r / H);
+            uchar4 c = __ldg(lab + v);
+            q[0] = 2 * x + 1; q[1] = 2 * y + 1; q[2] = 2 * z + 1; q[3] = 1;
+            q[4] = c.x; q[5] = c.y; q[6] = c.z;
+        }
+        unsigned grp = __match_any_sync(FULL, key);
+        unsigned s[7];
+#pragma unroll
+        for (int k = 0; k < 7; k++) s[k] = __reduce_add_sync(grp, q[k]);
+        if (key >= 0 && lane == __ffs(grp) - 1) {
+            unsigned long long *dst = sums + 8ull * key;
+#pragma unroll
+            for (int k = 0; k < 7; k++) atomicAdd(dst + k, (unsigned long long)s[k]);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Reseed (aver_exception.vs:22-81).  Alive seed: position floor(mean)+0.5,
+// colour = mean LAB.  Dead seed: midpoint of the means of slots id-1 and
+// id+1 (id 0 reads texel (W-1, 0); slot Kp is the -1 slot), colour sampled
+// at the new position.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void asv_slot_mean(const unsigned long long *sums, int Kp, int slot,
+                                              float q[3])
+{
+    if (slot < 0 || slot > Kp) { q[0] = q[1] = q[2] = 0.0f; return; }
+    const unsigned long long *s = sums + 8ull * slot;
+    float cnt = __ull2float_rn(s[3]);
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        float sf = __ull2float_rn(s[a]) * 0.5f;
+        q[a] = ((int)cnt != 0) ? sf / cnt : sf;
+    }
+}
+
+__global__ void k_finalize(AsvDev d)
+{
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= d.total_seeds) return;
+    int id;
+    int si = asv_seed_seg(d, g, id);
+    const SegDesc &S = d.segs[si];
+    if (id >= S.Kp) return;
+    const unsigned long long *sums = d.sums + 8ull * S.seed_off;
+    const unsigned long long *s = sums + 8ull * id;
+    float p[3], c[3];
+    if (s[3] != 0) {
+        float cnt = __ull2float_rn(s[3]);
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            float sf = __ull2float_rn(s[a]) * 0.5f;
+            p[a] = floorf(sf / cnt) + 0.5f;
+            c[a] = __ull2float_rn(s[4 + a]) / cnt;
+        }
+    } else {
+        float q1[3], q2[3];
+        asv_slot_mean(sums, S.Kp, id == 0 ? S.W - 1 : id - 1, q1);
+        asv_slot_mean(sums, S.Kp, id + 1, q2);
+#pragma unroll
+        for (int a = 0; a < 3; a++) p[a] = floorf(0.5f * (q1[a] + q2[a])) + 0.5f;
+        int x = min(max((int)floorf(p[0]), 0), S.W - 1);
+        int y = min(max((int)floorf(p[1]), 0), S.H - 1);
+        int z = min(max((int)floorf(p[2]), 0), S.D - 1);
+        uchar4 l = d.lab[S.vox_off + ((long long)z * S.H + y) * S.W + x];
+        c[0] = l.x; c[1] = l.y; c[2] = l.z;
+    }
+    d.pos[g] = make_float4(p[0], p[1], p[2], (float)id);
+    d.slab[g] = make_float4(c[0], c[1], c[2], 0.0f);
+}
+
+// ---------------------------------------------------------------------------
+// Post-processing (GPU-AS/Image.cpp:1579-1778).
+//   k_post_stats: one block per segment -- dead seeds, alive ranks, the
+//     relabel LUT of the <= 3 dead case, mode and -1 flags.
+//   k_post_chunk_max / k_post_prefix / k_post_apply: forward fills of the
+//     reference's raster loops as a max-scan of "source" voxel indices.
+// The post-processed labels go to the buffer the last pass did not write.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) k_post_stats(AsvDev d)
+{
+    const int si = blockIdx.x;
+    const SegDesc &S = d.segs[si];
+    const int Kp = S.Kp;
+    const unsigned long long *sums = d.sums + 8ull * S.seed_off;
+    int *rank = d.rank + S.seed_off;
+    int *rec = d.post + si * ASV_POST_WORDS;
+    __shared__ int warp_tot[32];
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    // alive rank: exclusive scan of (count >= 1) in seed order (:1603-1618)
+    for (int b0 = 0; b0 < Kp; b0 += blockDim.x) {
+        int i = b0 + threadIdx.x;
+        int alive = (i < Kp && sums[8ull * i + 3] >= 1) ? 1 : 0;
+        unsigned bal = __ballot_sync(FULL, alive);
+        int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        int pre = __popc(bal & ((1u << lane) - 1u));
+        if (lane == 0) warp_tot[w] = __popc(bal);
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            int v = threadIdx.x < (blockDim.x >> 5) ? warp_tot[threadIdx.x] : 0;
+            int incl = v;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int n = __shfl_up_sync(FULL, incl, o);
+                if (threadIdx.x >= o) incl += n;
+            }
+            warp_tot[threadIdx.x] = incl - v;   // exclusive
+        }
+        __syncthreads();
+        if (i < Kp) rank[i] = alive ? carry + warp_tot[w] + pre : -1;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry += warp_tot[w] + pre + alive;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        int valid = carry, dead = Kp - valid;
+        long long negc = (long long)sums[8ull * Kp + 3];
+        rec[POST_DEAD] = dead;
+        rec[POST_NEG] = negc > 0x7fffffffLL ? 0x7fffffff : (int)negc;
+        rec[POST_VALID] = valid;
+        rec[POST_INVALID] = negc > 0 ? 1 : 0;
+        int mode = dead == 0 ? 0 : (dead <= 3 ? 1 : 2);
+        rec[POST_MODE] = mode;
+        const int32_t *lbl = (S.final_buf ? d.labB : d.labA) + S.vox_off;
+        int l0 = lbl[0];
+        rec[POST_L0] = l0;
+        rec[POST_M0] = (l0 >= 0 && l0 < Kp && rank[l0] >= 0) ? rank[l0] : 0;
+        int nd = 0;
+        for (int i = 0; i < Kp && nd < 4; i++)
+            if (sums[8ull * i + 3] < 1) rec[POST_DEAD0 + nd++] = i;
+    }
+}
+
+// relabelled value of a raw label before the fills (the <= 3 dead relabel
+// of label_replace.gs:26-29 applied in order, :1652-1673)
+__device__ __forceinline__ int asv_relabel(const int *rec, int Kp, int l)
+{
+    if (rec[POST_MODE] != 1 || l < 0) return l;
+    int last = Kp;
+    for (int k = 0; k < rec[POST_DEAD]; k++) {
+        last -= 1;
+        if (l == last) l = rec[POST_DEAD0 + k];
+    }
+    return l;
+}
+
+// source index of voxel v for the forward fill, or -1
+__device__ __forceinline__ long long asv_fill_src(const int *rec, int Kp, long long v, int l)
+{
+    if (rec[POST_MODE] == 2) {                                  // :1738-1746
+        if (v == 0) return 0;
+        return (l != rec[POST_L0] && l != -1) ? v : -1;
+    }
+    int r = asv_relabel(rec, Kp, l);                            // :1763-1775
+    if (v == 0) return 0;
+    return r != -1 ? v : -1;
+}
+
+__device__ __forceinline__ bool asv_needs_scan(const int *rec)
+{
+    return rec[POST_MODE] == 2 || rec[POST_INVALID] != 0;
+}
+
+__global__ void __launch_bounds__(256) k_post_chunk_max(AsvDev d)
+{
+    int si = asv_find_seg(d.chunk_prefix, d.nseg, blockIdx.x);
+    const SegDesc &S = d.segs[si];
+    const int *rec = d.post + si * ASV_POST_WORDS;
+    if (!asv_needs_scan(rec)) return;
+    const int32_t *lbl = (S.final_buf ? d.labB : d.labA) + S.vox_off;
+    long long base = (long long)(blockIdx.x - d.chunk_prefix[si]) * ASV_CHUNK;
+    long long m = -1;
+    for (int i = 0; i < ASV_CHUNK / 256; i++) {
+        long long v = base + i * 256 + threadIdx.x;
+        if (v < S.nvox) { long long s = asv_fill_src(rec, S.Kp, v, lbl[v]); if (s > m) m = s; }
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) { long long n = __shfl_xor_sync(FULL, m, o); if (n > m) m = n; }
+    __shared__ long long wm[8];
+    if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long r = wm[0];
+        for (int k = 1; k < 8; k++) if (wm[k] > r) r = wm[k];
+        // store +1 so that a chunk without source is 0
+        d.scan[blockIdx.x] = (int)(r + 1);
+    }
+}
+
+// exclusive max-scan of the chunk maxima within each segment (1 block / segment)
+__global__ void __launch_bounds__(1024) k_post_prefix(AsvDev d)
+{
+    int si = blockIdx.x;
+    const int *rec = d.post + si * ASV_POST_WORDS;
+    if (!asv_needs_scan(rec)) return;
+    int c0 = d.chunk_prefix[si], c1 = d.chunk_prefix[si + 1];
+    __shared__ int carry;
+    __shared__ int wmax[32];
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int b0 = c0; b0 < c1; b0 += blockDim.x) {
+        int c = b0 + threadIdx.x;
+        int v = c < c1 ? d.scan[c] : 0;
+        int incl = v;
+        int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) { int n = __shfl_up_sync(FULL, incl, o); if (lane >= o && n > incl) incl = n; }
+        if (lane == 31) wmax[w] = incl;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            int x = wmax[threadIdx.x];
+            int ix = x;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) { int n = __shfl_up_sync(FULL, ix, o); if (threadIdx.x >= o && n > ix) ix = n; }
+            wmax[threadIdx.x] = ix;
+        }
+        __syncthreads();
+        int before = w > 0 ? wmax[w - 1] : 0;
+        int excl_in_warp = __shfl_up_sync(FULL, incl, 1);
+        if (lane == 0) excl_in_warp = 0;
+        int ex = max(max(carry, before), excl_in_warp);
+        int tot = max(carry, wmax[31]);
+        __syncthreads();
+        if (c < c1) d.scan[c] = ex;      // max source+1 in earlier chunks of the segment
+        if (threadIdx.x == 0) carry = tot;
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(256) k_post_apply(AsvDev d)
+{
+    int si = asv_find_seg(d.chunk_prefix, d.nseg, blockIdx.x);
+    const SegDesc &S = d.segs[si];
+    const int *rec = d.post + si * ASV_POST_WORDS;
+    const int32_t *lbl = (S.final_buf ? d.labB : d.labA) + S.vox_off;
+    int32_t *out = (S.final_buf ? d.labA : d.labB) + S.vox_off;
+    const int *rank = d.rank + S.seed_off;
+    const int Kp = S.Kp;
+    long long base = (long long)(blockIdx.x - d.chunk_prefix[si]) * ASV_CHUNK;
+    const bool scan = asv_needs_scan(rec);
+    const int mode = rec[POST_MODE];
+    // carried source index from earlier chunks (stored +1)
+    long long carry = scan ? (long long)d.scan[blockIdx.x] - 1 : -1;
+    // each thread owns ASV_CHUNK/256 consecutive voxels for the in-block scan
+    const int per = ASV_CHUNK / 256;
+    long long v0 = base + (long long)threadIdx.x * per;
+    long long m = -1;
+    if (scan)
+        for (int k = 0; k < per; k++) {
+            long long v = v0 + k;
+            if (v < S.nvox) { long long s = asv_fill_src(rec, Kp, v, lbl[v]); if (s > m) m = s; }
+        }
+    // exclusive max-scan of the per-thread maxima across the block
+    long long excl = -1;
+    if (scan) {
+        long long incl = m;
+        int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) { long long n = __shfl_up_sync(FULL, incl, o); if (lane >= o && n > incl) incl = n; }
+        __shared__ long long wmx[8];
+        if (lane == 31) wmx[w] = incl;
+        __syncthreads();
+        long long before = -1;
+        for (int k = 0; k < w; k++) if (wmx[k] > before) before = wmx[k];
+        long long ew = __shfl_up_sync(FULL, incl, 1);
+        if (lane == 0) ew = -1;
+        excl = max(max(before, ew), carry);
+    }
+    long long src = excl;
+    for (int k = 0; k < per; k++) {
+        long long v = v0 + k;
+        if (v >= S.nvox) break;
+        int l = lbl[v];
+        int r;
+        if (!scan) {
+            r = asv_relabel(rec, Kp, l);
+        } else {
+            long long s = asv_fill_src(rec, Kp, v, l);
+            if (s > src) src = s;
+            if (mode == 2) {
+                // out = map(label at src); src 0 -> map(L0)
+                if (src <= 0) r = rec[POST_M0];
+                else {
+                    int ls = lbl[src];
+                    r = (ls >= 0 && ls < Kp && rank[ls] >= 0) ? rank[ls] : 0;
+                }
+            } else {
+                int rl = asv_relabel(rec, Kp, l);
+                if (v == 0 || rl != -1) r = rl;
+                else if (src >= 1) r = asv_relabel(rec, Kp, lbl[src]);
+                else {
+                    int r0 = asv_relabel(rec, Kp, lbl[0]);
+                    r = r0 >= 0 ? r0 : 0;
+                }
+            }
+        }
+        out[v] = r;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// launch wrappers
+// ---------------------------------------------------------------------------
+static inline int seed_blocks(const AsvDev &d) { return (d.total_seeds + 127) / 128; }
+
+void asv_launch_srgb_table(const AsvDev &d, cudaStream_t st) { k_srgb_table<<<1, 256, 0, st>>>(d.srgb); }
+void asv_launch_rgb2lab(const AsvDev &d, cudaStream_t st) { k_rgb2lab<<<d.total_chunks, 256, 0, st>>>(d); }
+void asv_launch_density(const AsvDev &d, cudaStream_t st) { k_density<<<d.total_chunks, 256, 0, st>>>(d); }
+void asv_launch_density_adjust(const AsvDev &d, cudaStream_t st) { k_density_adjust<<<d.nseg, 32, 0, st>>>(d, d.Mring); }
+void asv_launch_first_init(const AsvDev &d, cudaStream_t st) { k_first_init<<<seed_blocks(d), 128, 0, st>>>(d); }
+void asv_launch_draw(const AsvDev &d, cudaStream_t st) { k_draw<<<seed_blocks(d), 128, 0, st>>>(d); }
+
+int asv_jfa_grid_blocks(int total_tiles)
+{
+    static int blocks = 0;
+    if (!blocks) {
+        int dev = 0, sms = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_jfa, 256, 0);
+        blocks = sms * (per > 0 ? per : 1);
+        if (blocks <= 0) blocks = 1024;
+    }
+    return total_tiles < blocks ? total_tiles : blocks;
+}
+
+void asv_launch_jfa(const AsvDev &d, int pass, int grid_blocks, cudaStream_t st)
+{
+    const int32_t *in = (pass & 1) ? d.labB : d.labA;
+    int32_t *out = (pass & 1) ? d.labA : d.labB;
+    k_jfa<<<grid_blocks, 256, 0, st>>>(d, pass, in, out);
+}
+
+void asv_launch_jfa_single(const AsvDev &d, const int32_t *in, int32_t *out, int step, float ratio,
+                           cudaStream_t st)
+{
+    k_jfa_single<<<asv_jfa_grid_blocks(d.total_tiles), 256, 0, st>>>(d, in, out, step, ratio);
+}
+
+void asv_launch_centroids(const AsvDev &d, cudaStream_t st) { k_centroids<<<d.total_chunks, 256, 0, st>>>(d); }
+void asv_launch_finalize(const AsvDev &d, cudaStream_t st) { k_finalize<<<seed_blocks(d), 128, 0, st>>>(d); }
+
+void asv_launch_post(const AsvDev &d, cudaStream_t st)
+{
+    k_post_stats<<<d.nseg, 1024, 0, st>>>(d);
+    k_post_chunk_max<<<d.total_chunks, 256, 0, st>>>(d);
+    k_post_prefix<<<d.nseg, 1024, 0, st>>>(d);
+    k_post_apply<<<d.total_chunks, 256, 0, st>>>(d);
+}

@@ -1,0 +1,212 @@
+"""Python mirror of the reference's Image/Render operator surface over libasv.
+
+`Image` has one method per method of the reference's `Image` class
+(GPU-AS/Image.h:73-88), each a thin call into the C ABI; `Render.run` is the
+plain per-clip pipeline of `Render::run` (GPU-AS/Render.cpp:100-350) with
+host buffers in and labels out.  Everything runs on the CUDA path of
+libasv.so; there is no CPU fallback.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import AsvError, Config, Info, Stats, SynthParams
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def synth_clip(W, H, D, n_ellipses=12, noise_sigma=5.0, vmax=3.0, jitter=0.0, drift_amp=0.0,
+               drift_period=60.0, seed=1, frame0=0):
+    """Seeded synthetic clip (rgb uint8 [D,H,W,3], fwd/bwd float32 [D,H,W,2])."""
+    lib = _lib.load()
+    rgb = np.empty((D, H, W, 3), np.uint8)
+    fwd = np.empty((D, H, W, 2), np.float32)
+    bwd = np.empty((D, H, W, 2), np.float32)
+    p = SynthParams(W, H, frame0, D, n_ellipses, noise_sigma, vmax, jitter, drift_amp,
+                    drift_period, seed)
+    if lib.asv_synth_clip(ctypes.byref(p), _ptr(rgb), _ptr(fwd), _ptr(bwd)) != 0:
+        raise ValueError("bad synthetic clip parameters")
+    return rgb, fwd, bwd
+
+
+def config(variant=_lib.VARIANT_PLAIN, lloyd_iters=20, full_ladder=0, middlebury=0,
+           density_adjust=1, device=0, stream=None, hbm_budget=0, use_graph=1, instrument=0):
+    c = Config()
+    _lib.load().asv_config_default(ctypes.byref(c))
+    c.variant, c.lloyd_iters, c.full_ladder, c.middlebury = variant, lloyd_iters, full_ladder, middlebury
+    c.density_adjust, c.device, c.stream, c.hbm_budget = density_adjust, device, stream, hbm_budget
+    c.use_graph, c.instrument = use_graph, instrument
+    return c
+
+
+class Image:
+    """One clip on the GPU; methods follow the reference's Image class."""
+
+    def __init__(self, cfg=None, **kw):
+        self.lib = _lib.load()
+        self.cfg = cfg if cfg is not None else config(**kw)
+        h = ctypes.c_void_p()
+        st = self.lib.asv_create(ctypes.byref(self.cfg), ctypes.byref(h))
+        if st != _lib.ASV_OK:
+            raise AsvError(st, self.lib.asv_status_string(st).decode())
+        self.h = h
+        self.shape = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.asv_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _ck(self, st):
+        if st != _lib.ASV_OK:
+            raise AsvError(st, self.lib.asv_last_error(self.h).decode())
+
+    # --- reference Image methods ------------------------------------------
+    def init_gpu(self, rgb, K):
+        rgb = np.ascontiguousarray(rgb, np.uint8)
+        D, H, W, _ = rgb.shape
+        self._ck(self.lib.asv_init_gpu(self.h, _ptr(rgb), W, H, D, K))
+        self.shape = (D, H, W)
+
+    def upload_flow(self, fwd, bwd):
+        fwd = np.ascontiguousarray(fwd, np.float32)
+        bwd = np.ascontiguousarray(bwd, np.float32)
+        self._ck(self.lib.asv_upload_flow(self.h, _ptr(fwd), _ptr(bwd)))
+
+    def initialization(self):
+        self._ck(self.lib.asv_initialization(self.h))
+
+    def seed_matrix(self):
+        self._ck(self.lib.asv_seed_matrix(self.h))
+
+    def RGB2LAB(self):
+        self._ck(self.lib.asv_rgb2lab(self.h))
+
+    def Ld_first_init(self):
+        self._ck(self.lib.asv_ld_first_init(self.h))
+
+    def flood(self, it):
+        self._ck(self.lib.asv_flood(self.h, it))
+
+    def centroids_next_seeds(self, it):
+        self._ck(self.lib.asv_centroids_next_seeds(self.h, it))
+
+    def Ld_next_seeds_matrix(self, it):
+        self._ck(self.lib.asv_ld_next_seeds_matrix(self.h, it))
+
+    def check_dead_seeds(self):
+        out = np.empty(self.shape, np.int32)
+        self._ck(self.lib.asv_check_dead_seeds(self.h, _ptr(out)))
+        return out
+
+    def run_lloyd(self):
+        self._ck(self.lib.asv_run_lloyd(self.h))
+
+    # --- state ---------------------------------------------------------------
+    def info(self):
+        i = Info()
+        self._ck(self.lib.asv_get_info(self.h, ctypes.byref(i)))
+        return i
+
+    def labels(self):
+        out = np.empty(self.shape, np.int32)
+        self._ck(self.lib.asv_get_labels(self.h, _ptr(out)))
+        return out
+
+    def raw_labels(self):
+        out = np.empty(self.shape, np.int32)
+        self._ck(self.lib.asv_get_raw_labels(self.h, _ptr(out)))
+        return out
+
+    def seeds(self):
+        out = np.empty((self.info().Kp, 12), np.float32)
+        self._ck(self.lib.asv_get_seeds(self.h, _ptr(out)))
+        return out
+
+    def set_seeds(self, seeds):
+        seeds = np.ascontiguousarray(seeds, np.float32)
+        self._ck(self.lib.asv_set_seeds(self.h, _ptr(seeds), seeds.shape[0]))
+
+    def lab(self):
+        out = np.empty(self.shape + (4,), np.uint8)
+        self._ck(self.lib.asv_get_lab(self.h, _ptr(out)))
+        return out
+
+    def sums(self):
+        out = np.empty((self.info().Kp + 1, 7), np.int64)
+        self._ck(self.lib.asv_get_sums(self.h, _ptr(out)))
+        return out
+
+    def check_dead_seeds_host(self, raw):
+        raw = np.ascontiguousarray(raw, np.int32)
+        out = np.empty_like(raw)
+        self._ck(self.lib.asv_check_dead_seeds_host(self.h, _ptr(raw), _ptr(out)))
+        return out
+
+    def jfa_pass(self, labels_in, step, ratio):
+        labels_in = np.ascontiguousarray(labels_in, np.int32)
+        out = np.empty_like(labels_in)
+        self._ck(self.lib.asv_jfa_pass_host(self.h, step, ratio, _ptr(labels_in), _ptr(out)))
+        return out
+
+    def stats(self):
+        s = Stats()
+        self._ck(self.lib.asv_get_stats(self.h, ctypes.byref(s)))
+        return s
+
+    def stream(self):
+        p = ctypes.c_void_p()
+        self._ck(self.lib.asv_get_stream(self.h, ctypes.byref(p)))
+        return p.value
+
+    def synchronize(self):
+        self._ck(self.lib.asv_synchronize(self.h))
+
+    def segment(self, rgb, fwd, bwd, K):
+        """Render::run's plain per-clip sequence; returns post-processed labels."""
+        self.init_gpu(rgb, K)
+        self.upload_flow(fwd, bwd)
+        self.initialization()
+        self.seed_matrix()
+        self.RGB2LAB()
+        self.run_lloyd()
+        return self.labels()
+
+
+def write_labels_txt(path, labels):
+    D, H, W = labels.shape
+    lab = np.ascontiguousarray(labels, np.int32)
+    if _lib.load().asv_write_labels_txt(path.encode(), _ptr(lab), W, H, D) != 0:
+        raise OSError(f"cannot write {path}")
+
+
+def write_render_ppm(prefix, labels, n_labels):
+    D, H, W = labels.shape
+    lab = np.ascontiguousarray(labels, np.int32)
+    if _lib.load().asv_write_render_ppm(prefix.encode(), _ptr(lab), W, H, D, n_labels) != 0:
+        raise OSError(f"cannot write {prefix}*.ppm")
+
+
+def preprocess_frame(bgr):
+    """Render::cvMat2TexureInput on one BGR frame stored top row first."""
+    bgr = np.ascontiguousarray(bgr, np.uint8)
+    H, W, _ = bgr.shape
+    out = np.empty_like(bgr)
+    if _lib.load().asv_preprocess_frame(_ptr(bgr), W, H, _ptr(out)) != 0:
+        raise ValueError("bad frame")
+    return out

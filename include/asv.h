@@ -1,0 +1,179 @@
+/*
+ * asv.h -- C ABI of the GB300 supervoxel engine (libasv.so).
+ *
+ * The reference (dongxiao0401/anisotropic_supervoxel) has no plugin API; its
+ * operator surface is the `Image` class that `Render::run` drives in a fixed
+ * order (GPU-AS/Image.h:73-88, call order GPU-AS/Render.cpp:254-319).  Each
+ * entry point below replaces one of those methods; the comment on each names
+ * the method and the lines it replaces.
+ *
+ * Conventions
+ *  - Every call returns asv_status (0 = ASV_OK).  asv_last_error() gives the
+ *    message of the last failing call on a context.  No exception crosses
+ *    the ABI.
+ *  - The context owns all device memory.  Host buffers passed in or out stay
+ *    owned by the caller and are not retained after the call returns.
+ *  - A context runs on one CUDA stream (its own, or the one in the config)
+ *    and is not thread-safe; distinct contexts are independent.
+ *  - Volumes are x-fastest [D][H][W] in texture orientation (row y = 0 is
+ *    the bottom image row, as after the reference's vertical flip,
+ *    GPU-AS/Render.cpp:354-359).  RGB is 3 bytes per voxel, flow is 2
+ *    floats (dx, dy) per voxel, labels are int32 (-1 = no seed reached).
+ *  - Sizes: 2 <= D, W,H,D <= 4096, requested seeds K >= 1, actual seed count
+ *    K' < 32768 (the reference stores labels as R16I, GPU-AS/Image.cpp:263).
+ */
+#ifndef ASV_H
+#define ASV_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int asv_status;
+enum {
+    ASV_OK = 0,
+    ASV_ERR_BAD_ARG = 1,     /* invalid size / pointer / order of calls */
+    ASV_ERR_OOM = 2,         /* device allocation failed */
+    ASV_ERR_OVER_BUDGET = 3, /* request exceeds the configured HBM budget */
+    ASV_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up */
+    ASV_ERR_CUDA = 5,        /* a CUDA runtime call failed */
+    ASV_ERR_STATE = 6,       /* call out of order (e.g. flood before init) */
+    ASV_ERR_NO_DEVICE = 7    /* no CUDA device visible */
+};
+
+enum { ASV_VARIANT_PLAIN = 0, ASV_VARIANT_STREAM = 1 };
+
+typedef struct asv_config {
+    int variant;        /* ASV_VARIANT_PLAIN: compactness 8 + flow-angle filter on reseed
+                           (GPU-AS/Image.cpp:1050, :1407-1410); ASV_VARIANT_STREAM:
+                           compactness 6, no filter (streamGPU-AS/Image.cpp:968). */
+    int lloyd_iters;    /* Lloyd iterations; reference default 20 (GPU-AS/Render.cpp:11) */
+    int full_ladder;    /* 0: reference JFA ladder; 1: powers of two from log2(max dim) */
+    int middlebury;     /* 1: s = floor(sqrt(W*H/K)) (GPU-AS/Image.cpp:25-29) */
+    int density_adjust; /* 1: gradient-density seed placement (reference); 0: grid only */
+    int device;         /* CUDA device ordinal */
+    void *stream;       /* cudaStream_t to run on; NULL: the context creates its own */
+    size_t hbm_budget;  /* bytes the context may allocate; 0 = unlimited */
+    int use_graph;      /* 1: asv_run_lloyd replays a captured CUDA graph */
+    int instrument;     /* 1: record per-stage CUDA-event times (asv_get_stats) */
+} asv_config;
+
+typedef struct asv_info {
+    int W, H, D;
+    int K;              /* requested seeds */
+    int Kp;             /* ac_seeds_num: seeds actually placed */
+    int s;              /* JFA base step (GPU-AS/Image.cpp:24-33) */
+    float ratio;        /* (compactness/s)^2 */
+    int passes;         /* JFA passes per Lloyd iteration */
+    int steps[32];      /* step of each pass */
+    int dead;           /* dead seeds after the last iteration (GPU-AS/Image.cpp:1603-1618) */
+    int neg_count;      /* voxels left at label -1 by the last JFA pass */
+    int final_label_num;
+} asv_info;
+
+typedef struct asv_stats {
+    double jfa_ms;      /* summed device time of the JFA passes of the last run */
+    int jfa_launches;
+    double centroid_ms;
+    double metric_ms;
+    double total_ms;    /* device time of the last asv_run_lloyd */
+    int launches;       /* kernels launched by the last asv_run_lloyd */
+} asv_stats;
+
+typedef struct asv_ctx asv_ctx;
+
+/* ---- lifetime ---------------------------------------------------------- */
+void asv_config_default(asv_config *cfg);
+asv_status asv_create(const asv_config *cfg, asv_ctx **out);
+asv_status asv_destroy(asv_ctx *ctx);
+const char *asv_last_error(const asv_ctx *ctx);
+const char *asv_status_string(asv_status st);
+int asv_version(void);
+
+/* ---- the reference's Image methods, one entry point each -------------- */
+
+/* Image::init_gpu + init_image_texture + init_seeds + init_variables
+ * (GPU-AS/Image.cpp:320-345, :198-272, :20-158, :1047-1053): uploads the
+ * RGB8 clip (D*H*W*3 bytes) and places the regular grid of seeds for K. */
+asv_status asv_init_gpu(asv_ctx *ctx, const uint8_t *rgb, int W, int H, int D, int K);
+
+/* Output of Image::forward_backward_flow (GPU-AS/Image.cpp:643-686), which
+ * the reference computes with OpenCV; here it is an input: fwd[z] is the
+ * flow z -> z+1, bwd[z] the flow z -> z-1, each D*H*W*2 floats.  fwd[D-1]
+ * and bwd[0] are not read by the metric solve. */
+asv_status asv_upload_flow(asv_ctx *ctx, const float *fwd, const float *bwd);
+
+/* Image::initialization (GPU-AS/Image.cpp:350-620): gradient-density seed
+ * placement (derivative_t.gs, density_grid.vs, 1-D redistribution). */
+asv_status asv_initialization(asv_ctx *ctx);
+
+/* Image::seed_matrix (GPU-AS/Image.cpp:689-872) with matrix_slover
+ * (:874-1009): per-seed metric tensor from flow, with the 1-ring / 2-ring /
+ * nearest-PSD fallbacks, on the device. */
+asv_status asv_seed_matrix(asv_ctx *ctx);
+
+/* Image::RGB2LAB (GPU-AS/Image.cpp:296-315, shaders/RGB2LAB.fs). */
+asv_status asv_rgb2lab(asv_ctx *ctx);
+
+/* Image::Ld_first_init (GPU-AS/Image.cpp:1017-1045, shaders/draw_seeds). */
+asv_status asv_ld_first_init(asv_ctx *ctx);
+
+/* Image::flood (GPU-AS/Image.cpp:1061-1190, shaders/flood.gs): the JFA
+ * ladder of one Lloyd iteration. */
+asv_status asv_flood(asv_ctx *ctx, int lloyd_iter);
+
+/* Image::centroids_next_seeds (GPU-AS/Image.cpp:1238-1297, shaders/
+ * centroids.vs, aver_exception.vs): per-label sums and, unless lloyd_iter is
+ * the last iteration, the reseed. */
+asv_status asv_centroids_next_seeds(asv_ctx *ctx, int lloyd_iter);
+
+/* Image::Ld_next_seeds_matrix (GPU-AS/Image.cpp:1300-1575): metric at the
+ * new seed positions and the seed redraw, without the host round trip. */
+asv_status asv_ld_next_seeds_matrix(asv_ctx *ctx, int lloyd_iter);
+
+/* Image::check_dead_seeds + sequence_label (GPU-AS/Image.cpp:1579-1778):
+ * dead-seed relabel and -1 fill on the device; copies the final labels to
+ * labels_out (D*H*W int32) when it is not NULL. */
+asv_status asv_check_dead_seeds(asv_ctx *ctx, int32_t *labels_out);
+
+/* The whole Lloyd loop of Render::run (GPU-AS/Render.cpp:277-303): first
+ * init, `lloyd_iters` x (reseed, flood, centroids), check_dead_seeds.  The
+ * final labels stay on the device (read them with asv_get_labels). */
+asv_status asv_run_lloyd(asv_ctx *ctx);
+
+/* Convenience: init_gpu + upload_flow + initialization + seed_matrix +
+ * RGB2LAB + run_lloyd + labels, the plain per-clip form of Render::run. */
+asv_status asv_segment_clip(asv_ctx *ctx, const uint8_t *rgb, const float *fwd,
+                            const float *bwd, int W, int H, int D, int K,
+                            int32_t *labels_out);
+
+/* ---- state access ------------------------------------------------------ */
+asv_status asv_get_info(asv_ctx *ctx, asv_info *info);
+asv_status asv_get_labels(asv_ctx *ctx, int32_t *out);     /* post-processed */
+asv_status asv_get_raw_labels(asv_ctx *ctx, int32_t *out); /* last JFA pass */
+/* seed table, Kp x 12 floats: x, y, z, L, a, b, M00, M01, M02, M11, M12, M22 */
+asv_status asv_get_seeds(asv_ctx *ctx, float *out);
+asv_status asv_set_seeds(asv_ctx *ctx, const float *in, int Kp);
+asv_status asv_get_lab(asv_ctx *ctx, uint8_t *out);        /* D*H*W*4 (L, a, b, 0) */
+/* per-label sums of the last centroid pass, (Kp+1) x 7 int64: sum(2x+1),
+ * sum(2y+1), sum(2z+1), count, sum L, sum a, sum b; row Kp = label -1 */
+asv_status asv_get_sums(asv_ctx *ctx, int64_t *out);
+/* check_dead_seeds over caller-given raw labels (D*H*W int32, -1 allowed):
+ * recomputes the per-label sums from them, then relabels and fills as
+ * asv_check_dead_seeds does; post-processed labels to out. */
+asv_status asv_check_dead_seeds_host(asv_ctx *ctx, const int32_t *raw_in, int32_t *out);
+/* one JFA pass over host label volumes with the current seed table */
+asv_status asv_jfa_pass_host(asv_ctx *ctx, int step, float ratio, const int32_t *in, int32_t *out);
+asv_status asv_get_stats(asv_ctx *ctx, asv_stats *st);
+asv_status asv_get_stream(asv_ctx *ctx, void **stream);
+asv_status asv_synchronize(asv_ctx *ctx);
+/* bytes of device memory a clip of this size needs (admission control) */
+size_t asv_clip_bytes(int W, int H, int D, int K);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,60 @@
+/*
+ * asv_host.h -- host pipeline around the C ABI (libasv.so): synthetic clip
+ * source, frame preprocessing and the reference's output writers.
+ *
+ * These replace the host parts of the reference's Render class that sit
+ * either side of the supervoxel path (GPU-AS/Render.cpp, GPU-AS/Image.cpp
+ * print_sv_txt / print_render); they run on the CPU as in the reference.
+ */
+#ifndef ASV_HOST_H
+#define ASV_HOST_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Seeded synthetic video: linear-gradient background plus moving ellipses
+ * of uniform-random LAB colour, additive Gaussian noise, and the exact
+ * generating motion as forward/backward flow.  Frames are produced in
+ * texture orientation (y up), i.e. directly in the layout asv_init_gpu
+ * takes.  Frame f of a video depends only on (seed, f), so windows of a
+ * long video can be generated independently. */
+typedef struct asv_synth_params {
+    int W, H;
+    int frame0;         /* first frame index to generate */
+    int nframes;        /* frames to generate */
+    int n_ellipses;
+    float noise_sigma;  /* Gaussian noise on uint8 */
+    float vmax;         /* speed drawn uniformly in [0, vmax] px/frame */
+    float jitter;       /* per-frame velocity jitter, uniform in [-jitter, jitter] */
+    float drift_amp;    /* background drift amplitude in px (0 = static) */
+    float drift_period; /* background drift period in frames */
+    uint64_t seed;
+} asv_synth_params;
+
+/* rgb: nframes*H*W*3; fwd, bwd: nframes*H*W*2 (either may be NULL). */
+int asv_synth_clip(const asv_synth_params *p, uint8_t *rgb, float *fwd, float *bwd);
+
+/* Render::cvMat2TexureInput (GPU-AS/Render.cpp:354-359): 3x3 Gaussian blur
+ * (sigma 0 -> [1,2,1]/4 separable, border reflect-101, rounded half up),
+ * BGR -> RGB and vertical flip, for one frame stored top row first. */
+int asv_preprocess_frame(const uint8_t *bgr, int W, int H, uint8_t *rgb_tex);
+
+/* Image::print_sv_txt (GPU-AS/Image.cpp:1780-1806): frames in order, rows
+ * from y = H-1 down to 0, each label left-aligned in 4 columns plus a
+ * space, a newline per row and two blank lines per frame. */
+int asv_write_labels_txt(const char *path, const int32_t *labels, int W, int H, int D);
+
+/* Image::print_render (GPU-AS/Image.cpp:1883-1935): one colour per label
+ * from rand() % 256 (C library generator in its default state), -1 black,
+ * written as binary PPM frames <prefix>NNNNN.ppm, top row first. */
+int asv_write_render_ppm(const char *prefix, const int32_t *labels, int W, int H, int D,
+                         int n_labels);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,985 @@
+/*
+ * asv_oracle.c -- CPU restatement of the reference supervoxel path.
+ *
+ * TEST INFRASTRUCTURE ONLY (see asv_oracle.h).  Compiled with
+ * -ffp-contract=off: every float/double operation below is one IEEE
+ * operation in the order written, which is the evaluation order the CUDA
+ * kernels reproduce.
+ *
+ * Reference files (paths inside dongxiao0401/anisotropic_supervoxel):
+ *   GPU-AS/Image.cpp, GPU-AS/Render.cpp, GPU-AS/shaders,
+ *   streamGPU-AS/Image.cpp, streamGPU-AS/Render.cpp.
+ */
+#include "asv_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define IDX(x, y, z) (((long)(z) * H + (y)) * (long)W + (x))
+
+static int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+/* ======================================================================
+ * Grid seeds: GPU-AS/Image.cpp:20-92 (init_seeds),
+ *             streamGPU-AS/Image.cpp:26-103 (initialization_grid).
+ * ==================================================================== */
+int orc_grid_seeds(int W, int H, int D, int K, int middlebury, float *seeds4, int cap,
+                   orc_grid_info *info)
+{
+    if (W < 1 || H < 1 || D < 1 || K < 1) return -1;
+    long N = (long)W * H * D;
+    double voxel_size = (double)(N / K);                       /* Image.cpp:24 (int division) */
+    int s;
+    if (middlebury) s = (int)floor(pow(1.0 * W * H / K, 0.5)); /* Image.cpp:28 */
+    else s = (int)floor(pow(voxel_size, 1.0 / 3));             /* Image.cpp:32 */
+    long kdd = (long)K * D * D / W / H;                         /* Image.cpp:37 */
+    int dNum = (int)pow((double)(float)kdd, 1.0 / 3.0);
+    if (dNum == 0) dNum = 1;
+    int fsn = K / dNum;                                         /* :42 */
+    int wNum = (int)sqrtf((float)((long)fsn * W / H));          /* :43 float sqrt */
+    if (wNum == 0) return -2;
+    int hNum = fsn / wNum;                                      /* :44 */
+    if (hNum == 0) return -2;
+    int Kp = dNum * hNum * wNum;                                /* :45 */
+    if (info) {
+        info->s = s; info->dNum = dNum; info->hNum = hNum; info->wNum = wNum; info->Kp = Kp;
+    }
+    if (!seeds4) return Kp;
+    if (cap < Kp) return -3;
+    int stepD = D / dNum, stepH = H / hNum, stepW = W / wNum;   /* :46-48 */
+    int d_rem = D - stepD * dNum, h_rem = H - stepH * hNum, w_rem = W - stepW * wNum;
+    int td = (d_rem < 1) ? 0 : 1, th, tw;                       /* :57-60 */
+    int count = 0;
+    for (int k = 0; k < dNum; k++) {
+        th = 1;
+        for (int i = 0; i < hNum; i++) {
+            tw = 1;
+            for (int j = 0; j < wNum; j++) {
+                int sx = (int)(j * stepW + 0.5 * stepW + tw);   /* :71-73 double -> int */
+                int sy = (int)(i * stepH + 0.5 * stepH + th);
+                int sz = (int)(k * stepD + 0.5 * stepD + td);
+                if (sx > W - 1) sx = W - 1;
+                if (sy > H - 1) sy = H - 1;
+                if (sz > D - 1) sz = D - 1;
+                if (tw < w_rem) tw++;
+                seeds4[4 * count + 0] = (float)(sx + 0.5);
+                seeds4[4 * count + 1] = (float)(sy + 0.5);
+                seeds4[4 * count + 2] = (float)(sz + 0.5);
+                seeds4[4 * count + 3] = (float)count;
+                count++;
+            }
+            if (th < h_rem) th++;
+        }
+        if (td < d_rem) td++;
+    }
+    return Kp;
+}
+
+/* ratio = (compactness/s)^2 in float: GPU-AS/Image.cpp:1050-1051,
+ * streamGPU-AS/Image.cpp:968-969. */
+float orc_ratio(int s, float compactness)
+{
+    float q = compactness / (float)s;
+    return q * q;
+}
+
+/* ======================================================================
+ * RGB -> LAB: GPU-AS/shaders/RGB2LAB.fs:11-79.  Input texel = unorm8/255.
+ * ==================================================================== */
+static float pow_cr(float x, float y) { return (float)pow((double)x, (double)y); }
+
+static void lab_of(const uint8_t *c, uint8_t *out)
+{
+    float rgb[3], t[3];
+    for (int k = 0; k < 3; k++) rgb[k] = (float)c[k] / 255.0f;
+    for (int k = 0; k < 3; k++) {
+        if (rgb[k] <= 0.04045f) t[k] = rgb[k] / 12.92f;                      /* fs:27-40 */
+        else t[k] = pow_cr((rgb[k] + 0.055f) / 1.055f, 2.4f);
+    }
+    float X = (t[0] * 0.412453f + t[1] * 0.357580f) + t[2] * 0.180423f;    /* fs:19-21,42-44 */
+    float Y = (t[0] * 0.212671f + t[1] * 0.715160f) + t[2] * 0.072169f;
+    float Z = (t[0] * 0.019334f + t[1] * 0.119193f) + t[2] * 0.950227f;
+    float r[3] = { X / 0.950456f, Y / 1.0f, Z / 1.088754f };                 /* fs:54-55 */
+    float f[3];
+    for (int k = 0; k < 3; k++) {
+        if (r[k] > 0.008856f) f[k] = pow_cr(r[k], 1.0f / 3.0f);               /* fs:57-70 */
+        else f[k] = (903.3f * r[k] + 16.0f) / 116.0f;
+    }
+    float L = 116.0f * f[1] - 16.0f;                                          /* fs:72 */
+    float A = 500.0f * (f[0] - f[1]);
+    float B = 200.0f * (f[1] - f[2]);
+    L = L * 2.55f; A = A + 128.0f; B = B + 128.0f;                            /* fs:74-76 */
+    float v[3] = { floorf(L + 0.5f), floorf(A + 0.5f), floorf(B + 0.5f) };   /* fs:77 */
+    for (int k = 0; k < 3; k++) {
+        float q = v[k] < 0.0f ? 0.0f : (v[k] > 255.0f ? 255.0f : v[k]);
+        out[k] = (uint8_t)q;
+    }
+}
+
+void orc_rgb2lab(const uint8_t *rgb, long n, uint8_t *lab4)
+{
+    for (long i = 0; i < n; i++) {
+        lab_of(rgb + 3 * i, lab4 + 4 * i);
+        lab4[4 * i + 3] = 0;
+    }
+}
+
+/* ======================================================================
+ * Gradient: GPU-AS/shaders/derivative_t.gs:24-49 (left, "up" = y-1 and
+ * previous frame, clamp-to-edge), stored as RGB16F (Image.cpp:236-238).
+ * ==================================================================== */
+uint16_t orc_float_to_half(float f)
+{
+    uint32_t u; memcpy(&u, &f, 4);
+    uint32_t sign = (u >> 16) & 0x8000u;
+    uint32_t exp = (u >> 23) & 0xffu;
+    uint32_t man = u & 0x7fffffu;
+    if (exp == 0xffu) return (uint16_t)(sign | 0x7c00u | (man ? 0x200u : 0u));
+    int e = (int)exp - 127 + 15;
+    if (e >= 31) return (uint16_t)(sign | 0x7c00u);
+    if (e <= 0) {
+        if (e < -10) return (uint16_t)sign;
+        man |= 0x800000u;
+        int shift = 14 - e;
+        uint32_t h = man >> shift;
+        uint32_t rem = man & ((1u << shift) - 1u), half = 1u << (shift - 1);
+        if (rem > half || (rem == half && (h & 1u))) h++;
+        return (uint16_t)(sign | h);
+    }
+    uint32_t h = ((uint32_t)e << 10) | (man >> 13);
+    uint32_t rem = man & 0x1fffu;
+    if (rem > 0x1000u || (rem == 0x1000u && (h & 1u))) h++;
+    return (uint16_t)(sign | h);
+}
+
+/* value of a non-negative half in units of 2^-24 */
+static uint64_t half_units(uint16_t h)
+{
+    uint32_t e = (h >> 10) & 0x1fu, m = h & 0x3ffu;
+    if (e == 0) return m;
+    return (uint64_t)(1024u + m) << (e - 1);
+}
+
+static float gradient_of(const uint8_t *rgb, int W, int H, int D, int x, int y, int z)
+{
+    (void)D;
+    const uint8_t *c = rgb + 3 * IDX(x, y, z);
+    const uint8_t *nb[3] = { rgb + 3 * IDX(x > 0 ? x - 1 : 0, y, z),
+                             rgb + 3 * IDX(x, y > 0 ? y - 1 : 0, z),
+                             rgb + 3 * IDX(x, y, z > 0 ? z - 1 : 0) };
+    float g = 0.0f;
+    for (int k = 0; k < 3; k++) {
+        float s = (float)abs((int)nb[k][0] - (int)c[0]);
+        s = s + (float)abs((int)nb[k][1] - (int)c[1]);
+        s = s + (float)abs((int)nb[k][2] - (int)c[2]);
+        g = g + 0.33f * s;                                  /* derivative_t.gs:36,43,49 */
+    }
+    return g;
+}
+
+void orc_gradient_half(const uint8_t *rgb, int W, int H, int D, uint16_t *half_out)
+{
+    for (int z = 0; z < D; z++)
+        for (int y = 0; y < H; y++)
+            for (int x = 0; x < W; x++)
+                half_out[IDX(x, y, z)] = orc_float_to_half(gradient_of(rgb, W, H, D, x, y, z));
+}
+
+/* ======================================================================
+ * Gradient-density seed placement: GPU-AS/Image.cpp:350-620.
+ * ==================================================================== */
+static int mid_floor(float a, float b) { return (int)floor(0.5 * (double)(a + b)); } /* :375 */
+
+/* Per-axis cell ranges of the grid seeds (Image.cpp:360-443).  The ranges
+ * of a row/column depend on one index only, so the grid-cell id the
+ * reference writes voxel by voxel (last k wins, :449-468) is the largest
+ * (t, j, i) whose ranges contain the voxel. */
+static void axis_ranges(const float *grid4, const orc_grid_info *g, int W, int H, int D,
+                        int *xl, int *xr, int *yl, int *yr, int *zl, int *zr)
+{
+    int wN = g->wNum, hN = g->hNum, dN = g->dNum;
+    for (int i = 0; i < wN; i++) {
+        float c = grid4[4 * i];
+        xl[i] = i > 0 ? mid_floor(grid4[4 * (i - 1)], c) : 0;
+        xr[i] = i < wN - 1 ? mid_floor(grid4[4 * (i + 1)], c) : W - 1;
+    }
+    for (int j = 0; j < hN; j++) {
+        float c = grid4[4 * (j * wN) + 1];
+        yl[j] = j > 0 ? mid_floor(grid4[4 * ((j - 1) * wN) + 1], c) : 0;
+        yr[j] = j < hN - 1 ? mid_floor(grid4[4 * ((j + 1) * wN) + 1], c) : H - 1;
+    }
+    for (int t = 0; t < dN; t++) {
+        float c = grid4[4 * (t * wN * hN) + 2];
+        zl[t] = t > 0 ? mid_floor(grid4[4 * ((t - 1) * wN * hN) + 2], c) : 0;
+        zr[t] = t < dN - 1 ? mid_floor(grid4[4 * ((t + 1) * wN * hN) + 2], c) : D - 1;
+    }
+}
+
+void orc_grid_cell_tables(int W, int H, int D, const float *grid4, const orc_grid_info *g,
+                          int *xcell, int *ycell, int *zcell)
+{
+    int *xl = malloc(sizeof(int) * g->wNum), *xr = malloc(sizeof(int) * g->wNum);
+    int *yl = malloc(sizeof(int) * g->hNum), *yr = malloc(sizeof(int) * g->hNum);
+    int *zl = malloc(sizeof(int) * g->dNum), *zr = malloc(sizeof(int) * g->dNum);
+    axis_ranges(grid4, g, W, H, D, xl, xr, yl, yr, zl, zr);
+    for (int x = 0; x < W; x++) { xcell[x] = -1; for (int i = 0; i < g->wNum; i++) if (xl[i] <= x && x <= xr[i]) xcell[x] = i; }
+    for (int y = 0; y < H; y++) { ycell[y] = -1; for (int j = 0; j < g->hNum; j++) if (yl[j] <= y && y <= yr[j]) ycell[y] = j; }
+    for (int z = 0; z < D; z++) { zcell[z] = -1; for (int t = 0; t < g->dNum; t++) if (zl[t] <= z && z <= zr[t]) zcell[z] = t; }
+    free(xl); free(xr); free(yl); free(yr); free(zl); free(zr);
+}
+
+int orc_density_adjust(const uint8_t *rgb, int W, int H, int D, const float *grid4,
+                       const orc_grid_info *g, float *seeds4_out, float *density_out)
+{
+    int Kp = g->Kp;
+    int *xc = malloc(sizeof(int) * W), *yc = malloc(sizeof(int) * H), *zc = malloc(sizeof(int) * D);
+    orc_grid_cell_tables(W, H, D, grid4, g, xc, yc, zc);
+    int nslot = Kp + 64;
+    uint64_t *acc = calloc((size_t)nslot, sizeof(uint64_t));
+    /* density_grid.vs:23-30: cell id read from an R16F texture (:474), slot
+     * = id; the sum texture is cleared to 3.0 (Image.cpp:506-507). */
+    for (int z = 0; z < D; z++)
+        for (int y = 0; y < H; y++)
+            for (int x = 0; x < W; x++) {
+                if (xc[x] < 0 || yc[y] < 0 || zc[z] < 0) continue;
+                int k = (zc[z] * g->hNum + yc[y]) * g->wNum + xc[x];
+                uint16_t kh = orc_float_to_half((float)k);
+                int slot = (int)(half_units(kh) >> 24);
+                if (slot >= nslot) continue;
+                uint16_t gh = orc_float_to_half(gradient_of(rgb, W, H, D, x, y, z));
+                acc[slot] += half_units(gh);
+            }
+    float *dens = malloc(sizeof(float) * Kp), *len = malloc(sizeof(float) * Kp);
+    for (int i = 0; i < Kp; i++) {
+        uint64_t tot = acc[i] + ((uint64_t)3 << 24);
+        float res = (float)tot * 0x1p-24f;                 /* read back as float */
+        if (density_out) density_out[i] = res;
+        dens[i] = (float)(0.001 * (double)res);            /* :554 */
+    }
+    for (int i = 0; i < Kp; i++) len[i] = i == 0 ? dens[0] : dens[i] + len[i - 1]; /* :558-569 */
+    float interval = len[Kp - 1] / (float)(Kp + 1);        /* :570 */
+    int *xl = malloc(sizeof(int) * g->wNum), *xr = malloc(sizeof(int) * g->wNum);
+    int *yl = malloc(sizeof(int) * g->hNum), *yr = malloc(sizeof(int) * g->hNum);
+    int *zl = malloc(sizeof(int) * g->dNum), *zr = malloc(sizeof(int) * g->dNum);
+    axis_ranges(grid4, g, W, H, D, xl, xr, yl, yr, zl, zr);
+    int i = 0, j1 = 0, n = 0;
+    while (i < Kp) {                                       /* :586-616 */
+        float seed_in = (float)(i + 1) * interval;
+        if (seed_in < len[j1]) {
+            int c = j1 % g->wNum;                          /* seed_range1d of cell j1 */
+            int x1 = xl[c], x2 = xr[c];
+            float frac = j1 == 0 ? seed_in / len[j1]
+                                 : (seed_in - len[j1 - 1]) / (len[j1] - len[j1 - 1]);
+            float ax = floorf((float)x1 + (float)(x2 - x1) * frac);
+            seeds4_out[4 * n + 0] = (float)(ax + 0.5);
+            seeds4_out[4 * n + 1] = grid4[4 * j1 + 1];
+            seeds4_out[4 * n + 2] = grid4[4 * j1 + 2];
+            seeds4_out[4 * n + 3] = (float)i;
+            n++; i++;
+        } else {
+            j1++;
+            if (j1 == Kp) break;
+        }
+    }
+    free(xl); free(xr); free(yl); free(yr); free(zl); free(zr);
+    free(xc); free(yc); free(zc); free(acc); free(dens); free(len);
+    return n;
+}
+
+/* ======================================================================
+ * Metric tensor from flow: GPU-AS/Image.cpp:874-1009 (matrix_slover).
+ * Min-norm least squares (the reference calls Eigen BDCSVD::solve) is
+ * computed here with a one-sided Jacobi SVD in FP64 and Eigen's rank rule:
+ * keep singular values >= max(sigma_max * min(m,6) * FLT_EPSILON, FLT_MIN).
+ * ==================================================================== */
+#define SVD_SWEEPS 40
+
+static void lsq_minnorm(int m, double U[18][6], const double *b, double x[6])
+{
+    double V[6][6];
+    for (int r = 0; r < 6; r++) for (int c = 0; c < 6; c++) V[r][c] = r == c ? 1.0 : 0.0;
+    for (int sw = 0; sw < SVD_SWEEPS; sw++) {
+        int rot = 0;
+        for (int p = 0; p < 5; p++)
+            for (int q = p + 1; q < 6; q++) {
+                double al = 0.0, be = 0.0, ga = 0.0;
+                for (int i = 0; i < m; i++) {
+                    al = al + U[i][p] * U[i][p];
+                    be = be + U[i][q] * U[i][q];
+                    ga = ga + U[i][p] * U[i][q];
+                }
+                if (ga == 0.0) continue;
+                if (fabs(ga) <= 1e-15 * sqrt(al * be)) continue;
+                double zeta = (be - al) / (2.0 * ga);
+                double t = 1.0 / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+                if (zeta < 0.0) t = -t;
+                double c = 1.0 / sqrt(1.0 + t * t);
+                double s = c * t;
+                for (int i = 0; i < m; i++) {
+                    double up = U[i][p], uq = U[i][q];
+                    U[i][p] = c * up - s * uq;
+                    U[i][q] = s * up + c * uq;
+                }
+                for (int i = 0; i < 6; i++) {
+                    double vp = V[i][p], vq = V[i][q];
+                    V[i][p] = c * vp - s * vq;
+                    V[i][q] = s * vp + c * vq;
+                }
+                rot++;
+            }
+        if (!rot) break;
+    }
+    double sig[6], smax = 0.0;
+    for (int j = 0; j < 6; j++) {
+        double a = 0.0;
+        for (int i = 0; i < m; i++) a = a + U[i][j] * U[i][j];
+        sig[j] = sqrt(a);
+        if (sig[j] > smax) smax = sig[j];
+    }
+    double thr = smax * ((double)(m < 6 ? m : 6) * (double)FLT_EPSILON);
+    if (thr < (double)FLT_MIN) thr = (double)FLT_MIN;
+    for (int r = 0; r < 6; r++) x[r] = 0.0;
+    for (int j = 0; j < 6; j++) {
+        if (!(sig[j] >= thr)) continue;
+        double ub = 0.0;
+        for (int i = 0; i < m; i++) ub = ub + U[i][j] * b[i];
+        double coef = ub / (sig[j] * sig[j]);
+        for (int r = 0; r < 6; r++) x[r] = x[r] + V[r][j] * coef;
+    }
+}
+
+/* Symmetric 3x3 eigen-decomposition, cyclic Jacobi in FP64. */
+static void sym3_eig(const double Ain[3][3], double w[3], double V[3][3])
+{
+    double a[3][3];
+    memcpy(a, Ain, sizeof(a));
+    for (int r = 0; r < 3; r++) for (int c = 0; c < 3; c++) V[r][c] = r == c ? 1.0 : 0.0;
+    static const int P[3] = { 0, 0, 1 }, Q[3] = { 1, 2, 2 };
+    for (int sw = 0; sw < 50; sw++) {
+        int rot = 0;
+        for (int k = 0; k < 3; k++) {
+            int p = P[k], q = Q[k];
+            double apq = a[p][q];
+            if (apq == 0.0) continue;
+            if (fabs(apq) <= 1e-18 * (fabs(a[p][p]) + fabs(a[q][q]))) continue;
+            double th = (a[q][q] - a[p][p]) / (2.0 * apq);
+            double t = 1.0 / (fabs(th) + sqrt(th * th + 1.0));
+            if (th < 0.0) t = -t;
+            double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+            for (int r = 0; r < 3; r++) {
+                double ap = a[r][p], aq = a[r][q];
+                a[r][p] = c * ap - s * aq;
+                a[r][q] = s * ap + c * aq;
+            }
+            for (int r = 0; r < 3; r++) {
+                double ap = a[p][r], aq = a[q][r];
+                a[p][r] = c * ap - s * aq;
+                a[q][r] = s * ap + c * aq;
+            }
+            for (int r = 0; r < 3; r++) {
+                double vp = V[r][p], vq = V[r][q];
+                V[r][p] = c * vp - s * vq;
+                V[r][q] = s * vp + c * vq;
+            }
+            rot++;
+        }
+        if (!rot) break;
+    }
+    for (int k = 0; k < 3; k++) w[k] = a[k][k];
+}
+
+static void m6_to_3(const float M[6], double A[3][3])
+{
+    A[0][0] = M[0]; A[0][1] = M[1]; A[0][2] = M[2];
+    A[1][0] = M[1]; A[1][1] = M[3]; A[1][2] = M[4];
+    A[2][0] = M[2]; A[2][1] = M[4]; A[2][2] = M[5];
+}
+
+/* any eigenvalue < 0: Image.cpp:997-1006 */
+static int m6_negative(const float M[6])
+{
+    double A[3][3], w[3], V[3][3];
+    m6_to_3(M, A);
+    sym3_eig(A, w, V);
+    return (w[0] < 0.0 || w[1] < 0.0 || w[2] < 0.0) ? 1 : 0;
+}
+
+/* nearest PSD by clipping negative eigenvalues: Image.cpp:786-835 */
+static void m6_nearest_psd(const float M[6], float out[6])
+{
+    double A[3][3], w[3], V[3][3];
+    m6_to_3(M, A);
+    sym3_eig(A, w, V);
+    for (int k = 0; k < 3; k++) if (w[k] < 0.0) w[k] = 0.0;
+    static const int R[6] = { 0, 0, 0, 1, 1, 2 }, C[6] = { 0, 1, 2, 1, 2, 2 };
+    for (int e = 0; e < 6; e++) {
+        int i = R[e], j = C[e];
+        double acc = (V[i][0] * w[0]) * V[j][0];
+        acc = acc + (V[i][1] * w[1]) * V[j][1];
+        acc = acc + (V[i][2] * w[2]) * V[j][2];
+        out[e] = (float)acc;
+    }
+}
+
+static float round_half_up(float f) { return (float)floor((double)f + 0.5); } /* :901 */
+
+int orc_metric_solve(const float *fwd, const float *bwd, int W, int H, int D, float sx, float sy,
+                     int frame, float M[6])
+{
+    static const float expected_b[9] = { 3, 2, 3, 2, 1, 2, 3, 2, 3 };      /* :884 */
+    double A[18][6], b[18];
+    int m = 0, id_b = 0;
+    for (int oy = -1; oy < 2; oy++)
+        for (int ox = -1; ox < 2; ox++, id_b++) {
+            int nx = (int)sx + ox, ny = (int)sy + oy;
+            if (!(nx >= 0 && nx < W && ny >= 0 && ny < H)) continue;
+            long o = 2 * IDX(nx, ny, frame);
+            if (frame != D - 1) {                                            /* :898-913 */
+                float dx = (float)ox + round_half_up(fwd[o]);
+                float dy = (float)oy + round_half_up(fwd[o + 1]);
+                A[m][0] = (double)(dx * dx); A[m][1] = (double)(2.0f * dx * dy);
+                A[m][2] = (double)(2.0f * dx); A[m][3] = (double)(dy * dy);
+                A[m][4] = (double)(2.0f * dy); A[m][5] = 1.0;
+                b[m++] = expected_b[id_b];
+            }
+            if (frame != 0) {                                                /* :915-930 */
+                float dx = round_half_up(bwd[o]) + (float)ox;
+                float dy = round_half_up(bwd[o + 1]) + (float)oy;
+                A[m][0] = (double)(dx * dx); A[m][1] = (double)(2.0f * dx * dy);
+                A[m][2] = (double)(-2.0f * dx); A[m][3] = (double)(dy * dy);
+                A[m][4] = (double)(-2.0f * dy); A[m][5] = 1.0;
+                b[m++] = expected_b[id_b];
+            }
+        }
+    double x[6];
+    if (m == 0) { for (int k = 0; k < 6; k++) x[k] = 0.0; }
+    else lsq_minnorm(m, A, b, x);
+    for (int k = 0; k < 6; k++) M[k] = (float)x[k];
+    return m6_negative(M);
+}
+
+/* flow-angle filter of the plain reseed (Image.cpp:1406-1409); flow of the
+ * last frame is the 4x4 zero Mat (:664-667), read as zero everywhere. */
+static int angle_ok(const float *fwd, int W, int H, int D, int frame, int sx, int sy, int nx, int ny)
+{
+    float sfx = 0.0f, sfy = 0.0f, nfx = 0.0f, nfy = 0.0f;
+    if (frame != D - 1) {
+        long o = 2 * IDX(sx, sy, frame), p = 2 * IDX(nx, ny, frame);
+        sfx = fwd[o]; sfy = fwd[o + 1]; nfx = fwd[p]; nfy = fwd[p + 1];
+    }
+    float num = sfx * nfx + sfy * nfy;
+    double den = sqrt((double)sfx * (double)sfx + (double)sfy * (double)sfy) *
+                 sqrt((double)nfx * (double)nfx + (double)nfy * (double)nfy);
+    float c = (float)((double)num / den);
+    return (c >= ORC_FLOW_COS_MIN && c <= 1.0f) ? 1 : 0;
+}
+
+static const int R1X[8] = { -1, 0, 1, -1, 1, -1, 0, 1 }, R1Y[8] = { -1, -1, -1, 0, 0, 1, 1, 1 };
+static const int R2X[16] = { -2, -1, 0, 1, 2, -2, 2, -2, 2, -2, 2, -2, -1, 0, 1, 2 };
+static const int R2Y[16] = { -2, -2, -2, -2, -2, -1, -1, 0, 0, 1, 1, 2, 2, 2, 2, 2 };
+
+/* seed_matrix (Image.cpp:689-856, reseed == 0) and Ld_next_seeds_matrix
+ * (Image.cpp:1351-1534, reseed == 1; angle filter in the plain form only). */
+void orc_seed_metrics(const float *fwd, const float *bwd, int W, int H, int D, int Kp,
+                      const float *pos3, int reseed, int angle_filter, float *M6, int *kind)
+{
+    int filt = reseed && angle_filter;
+    for (int i = 0; i < Kp; i++) {
+        float fx = floorf(pos3[3 * i]), fy = floorf(pos3[3 * i + 1]);
+        int frame = (int)pos3[3 * i + 2];
+        float self[6], nb[6], sum[6] = { 0, 0, 0, 0, 0, 0 };
+        int k = 0;
+        if (!orc_metric_solve(fwd, bwd, W, H, D, fx, fy, frame, self)) {
+            memcpy(M6 + 6 * i, self, sizeof(self));
+        } else {
+            int n = 0;
+            for (int ring = 1; ring <= 2 && n == 0; ring++) {
+                int cnt = ring == 1 ? 8 : 16;
+                for (int t = 0; t < cnt; t++) {
+                    float nx = fx + (float)(ring == 1 ? R1X[t] : R2X[t]);
+                    float ny = fy + (float)(ring == 1 ? R1Y[t] : R2Y[t]);
+                    if (!(nx >= 0 && nx < W && ny >= 0 && ny < H)) continue;
+                    if (filt && !angle_ok(fwd, W, H, D, frame, (int)fx, (int)fy, (int)nx, (int)ny))
+                        continue;
+                    if (!orc_metric_solve(fwd, bwd, W, H, D, nx, ny, frame, nb)) {
+                        n++;
+                        for (int e = 0; e < 6; e++) sum[e] = sum[e] + nb[e];
+                    }
+                }
+                k = ring;
+            }
+            if (n > 0) {
+                for (int e = 0; e < 6; e++) M6[6 * i + e] = sum[e] / (float)n;
+            } else {
+                m6_nearest_psd(self, M6 + 6 * i);
+                k = 3;
+            }
+        }
+        if (kind) kind[i] = k;
+    }
+}
+
+/* ======================================================================
+ * JFA ladder: GPU-AS/Image.cpp:1055-1190.
+ * steps[] and the ratio multiplier of each pass; returns the pass count.
+ * ==================================================================== */
+int orc_ladder(int s, int full, int maxdim, int *steps, float *rmul, int cap)
+{
+    int n = 0;
+#define PUSH(st, rm) do { if (n < cap) { steps[n] = (st); rmul[n] = (rm); } n++; } while (0)
+    PUSH(1, 1.0f);                                                          /* :1096 */
+    if (!full) {
+        float st = (float)floor(0.5 * s);                                   /* :1057 */
+        while (st > 0) {                                                    /* :1105-1140 */
+            PUSH((int)st, 1.0f);
+            if ((int)st == 1) st = 0;
+            st = (float)floor(0.5 * st + 0.5);
+        }
+    } else {
+        int p = 1;
+        while (p * 2 <= maxdim) p *= 2;
+        for (; p >= 1; p /= 2) PUSH(p, 1.0f);
+    }
+    PUSH(2, 2.0f);                                                          /* :1143-1181 */
+    PUSH(1, 2.0f);
+#undef PUSH
+    return n;
+}
+
+/* ======================================================================
+ * Seed drawing: draw_seeds.vs / draw_next_seeds.vs write the seed record at
+ * the seed voxel, later seeds overwriting earlier ones (primitive order).
+ * ==================================================================== */
+void orc_draw_seeds(int W, int H, int D, int Kp, const float *pos3, int32_t *labels)
+{
+    long N = (long)W * H * D;
+    for (long v = 0; v < N; v++) labels[v] = -1;
+    for (int i = 0; i < Kp; i++) {
+        float px = pos3[3 * i], py = pos3[3 * i + 1], pz = pos3[3 * i + 2];
+        if (!(px >= 0.0f && py >= 0.0f && pz >= 0.0f)) continue;
+        int x = (int)px, y = (int)py, z = (int)pz;
+        if (x >= W || y >= H || z >= D) continue;
+        labels[IDX(x, y, z)] = i;
+    }
+}
+
+/* seed colour of the first iteration: LAB sampled at the seed voxel
+ * (draw_seeds.vs:23-24). */
+void orc_seed_lab(int W, int H, int D, int Kp, const float *pos3, const uint8_t *lab4, float *slab3)
+{
+    for (int i = 0; i < Kp; i++) {
+        int x = clampi((int)floorf(pos3[3 * i]), 0, W - 1);
+        int y = clampi((int)floorf(pos3[3 * i + 1]), 0, H - 1);
+        int z = clampi((int)floorf(pos3[3 * i + 2]), 0, D - 1);
+        const uint8_t *l = lab4 + 4 * IDX(x, y, z);
+        slab3[3 * i] = l[0]; slab3[3 * i + 1] = l[1]; slab3[3 * i + 2] = l[2];
+    }
+}
+
+/* ======================================================================
+ * One JFA pass: GPU-AS/shaders/flood.gs:26-182.
+ * ==================================================================== */
+static void jfa_voxel(int W, int H, int D, const int32_t *in, int32_t *out, const uint8_t *lab4,
+                      const float *pos3, const float *slab3, const float *M6, int step, float ratio,
+                      int x, int y, int z)
+{
+    float vx = (float)x + 0.5f, vy = (float)y + 0.5f, vz = (float)z + 0.5f;  /* flood.vs:18 */
+    const uint8_t *cl = lab4 + 4 * IDX(x, y, z);
+    float cL = cl[0], ca = cl[1], cb = cl[2];
+    float min_dist = 100000000.0f;                                            /* gs:63 */
+    int32_t best = -1;
+    int zs[3] = { z, clampi(z - step, 0, D - 1), clampi(z + step, 0, D - 1) }; /* gs:73,106,140 */
+    for (int sl = 0; sl < 3; sl++)
+        for (int oy = -1; oy <= 1; oy++)
+            for (int ox = -1; ox <= 1; ox++) {                                /* gs:36-46 */
+                int nx = clampi(x + ox * step, 0, W - 1), ny = clampi(y + oy * step, 0, H - 1);
+                int32_t l = in[IDX(nx, ny, zs[sl])];
+                if (l < 0) continue;                                          /* gs:77 */
+                const float *sp = pos3 + 3 * l, *sc = slab3 + 3 * l, *m = M6 + 6 * l;
+                float dx = vx - sp[0], dy = vy - sp[1], dz = vz - sp[2];
+                float p1 = (dx * dx) * m[0] + ((2.0f * dx) * dy) * m[1];           /* gs:85 */
+                p1 = p1 + ((2.0f * dx) * dz) * m[2];
+                float p2 = (dy * dy) * m[3] + ((2.0f * dy) * dz) * m[4];
+                p2 = p2 + (dz * dz) * m[5];
+                float pos = p1 + p2;
+                float eL = cL - sc[0], ea = ca - sc[1], eb = cb - sc[2];
+                float col = eL * eL + ea * ea;                                /* gs:89 */
+                col = col + eb * eb;
+                if (pos < 0.0f) pos = 0.0f;                                   /* gs:90-93 */
+                float dist = ratio * pos + col;                               /* gs:94 */
+                if (dist < min_dist) { min_dist = dist; best = l; }           /* gs:95-99 */
+            }
+    out[IDX(x, y, z)] = best;
+}
+
+void orc_jfa_pass(int W, int H, int D, const int32_t *in, int32_t *out, const uint8_t *lab4,
+                  const float *pos3, const float *slab3, const float *M6, int step, float ratio,
+                  int nthreads)
+{
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(nthreads > 0 ? nthreads : 1) if (nthreads > 1)
+#endif
+    for (int z = 0; z < D; z++)
+        for (int y = 0; y < H; y++)
+            for (int x = 0; x < W; x++)
+                jfa_voxel(W, H, D, in, out, lab4, pos3, slab3, M6, step, ratio, x, y, z);
+    (void)nthreads;
+}
+
+/* ======================================================================
+ * Centroid sums: centroids.vs:19-54 -- per label slot (label -1 -> slot
+ * Kp): sum of (x+.5, y+.5, z+.5), count, sum of LAB.  Kept exactly as
+ * integers: [0..2] = sum of (2x+1), (2y+1), (2z+1); [3] = count;
+ * [4..6] = sum of L, a, b.
+ * ==================================================================== */
+void orc_centroid_sums(int W, int H, int D, int Kp, const int32_t *labels, const uint8_t *lab4,
+                       int64_t *sums, int nthreads)
+{
+    long nsl = (long)(Kp + 1) * 7;
+    memset(sums, 0, sizeof(int64_t) * nsl);
+#ifdef _OPENMP
+    if (nthreads > 1) {
+#pragma omp parallel num_threads(nthreads)
+        {
+            int64_t *loc = calloc((size_t)nsl, sizeof(int64_t));
+#pragma omp for schedule(static)
+            for (int z = 0; z < D; z++)
+                for (int y = 0; y < H; y++)
+                    for (int x = 0; x < W; x++) {
+                        long v = IDX(x, y, z);
+                        int l = labels[v];
+                        int64_t *s = loc + 7L * (l < 0 ? Kp : l);
+                        s[0] += 2 * x + 1; s[1] += 2 * y + 1; s[2] += 2 * z + 1; s[3] += 1;
+                        s[4] += lab4[4 * v]; s[5] += lab4[4 * v + 1]; s[6] += lab4[4 * v + 2];
+                    }
+#pragma omp critical
+            for (long i = 0; i < nsl; i++) sums[i] += loc[i];
+            free(loc);
+        }
+        return;
+    }
+#endif
+    (void)nthreads;
+    for (int z = 0; z < D; z++)
+        for (int y = 0; y < H; y++)
+            for (int x = 0; x < W; x++) {
+                long v = IDX(x, y, z);
+                int l = labels[v];
+                int64_t *s = sums + 7L * (l < 0 ? Kp : l);
+                s[0] += 2 * x + 1; s[1] += 2 * y + 1; s[2] += 2 * z + 1; s[3] += 1;
+                s[4] += lab4[4 * v]; s[5] += lab4[4 * v + 1]; s[6] += lab4[4 * v + 2];
+            }
+}
+
+/* ======================================================================
+ * Reseed: aver_exception.vs:22-81 (run unless it is the last iteration).
+ * ==================================================================== */
+static void slot_mean(int W, int Kp, const int64_t *sums, int slot, float q[3])
+{
+    /* texel of a slot outside 0..Kp was cleared to zero (Image.cpp:1247-1248) */
+    if (slot < 0 || slot > Kp) { q[0] = q[1] = q[2] = 0.0f; return; }
+    (void)W;
+    const int64_t *s = sums + 7L * slot;
+    float cnt = (float)s[3];
+    for (int a = 0; a < 3; a++) {
+        float sf = (float)s[a] * 0.5f;
+        q[a] = ((int)cnt != 0) ? sf / cnt : sf;                    /* vs:37-40, 51-54 */
+    }
+}
+
+void orc_finalize(int W, int H, int D, int Kp, const int64_t *sums, const uint8_t *lab4,
+                  float *pos3, float *slab3)
+{
+    for (int id = 0; id < Kp; id++) {
+        const int64_t *s = sums + 7L * id;
+        if (s[3] != 0) {                                           /* vs:63-70 */
+            float cnt = (float)s[3];
+            for (int a = 0; a < 3; a++) {
+                float sf = (float)s[a] * 0.5f;
+                pos3[3 * id + a] = floorf(sf / cnt) + 0.5f;
+                slab3[3 * id + a] = (float)s[4 + a] / cnt;
+            }
+        } else {                                                   /* vs:25-62 */
+            /* id-1 for id 0 is texel (W-1, -1) clamped to row 0 = slot W-1 */
+            int s1 = id == 0 ? W - 1 : id - 1, s2 = id + 1;
+            float q1[3], q2[3];
+            slot_mean(W, Kp, sums, s1, q1);
+            slot_mean(W, Kp, sums, s2, q2);
+            for (int a = 0; a < 3; a++) pos3[3 * id + a] = floorf(0.5f * (q1[a] + q2[a])) + 0.5f;
+            int x = clampi((int)floorf(pos3[3 * id]), 0, W - 1);
+            int y = clampi((int)floorf(pos3[3 * id + 1]), 0, H - 1);
+            int z = clampi((int)floorf(pos3[3 * id + 2]), 0, D - 1);
+            const uint8_t *l = lab4 + 4 * IDX(x, y, z);
+            slab3[3 * id] = l[0]; slab3[3 * id + 1] = l[1]; slab3[3 * id + 2] = l[2];
+        }
+    }
+}
+
+/* ======================================================================
+ * Post-processing: check_dead_seeds + label_replace + sequence_label,
+ * GPU-AS/Image.cpp:1579-1778.  stats = {dead, neg_count, final_label_num}.
+ * ==================================================================== */
+int orc_postprocess(int W, int H, int D, int Kp, const int64_t *sums, int32_t *labels, int *stats)
+{
+    long N = (long)W * H * D;
+    int invalid = sums[7L * Kp + 3] > 0;                            /* :1590 */
+    int dead = 0, valid = 0;
+    int *dead_ids = malloc(sizeof(int) * (Kp + 1));
+    int *rank = malloc(sizeof(int) * (Kp + 1));
+    for (int i = 0; i < Kp; i++) {                                  /* :1603-1618 */
+        if (sums[7L * i + 3] < 1) { dead_ids[dead++] = i; rank[i] = -1; }
+        else rank[i] = valid++;
+    }
+    if (stats) { stats[0] = dead; stats[1] = (int)sums[7L * Kp + 3]; stats[2] = valid; }
+    if (dead >= 1 && dead <= 3) {                                   /* :1648-1674 */
+        int last = Kp;
+        for (int k = 0; k < dead; k++) {
+            last -= 1;
+            for (long v = 0; v < N; v++) if (labels[v] == last) labels[v] = dead_ids[k];
+        }
+    }
+    if (dead > 3) {                                                 /* :1727-1747 */
+        int l0 = labels[0];
+        int m = (l0 >= 0 && l0 < Kp && rank[l0] >= 0) ? rank[l0] : 0;
+        labels[0] = m;
+        for (long v = 1; v < N; v++) {
+            int l = labels[v];
+            if (l != l0 && l != -1) m = (l >= 0 && l < Kp && rank[l] >= 0) ? rank[l] : 0;
+            labels[v] = m;
+        }
+    } else if (invalid) {                                           /* :1750-1776 */
+        int last = 0;
+        if (labels[0] >= 0) last = labels[0];
+        for (long v = 1; v < N; v++) {
+            if (labels[v] != last) {
+                if (labels[v] == -1) labels[v] = last;
+                last = labels[v];
+            }
+        }
+    }
+    free(dead_ids); free(rank);
+    return dead;
+}
+
+/* final centroids of alive seeds (streamGPU-AS/Image.cpp:1563-1582) */
+void orc_final_centroids(int Kp, const int64_t *sums, float *seeds4_out, int *nalive)
+{
+    int n = 0;
+    for (int i = 0; i < Kp; i++) {
+        const int64_t *s = sums + 7L * i;
+        int area = (int)s[3];
+        if (area < 1) continue;
+        for (int a = 0; a < 3; a++) {
+            float sf = (float)s[a] * 0.5f;
+            seeds4_out[4 * n + a] = (float)(floorf(sf / (float)area) + 0.5);
+        }
+        seeds4_out[4 * n + 3] = (float)i;
+        n++;
+    }
+    *nalive = n;
+}
+
+/* ======================================================================
+ * One segmentation of a volume from given seeds: seed_matrix, RGB2LAB and
+ * the Lloyd loop (GPU-AS/Render.cpp:268-293; streamGPU-AS/Render.cpp:470-504).
+ * ==================================================================== */
+typedef struct seg_out {
+    int32_t *labels;   /* post-processed */
+    int32_t *raw;      /* last JFA output */
+    int64_t *sums;     /* (Kp+1)*7 of the last iteration */
+    float *pos3, *slab3, *M6;
+    int stats[3];
+} seg_out;
+
+static void segment(int W, int H, int D, int Kp, const float *init_pos3, int s, float ratio,
+                    int angle_filter, int iters, int full_ladder, const uint8_t *lab4,
+                    const float *fwd, const float *bwd, int nthreads, seg_out *o)
+{
+    long N = (long)W * H * D;
+    int steps[64]; float rmul[64];
+    int maxdim = W > H ? W : H; if (D > maxdim) maxdim = D;
+    int P = orc_ladder(s, full_ladder, maxdim, steps, rmul, 64);
+    int32_t *bufA = malloc(sizeof(int32_t) * N), *bufB = malloc(sizeof(int32_t) * N);
+    float *pos3 = o->pos3, *slab3 = o->slab3, *M6 = o->M6;
+    memcpy(pos3, init_pos3, sizeof(float) * 3 * Kp);
+    orc_seed_metrics(fwd, bwd, W, H, D, Kp, pos3, 0, angle_filter, M6, NULL);
+    orc_seed_lab(W, H, D, Kp, pos3, lab4, slab3);
+    int32_t *cur = NULL;
+    for (int it = 1; it <= iters; it++) {
+        if (it > 1) orc_seed_metrics(fwd, bwd, W, H, D, Kp, pos3, 1, angle_filter, M6, NULL);
+        orc_draw_seeds(W, H, D, Kp, pos3, bufA);
+        int32_t *src = bufA, *dst = bufB;
+        for (int p = 0; p < P; p++) {
+            float r = rmul[p] * ratio;
+            orc_jfa_pass(W, H, D, src, dst, lab4, pos3, slab3, M6, steps[p], r, nthreads);
+            int32_t *t = src; src = dst; dst = t;
+        }
+        cur = src;
+        orc_centroid_sums(W, H, D, Kp, cur, lab4, o->sums, nthreads);
+        if (it != iters) orc_finalize(W, H, D, Kp, o->sums, lab4, pos3, slab3);
+    }
+    memcpy(o->raw, cur, sizeof(int32_t) * N);
+    memcpy(o->labels, cur, sizeof(int32_t) * N);
+    orc_postprocess(W, H, D, Kp, o->sums, o->labels, o->stats);
+    free(bufA); free(bufB);
+}
+
+int orc_run_clip(const orc_params *p, const uint8_t *rgb, const float *fwd, const float *bwd,
+                 int32_t *labels_out, int32_t *raw_labels_out, float *seeds_out, int *info_out)
+{
+    int W = p->W, H = p->H, D = p->D;
+    long N = (long)W * H * D;
+    if (D < 2) return -1;
+    orc_grid_info g;
+    int Kp = orc_grid_seeds(W, H, D, p->K, p->middlebury, NULL, 0, &g);
+    if (Kp <= 0) return -2;
+    float *grid4 = malloc(sizeof(float) * 4 * Kp), *adj4 = malloc(sizeof(float) * 4 * Kp);
+    orc_grid_seeds(W, H, D, p->K, p->middlebury, grid4, Kp, &g);
+    int n = Kp;
+    if (p->density_adjust) n = orc_density_adjust(rgb, W, H, D, grid4, &g, adj4, NULL);
+    else memcpy(adj4, grid4, sizeof(float) * 4 * Kp);
+    if (n != Kp) { free(grid4); free(adj4); return -3; }
+    float *pos3 = malloc(sizeof(float) * 3 * Kp);
+    for (int i = 0; i < Kp; i++) for (int a = 0; a < 3; a++) pos3[3 * i + a] = adj4[4 * i + a];
+    uint8_t *lab4 = malloc((size_t)N * 4);
+    orc_rgb2lab(rgb, N, lab4);
+    seg_out o;
+    o.labels = labels_out;
+    o.raw = raw_labels_out ? raw_labels_out : malloc(sizeof(int32_t) * N);
+    o.sums = malloc(sizeof(int64_t) * 7 * (Kp + 1));
+    o.pos3 = malloc(sizeof(float) * 3 * Kp); o.slab3 = malloc(sizeof(float) * 3 * Kp);
+    o.M6 = malloc(sizeof(float) * 6 * Kp);
+    float compact = p->variant == 1 ? 6.0f : 8.0f;
+    segment(W, H, D, Kp, pos3, g.s, orc_ratio(g.s, compact), p->variant == 0, p->iters,
+            p->full_ladder, lab4, fwd, bwd, p->nthreads, &o);
+    if (seeds_out)
+        for (int i = 0; i < Kp; i++) {
+            for (int a = 0; a < 3; a++) seeds_out[12 * i + a] = o.pos3[3 * i + a];
+            for (int a = 0; a < 3; a++) seeds_out[12 * i + 3 + a] = o.slab3[3 * i + a];
+            for (int a = 0; a < 6; a++) seeds_out[12 * i + 6 + a] = o.M6[6 * i + a];
+        }
+    if (info_out) {
+        info_out[0] = Kp; info_out[1] = g.s; info_out[2] = o.stats[0];
+        info_out[3] = o.stats[1]; info_out[4] = o.stats[2];
+    }
+    if (!raw_labels_out) free(o.raw);
+    free(o.sums); free(o.pos3); free(o.slab3); free(o.M6);
+    free(grid4); free(adj4); free(pos3); free(lab4);
+    return Kp;
+}
+
+/* ======================================================================
+ * Streaming form: streamGPU-AS/Render.cpp:156-569.
+ * info_out = {blocks, seeds_num_placed}.
+ * ==================================================================== */
+int orc_stream_blocks(int D_all, int block_size, int *intervals, int cap)
+{
+    int one_third = block_size / 3, two_third = 2 * block_size / 3;     /* :200-201 */
+    int n = 0, last_end = block_size, done = 0;
+#define PUSHB(a, b) do { if (n + 1 < cap) { intervals[n] = (a); intervals[n + 1] = (b); } n += 2; } while (0)
+    if (D_all < block_size + one_third) { PUSHB(0, D_all); done = 1; }
+    else {
+        PUSHB(0, last_end);
+        while (last_end + two_third < D_all) {
+            if (D_all - last_end - two_third < one_third) { PUSHB(last_end - one_third, D_all); done = 1; }
+            else PUSHB(last_end - one_third, last_end + two_third);
+            last_end += two_third;
+        }
+        if (!done) PUSHB(last_end - one_third, D_all);
+    }
+#undef PUSHB
+    return n / 2;
+}
+
+int orc_run_stream(const orc_stream_params *p, const uint8_t *rgb, const float *fwd,
+                   const float *bwd, int32_t *labels_all, int *info_out)
+{
+    int W = p->W, H = p->H, Dall = p->D_all, bs = p->block_size > 0 ? p->block_size : 30;
+    long slice = (long)W * H;
+    int seeds100 = p->seeds_num_100 > 0 ? p->seeds_num_100 : p->K_video * 100 / Dall; /* :157 */
+    int iv[512];
+    int nb = orc_stream_blocks(Dall, bs, iv, 512);
+    if (nb > 256) return -1;
+    int one_third = bs / 3;
+    int two_third = bs - one_third;                                      /* post_and_next :516 */
+    float *kept = NULL; int kept_num = 0;
+    int *prev_map = NULL; int prev_map_n = 0;
+    int placed = 0;
+    for (int b = 0; b < nb; b++) {
+        int start = iv[2 * b], end = iv[2 * b + 1], Db = end - start;
+        long Nb = slice * Db;
+        int seeds_num;
+        if (b == 0) seeds_num = nb > 1 ? seeds100 * (Db - 10) / 100 : seeds100 * Db / 100; /* :351-356 */
+        else seeds_num = seeds100 * (Db - 10) / 100;                    /* :394 */
+        const uint8_t *brgb = rgb + 3 * slice * start;
+        const float *bf = fwd + 2 * slice * start, *bb = bwd + 2 * slice * start;
+        orc_grid_info g;
+        int Kn = orc_grid_seeds(W, H, Db, seeds_num, 0, NULL, 0, &g);
+        if (Kn <= 0) return -2;
+        float *grid4 = malloc(sizeof(float) * 4 * Kn), *adj4 = malloc(sizeof(float) * 4 * Kn);
+        orc_grid_seeds(W, H, Db, seeds_num, 0, grid4, Kn, &g);
+        int na = orc_density_adjust(brgb, W, H, Db, grid4, &g, adj4, NULL);
+        int Kp = kept_num + na;
+        float *pos3 = malloc(sizeof(float) * 3 * Kp);
+        int *map = malloc(sizeof(int) * Kp);
+        int added_id = placed;
+        for (int i = 0; i < Kp; i++) {                                   /* :438-460 */
+            if (i < kept_num) {
+                for (int a = 0; a < 3; a++) pos3[3 * i + a] = kept[4 * i + a];
+                int old = (int)kept[4 * i + 3];
+                map[i] = (b > 0 && old >= 0 && old < prev_map_n) ? prev_map[old] : 0;
+            } else {
+                int j = i - kept_num;
+                for (int a = 0; a < 3; a++) pos3[3 * i + a] = adj4[4 * j + a];
+                map[i] = b == 0 ? i : added_id++;
+            }
+        }
+        uint8_t *lab4 = malloc((size_t)Nb * 4);
+        orc_rgb2lab(brgb, Nb, lab4);
+        seg_out o;
+        o.labels = malloc(sizeof(int32_t) * Nb); o.raw = malloc(sizeof(int32_t) * Nb);
+        o.sums = malloc(sizeof(int64_t) * 7 * (Kp + 1));
+        o.pos3 = malloc(sizeof(float) * 3 * Kp); o.slab3 = malloc(sizeof(float) * 3 * Kp);
+        o.M6 = malloc(sizeof(float) * 6 * Kp);
+        segment(W, H, Db, Kp, pos3, g.s, orc_ratio(g.s, 6.0f), 0, p->iters, 0, lab4, bf, bb,
+                p->nthreads, &o);
+        float *info = malloc(sizeof(float) * 4 * Kp);
+        int nal = 0;
+        orc_final_centroids(Kp, o.sums, info, &nal);
+        placed += nal - kept_num;                                         /* :514 */
+        int done_frames = Db;
+        free(kept); kept = NULL; kept_num = 0;
+        if (b < nb - 1) {                                                 /* :519-557 */
+            kept = malloc(sizeof(float) * 4 * (nal > 0 ? nal : 1));
+            for (int i = 0; i < nal; i++) {
+                float z = info[4 * i + 2];
+                if (z > (float)(bs - one_third)) {
+                    float nz = z - (float)two_third;
+                    if (nz < 1) nz = 1.5f;
+                    kept[4 * kept_num + 0] = info[4 * i + 0];
+                    kept[4 * kept_num + 1] = info[4 * i + 1];
+                    kept[4 * kept_num + 2] = nz;
+                    kept[4 * kept_num + 3] = info[4 * i + 3];
+                    kept_num++;
+                }
+            }
+            done_frames = Db - one_third;
+        }
+        long done = slice * done_frames;                                  /* :559-563 */
+        for (long i = 0; i < done; i++) {
+            int l = o.labels[i];
+            labels_all[slice * start + i] = (l >= 0 && l < Kp) ? map[l] : 0;
+        }
+        free(prev_map); prev_map = map; prev_map_n = Kp;
+        free(info); free(o.labels); free(o.raw); free(o.sums); free(o.pos3); free(o.slab3);
+        free(o.M6); free(lab4); free(pos3); free(grid4); free(adj4);
+    }
+    free(kept); free(prev_map);
+    if (info_out) { info_out[0] = nb; info_out[1] = placed; }
+    return nb;
+}

@@ -1,0 +1,214 @@
+"""CUDA path (libasv through its C ABI) against the CPU restatement.
+
+The bar is bit-exact: the kernels evaluate every float operation in the
+restatement's order and the blend-order sums are exact integers on both
+sides, so labels, seeds, metrics and sums must be identical.
+"""
+import numpy as np
+import pytest
+
+from conftest import mismatch, small_clip
+
+pytestmark = pytest.mark.gpu
+
+
+def _gpu_clip(asv, rgb, fwd, bwd, K, iters, **cfg):
+    img = asv.Image(lloyd_iters=iters, **cfg)
+    img.init_gpu(rgb, K)
+    img.upload_flow(fwd, bwd)
+    img.initialization()
+    img.seed_matrix()
+    img.RGB2LAB()
+    return img
+
+
+def test_lab_exhaustive(asv, orc):
+    """RGB -> LAB on all 2^24 RGB8 values."""
+    v = np.arange(1 << 24, dtype=np.uint32)
+    rgb = np.stack([(v >> 16) & 255, (v >> 8) & 255, v & 255], -1).astype(np.uint8)
+    rgb = rgb.reshape(2, 2048, 4096, 3)
+    img = asv.Image(lloyd_iters=1)
+    img.init_gpu(rgb, 1000)
+    img.RGB2LAB()
+    got = img.lab()
+    want = orc.rgb2lab(rgb)
+    bad = np.nonzero((got[..., :3] != want[..., :3]).any(-1).ravel())[0]
+    assert bad.size == 0, f"{bad.size} RGB values differ, first {bad[:10]}"
+
+
+@pytest.mark.parametrize("W,H,D,K", [(64, 48, 12, 60), (37, 23, 9, 25), (240, 160, 30, 200),
+                                     (96, 64, 20, 400), (50, 50, 5, 3000)])
+def test_density_seeds(asv, orc, W, H, D, K):
+    rgb, fwd, bwd = small_clip(asv, W, H, D, seed=W * H + K)
+    grid, g = orc.grid_seeds(W, H, D, K)
+    want, _ = orc.density_adjust(rgb, grid, g)
+    img = _gpu_clip(asv, rgb, fwd, bwd, K, 2)
+    assert img.info().Kp == g.Kp
+    got = img.seeds()
+    assert mismatch(got[:, :3], want[:, :3]) == 0
+
+
+@pytest.mark.parametrize("W,H,D,K,jit", [(64, 48, 12, 60, 0.0), (80, 60, 16, 150, 0.5),
+                                         (33, 41, 7, 40, 0.5)])
+def test_seed_matrix(asv, orc, W, H, D, K, jit):
+    rgb, fwd, bwd = small_clip(asv, W, H, D, seed=3 * W + K, jitter=jit)
+    img = _gpu_clip(asv, rgb, fwd, bwd, K, 2)
+    s = img.seeds()
+    want, kind = orc.seed_metrics(fwd, bwd, s[:, :3], 0, 1)
+    assert mismatch(s[:, 6:12].view(np.uint32), want.view(np.uint32)) == 0
+
+
+def test_seed_matrix_fallbacks(asv, orc):
+    """Random flow makes non-PSD solves: exercise the 1-ring, 2-ring and nearest-PSD paths."""
+    W, H, D, K = 48, 40, 10, 120
+    rng = np.random.default_rng(5)
+    rgb = rng.integers(0, 256, (D, H, W, 3), dtype=np.uint8)
+    fwd = rng.normal(0, 2.0, (D, H, W, 2)).astype(np.float32)
+    bwd = rng.normal(0, 2.0, (D, H, W, 2)).astype(np.float32)
+    img = _gpu_clip(asv, rgb, fwd, bwd, K, 2)
+    s = img.seeds()
+    want, kind = orc.seed_metrics(fwd, bwd, s[:, :3], 0, 1)
+    assert set(np.unique(kind)) >= {0, 1}
+    assert mismatch(s[:, 6:12].view(np.uint32), want.view(np.uint32)) == 0
+
+
+@pytest.mark.parametrize("step", [1, 2, 3, 8, 11])
+def test_jfa_single_pass(asv, orc, step):
+    W, H, D, K = 70, 45, 14, 80
+    rgb, fwd, bwd = small_clip(asv, W, H, D, seed=11)
+    img = _gpu_clip(asv, rgb, fwd, bwd, K, 2)
+    lab4 = img.lab()
+    rng = np.random.default_rng(step)
+    kp = img.info().Kp
+    seeds = np.zeros((kp, 12), np.float32)
+    seeds[:, 0] = rng.integers(0, W, kp) + 0.5
+    seeds[:, 1] = rng.integers(0, H, kp) + 0.5
+    seeds[:, 2] = rng.integers(0, D, kp) + 0.5
+    seeds[:, 3:6] = rng.uniform(0, 255, (kp, 3)).astype(np.float32)
+    A = rng.normal(0, 1, (kp, 3, 3)).astype(np.float32)
+    M = np.einsum("kij,kil->kjl", A, A)
+    seeds[:, 6:12] = M[:, [0, 0, 0, 1, 1, 2], [0, 1, 2, 1, 2, 2]]
+    seeds[: kp // 8, 6:12] *= -1.0          # some non-PSD tables (clamped distance)
+    img.set_seeds(seeds)
+    labels = rng.integers(-1, kp, (D, H, W)).astype(np.int32)
+    ratio = 0.1234567
+    got = img.jfa_pass(labels, step, ratio)
+    want = orc.jfa_pass(labels, lab4, seeds, step, ratio)
+    assert mismatch(got, want) == 0
+
+
+CASES = [
+    # W, H, D, K, iters, variant, full_ladder, density
+    (64, 48, 12, 60, 4, 0, 0, 1),
+    (64, 48, 12, 60, 4, 1, 0, 1),
+    (64, 48, 12, 60, 3, 0, 1, 1),
+    (64, 48, 12, 60, 3, 0, 0, 0),
+    (37, 23, 9, 25, 5, 0, 0, 1),
+    (120, 80, 15, 300, 3, 0, 0, 1),
+    (40, 30, 6, 400, 3, 0, 0, 1),       # many seeds for the volume: dead seeds, -1 fill
+    (17, 9, 3, 2, 3, 0, 0, 1),          # two seeds
+]
+
+
+@pytest.mark.parametrize("W,H,D,K,iters,variant,full,dens", CASES)
+def test_clip_bit_exact(asv, orc, W, H, D, K, iters, variant, full, dens):
+    rgb, fwd, bwd = small_clip(asv, W, H, D, seed=W + 7 * K, jitter=0.5, drift=2.0)
+    img = _gpu_clip(asv, rgb, fwd, bwd, K, iters, variant=variant, full_ladder=full,
+                    density_adjust=dens)
+    img.run_lloyd()
+    labels, raw, seeds, info = orc.run_clip(rgb, fwd, bwd, K, iters=iters, variant=variant,
+                                            full_ladder=full, density_adjust=dens)
+    assert mismatch(img.raw_labels(), raw) == 0
+    assert mismatch(img.labels(), labels) == 0
+    assert mismatch(img.seeds().view(np.uint32), seeds.view(np.uint32)) == 0
+    gi = img.info()
+    assert (gi.dead, gi.neg_count, gi.final_label_num) == (info["dead"], info["neg"],
+                                                           info["final_label_num"])
+
+
+def test_clip_240x160x30(asv, orc):
+    """The 240x160x30 K=200 10-iteration workload, bit-exact end to end."""
+    from anisotropic_supervoxel_gb300 import workloads
+    w = workloads.CLIP_240x160x30
+    rgb, fwd, bwd = workloads.make_clip(w)
+    img = _gpu_clip(asv, rgb, fwd, bwd, w["K"], w["iters"])
+    img.run_lloyd()
+    labels, raw, seeds, info = orc.run_clip(rgb, fwd, bwd, w["K"], iters=w["iters"], nthreads=8)
+    assert img.info().Kp == 187
+    assert mismatch(img.raw_labels(), raw) == 0
+    assert mismatch(img.labels(), labels) == 0
+
+
+def test_post_processing_cases(asv, orc):
+    """Dead-seed relabel (<= 3 and > 3 dead) and the -1 forward fills on crafted volumes."""
+    W, H, D, K = 40, 30, 8, 60
+    rgb, fwd, bwd = small_clip(asv, W, H, D, seed=99)
+    img = _gpu_clip(asv, rgb, fwd, bwd, K, 2)
+    kp = img.info().Kp
+    lab4 = img.lab()
+    rng = np.random.default_rng(1)
+    base = rng.integers(0, kp, (D, H, W)).astype(np.int32)
+    cases = []
+    a = base.copy(); a[rng.random(a.shape) < 0.05] = -1; cases.append(a)          # -1 only
+    b = a.copy(); b[0, 0, 0] = -1; cases.append(b)                                 # -1 at voxel 0
+    c = base.copy(); c[np.isin(c, [3, kp - 1])] = 5; c[rng.random(c.shape) < 0.02] = -1
+    cases.append(c)                                                                # 2 dead (incl. last)
+    d = base.copy(); d[np.isin(d, [0, 1, 2, 7, 9, 11])] = 4; d[0, 0, :3] = -1
+    cases.append(d)                                                                # 6 dead, -1 first
+    e = base.copy(); e[np.isin(e, [kp - 3, kp - 2, kp - 1])] = 0; cases.append(e)  # 3 dead at the end
+    for raw in cases:
+        got = img.check_dead_seeds_host(raw)
+        sums = orc.centroid_sums(raw, lab4, kp)
+        want, _ = orc.postprocess(raw, sums, kp)
+        assert mismatch(got, want) == 0
+        assert mismatch(img.sums(), sums) == 0
+
+
+def test_graph_eager_and_stage_calls_agree(asv):
+    rgb, fwd, bwd = small_clip(asv, 64, 48, 12, seed=5, jitter=0.5)
+    outs = []
+    for use_graph in (1, 0):
+        img = _gpu_clip(asv, rgb, fwd, bwd, 60, 4, use_graph=use_graph)
+        img.run_lloyd()
+        img.run_lloyd()          # replay: same initial seeds, same result
+        outs.append(img.labels())
+    img = _gpu_clip(asv, rgb, fwd, bwd, 60, 4)
+    img.Ld_first_init()
+    for it in range(1, 5):
+        if it > 1:
+            img.Ld_next_seeds_matrix(it)
+        img.flood(it)
+        img.centroids_next_seeds(it)
+    outs.append(img.check_dead_seeds())
+    assert mismatch(outs[0], outs[1]) == 0
+    assert mismatch(outs[0], outs[2]) == 0
+
+
+def test_clip_320x240x85_properties(asv, orc):
+    """Full-size 320x240x85 K=1000 15-iteration workload: size-independent properties
+    (exact sums, every voxel counted once, determinism), plus bit-exact parity on the
+    half-scale clip."""
+    from anisotropic_supervoxel_gb300 import workloads
+    w = workloads.CLIP_320x240x85
+    rgb, fwd, bwd = workloads.make_clip(w)
+    img = _gpu_clip(asv, rgb, fwd, bwd, w["K"], w["iters"])
+    img.run_lloyd()
+    raw1, lab1 = img.raw_labels(), img.labels()
+    img.run_lloyd()
+    assert mismatch(img.raw_labels(), raw1) == 0
+    kp = img.info().Kp
+    assert kp == 936
+    sums = img.sums()
+    assert sums[:, 3].sum() == raw1.size
+    want = orc.centroid_sums(raw1, img.lab(), kp, nthreads=8)
+    assert mismatch(sums, want) == 0
+    assert lab1.min() >= -1 and lab1.max() < kp
+    assert (lab1.ravel()[1:] >= 0).all()
+    # half scale, bit-exact
+    rgb, fwd, bwd = workloads.make_clip(w, scale=0.5)
+    D, H, W, _ = rgb.shape
+    img = _gpu_clip(asv, rgb, fwd, bwd, w["K"] // 4, w["iters"])
+    img.run_lloyd()
+    labels, raw, seeds, info = orc.run_clip(rgb, fwd, bwd, w["K"] // 4, iters=w["iters"], nthreads=8)
+    assert mismatch(img.raw_labels(), raw) == 0
+    assert mismatch(img.labels(), labels) == 0
