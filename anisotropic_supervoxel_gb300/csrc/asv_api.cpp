@@ -756,8 +756,12 @@ asv_status asv_set_seeds(asv_ctx *ctx, const float *in, int Kp)
     int off = ctx->seg[0].seed_off;
     std::vector<float4> p(Kp), c(Kp);
     std::vector<float> m((size_t)Kp * 8, 0.f);
+    const SegHost &h = ctx->seg[0];
     for (int i = 0; i < Kp; i++) {
         const float *o = in + 12 * (size_t)i;
+        if (!(o[0] >= 0.f && o[0] < (float)h.W && o[1] >= 0.f && o[1] < (float)h.H && o[2] >= 0.f &&
+              o[2] < (float)h.D))
+            return fail(ctx, ASV_ERR_BAD_ARG, "seed position outside the volume");
         p[i] = make_float4(o[0], o[1], o[2], (float)i);
         c[i] = make_float4(o[3], o[4], o[5], 0.f);
         for (int e = 0; e < 6; e++) m[8 * (size_t)i + e] = o[6 + e];
@@ -801,6 +805,8 @@ asv_status asv_check_dead_seeds_host(asv_ctx *ctx, const int32_t *raw_in, int32_
     if (ctx->seg.size() != 1 || !ctx->have_lab)
         return fail(ctx, ASV_ERR_STATE, "need a clip and its LAB volume");
     const SegDesc &s = ctx->sd[0];
+    for (long long v = 0; v < s.nvox; v++)
+        if (raw_in[v] < -1 || raw_in[v] >= s.Kp) return fail(ctx, ASV_ERR_BAD_ARG, "label outside [-1, Kp)");
     int32_t *fin = (s.final_buf ? ctx->d.labB : ctx->d.labA) + s.vox_off;
     CK(cudaMemcpyAsync(fin, raw_in, 4 * (size_t)s.nvox, cudaMemcpyHostToDevice, ctx->st));
     do_centroids(ctx, false);

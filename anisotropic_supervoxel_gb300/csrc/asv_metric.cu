@@ -185,6 +185,8 @@ __device__ int asv_angle_ok(const float2 *__restrict__ fwd, int W, int H, int D,
 {
     float sfx = 0.0f, sfy = 0.0f, nfx = 0.0f, nfy = 0.0f;
     if (frame != D - 1) {
+        sx = min(max(sx, 0), W - 1);
+        sy = min(max(sy, 0), H - 1);
         float2 a = __ldg(fwd + ((long long)frame * H + sy) * W + sx);
         float2 c = __ldg(fwd + ((long long)frame * H + ny) * W + nx);
         sfx = a.x; sfy = a.y; nfx = c.x; nfy = c.y;
@@ -220,7 +222,7 @@ __global__ void k_metric_self(AsvDev d, int reseed)
     const SegDesc &S = d.segs[r.si];
     float4 p = reseed ? d.pos[r.g] : d.pos0[r.g];
     float fx = floorf(p.x), fy = floorf(p.y);
-    int frame = (int)p.z;
+    int frame = min(max((int)p.z, 0), S.D - 1);   // positions are inside; keep reads in bounds
     float M[6];
     int neg = asv_metric_solve(d.fwd + S.vox_off, d.bwd + S.vox_off, S.W, S.H, S.D, fx, fy, frame, M);
     for (int e = 0; e < 6; e++) d.Mself[8 * r.g + e] = M[e];
@@ -238,7 +240,7 @@ __global__ void k_metric_ring(AsvDev d, int reseed)
     const SegDesc &S = d.segs[r.si];
     float4 p = reseed ? d.pos[g] : d.pos0[g];
     float fx = floorf(p.x), fy = floorf(p.y);
-    int frame = (int)p.z;
+    int frame = min(max((int)p.z, 0), S.D - 1);
     float nx = fx + (float)c_ringx[t], ny = fy + (float)c_ringy[t];
     if (!(nx >= 0 && nx < S.W && ny >= 0 && ny < S.H)) { *ok = 0; return; }
     const float2 *fwd = d.fwd + S.vox_off, *bwd = d.bwd + S.vox_off;

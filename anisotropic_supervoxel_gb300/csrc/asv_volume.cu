@@ -253,7 +253,7 @@ __global__ void k_draw(AsvDev d)
 __device__ __forceinline__ void asv_jfa_voxel(const int32_t *__restrict__ in, int32_t *__restrict__ out,
                                               const uchar4 *__restrict__ lab,
                                               const float4 *__restrict__ tab, int W, int H, int D,
-                                              int x, int y, int z, int step, float ratio)
+                                              int Kp, int x, int y, int z, int step, float ratio)
 {
     const long long sl = (long long)W * H;
     const float vx = (float)x + 0.5f, vy = (float)y + 0.5f, vz = (float)z + 0.5f;
@@ -278,7 +278,7 @@ __device__ __forceinline__ void asv_jfa_voxel(const int32_t *__restrict__ in, in
 #pragma unroll
     for (int k = 0; k < 27; k++) {
         const int32_t l = cand[k];
-        if (l < 0 || l == best || l == last) continue;
+        if (l < 0 || l >= Kp || l == best || l == last) continue;
         last = l;
         const float4 t0 = __ldg(tab + 3 * l), t1 = __ldg(tab + 3 * l + 1), t2 = __ldg(tab + 3 * l + 2);
         const float dx = vx - t0.x, dy = vy - t0.y, dz = vz - t0.z;
@@ -311,7 +311,7 @@ __global__ void __launch_bounds__(256) k_jfa(AsvDev d, int pass, const int32_t *
         const int x = tx * ASV_TILE_X + lx, y = ty * ASV_TILE_Y + ly;
         if (x >= S.W || y >= S.H) continue;
         asv_jfa_voxel(in + S.vox_off, out + S.vox_off, d.lab + S.vox_off, d.jtab + 3 * S.seed_off,
-                      S.W, S.H, S.D, x, y, z, S.steps[pass], S.ratio[pass]);
+                      S.W, S.H, S.D, S.Kp, x, y, z, S.steps[pass], S.ratio[pass]);
     }
 }
 
@@ -327,8 +327,8 @@ __global__ void __launch_bounds__(256) k_jfa_single(AsvDev d, const int32_t *__r
         const int ty = rest % S.tiles_y, z = rest / S.tiles_y;
         const int x = tx * ASV_TILE_X + lx, y = ty * ASV_TILE_Y + ly;
         if (x >= S.W || y >= S.H) continue;
-        asv_jfa_voxel(in, out, d.lab + S.vox_off, d.jtab + 3 * S.seed_off, S.W, S.H, S.D, x, y, z,
-                      step, ratio);
+        asv_jfa_voxel(in, out, d.lab + S.vox_off, d.jtab + 3 * S.seed_off, S.W, S.H, S.D, S.Kp,
+                      x, y, z, step, ratio);
     }
 }
 
@@ -354,7 +354,7 @@ __global__ void __launch_bounds__(256) k_centroids(AsvDev d)
         unsigned q[7] = { 0, 0, 0, 0, 0, 0, 0 };
         if (v < S.nvox) {
             int l = __ldg(lbl + v);
-            key = l < 0 ? S.Kp : l;
+            key = (l < 0 || l >= S.Kp) ? S.Kp : l;   // out-of-range ids (never produced) count as -1
             int x = (int)(v % W);
             long long r = v / W;
             int y = (int)(r % H), z = (int)(r / H);
