@@ -212,6 +212,8 @@ asv_status asv_prepare_segment(asv_ctx *ctx, int W, int H, int D, int K, SegHost
 {
     if (W < 1 || H < 1 || D < 2 || W > 4096 || H > 4096 || D > 4096 || K < 1)
         return fail(ctx, ASV_ERR_BAD_ARG, "need 1 <= W,H <= 4096, 2 <= D <= 4096, K >= 1");
+    if ((long long)W * H * D >= (1LL << 31))
+        return fail(ctx, ASV_ERR_BAD_ARG, "a clip holds fewer than 2^31 voxels");
     sh->W = W; sh->H = H; sh->D = D; sh->K = K;
     if (grid_seeds(W, H, D, K, ctx->cfg.middlebury, &sh->g, &sh->grid) <= 0)
         return fail(ctx, ASV_ERR_BAD_ARG, "K too small for the seed grid (no column or row)");
@@ -512,6 +514,17 @@ asv_status asv_init_gpu(asv_ctx *ctx, const uint8_t *rgb, int W, int H, int D, i
     if (!ctx) return ASV_ERR_BAD_ARG;
     if (!rgb) return fail(ctx, ASV_ERR_BAD_ARG, "rgb is NULL");
     cudaSetDevice(ctx->cfg.device);
+    if (ctx->seg.size() == 1 && !ctx->allocs.empty()) {
+        const SegHost &o = ctx->seg[0];
+        if (o.W == W && o.H == H && o.D == D && o.K == K) {
+            // same clip shape: keep the device layout and the captured graph
+            CK(cudaMemcpyAsync(ctx->d.rgb, rgb, (size_t)W * H * D * 3, cudaMemcpyHostToDevice, ctx->st));
+            ctx->have_rgb = true;
+            ctx->have_flow = ctx->have_pos0 = ctx->have_M0 = ctx->have_lab = false;
+            ctx->seeded = ctx->ran = false;
+            return ASV_OK;
+        }
+    }
     SegHost h;
     asv_status s = asv_prepare_segment(ctx, W, H, D, K, &h);
     if (s != ASV_OK) return s;

@@ -10,29 +10,47 @@
 // FLT_MIN)).  A non-PSD M falls back to the mean of the PSD metrics of the
 // 1-ring, then 2-ring neighbours, then to the nearest PSD matrix.
 //
-// Three launches per solve: k_metric_self (one thread per seed),
-// k_metric_ring (one thread per seed and neighbour, only for non-PSD seeds),
-// k_metric_combine (one thread per seed).  Compiled with -fmad=false.
+// One warp per solve: lane i holds row i of the system; column dot products
+// are accumulated row by row in order (shuffles), so every lane computes the
+// same scalars with the same operation sequence as a sequential solver.
+// Launches: k_metric_self (a warp per seed), k_metric_ring (a warp per seed
+// and neighbour, only for non-PSD seeds), k_metric_combine (a thread per
+// seed).  Compiled with -fmad=false.
 #include "asv_common.cuh"
 
 #include <float.h>
 
 #define SVD_SWEEPS 40
+#define FULL 0xffffffffu
 
-__device__ void asv_lsq_minnorm(int m, double (*U)[6], const double *b, double x[6])
+// sequential sum over rows 0..m-1 of a per-lane value
+__device__ __forceinline__ double asv_row_sum(double v, int m)
 {
-    double V[6][6];
-    for (int r = 0; r < 6; r++)
-        for (int c = 0; c < 6; c++) V[r][c] = r == c ? 1.0 : 0.0;
+    double a = 0.0;
+    for (int i = 0; i < m; i++) a = a + __shfl_sync(FULL, v, i);
+    return a;
+}
+
+// min-norm least squares; u = this lane's row (zero beyond m), bl = its rhs.
+// Returns x[0..5] on every lane.
+__device__ void asv_lsq_minnorm_warp(int m, double u[6], double bl, double x[6])
+{
+    const int lane = threadIdx.x & 31;
+    double v[6];
+#pragma unroll
+    for (int c = 0; c < 6; c++) v[c] = lane == c ? 1.0 : 0.0;   // lane r < 6 holds row r of V
     for (int sw = 0; sw < SVD_SWEEPS; sw++) {
         int rot = 0;
+#pragma unroll
         for (int p = 0; p < 5; p++)
+#pragma unroll
             for (int q = p + 1; q < 6; q++) {
+                const double pa = u[p] * u[p], pb = u[q] * u[q], pg = u[p] * u[q];
                 double al = 0.0, be = 0.0, ga = 0.0;
                 for (int i = 0; i < m; i++) {
-                    al = al + U[i][p] * U[i][p];
-                    be = be + U[i][q] * U[i][q];
-                    ga = ga + U[i][p] * U[i][q];
+                    al = al + __shfl_sync(FULL, pa, i);
+                    be = be + __shfl_sync(FULL, pb, i);
+                    ga = ga + __shfl_sync(FULL, pg, i);
                 }
                 if (ga == 0.0) continue;
                 if (fabs(ga) <= 1e-15 * sqrt(al * be)) continue;
@@ -41,37 +59,34 @@ __device__ void asv_lsq_minnorm(int m, double (*U)[6], const double *b, double x
                 if (zeta < 0.0) t = -t;
                 double c = 1.0 / sqrt(1.0 + t * t);
                 double s = c * t;
-                for (int i = 0; i < m; i++) {
-                    double up = U[i][p], uq = U[i][q];
-                    U[i][p] = c * up - s * uq;
-                    U[i][q] = s * up + c * uq;
-                }
-                for (int i = 0; i < 6; i++) {
-                    double vp = V[i][p], vq = V[i][q];
-                    V[i][p] = c * vp - s * vq;
-                    V[i][q] = s * vp + c * vq;
-                }
+                double up = u[p], uq = u[q];
+                u[p] = c * up - s * uq;
+                u[q] = s * up + c * uq;
+                double vp = v[p], vq = v[q];
+                v[p] = c * vp - s * vq;
+                v[q] = s * vp + c * vq;
                 rot++;
             }
         if (!rot) break;
     }
     double sig[6], smax = 0.0;
+#pragma unroll
     for (int j = 0; j < 6; j++) {
-        double a = 0.0;
-        for (int i = 0; i < m; i++) a = a + U[i][j] * U[i][j];
-        sig[j] = sqrt(a);
+        sig[j] = sqrt(asv_row_sum(u[j] * u[j], m));
         if (sig[j] > smax) smax = sig[j];
     }
     double thr = smax * ((double)(m < 6 ? m : 6) * (double)FLT_EPSILON);
     if (thr < (double)FLT_MIN) thr = (double)FLT_MIN;
-    for (int r = 0; r < 6; r++) x[r] = 0.0;
+    double xr = 0.0;   // lane r < 6 accumulates x[r]
+#pragma unroll
     for (int j = 0; j < 6; j++) {
         if (!(sig[j] >= thr)) continue;
-        double ub = 0.0;
-        for (int i = 0; i < m; i++) ub = ub + U[i][j] * b[i];
+        double ub = asv_row_sum(u[j] * bl, m);
         double coef = ub / (sig[j] * sig[j]);
-        for (int r = 0; r < 6; r++) x[r] = x[r] + V[r][j] * coef;
+        xr = xr + v[j] * coef;
     }
+#pragma unroll
+    for (int r = 0; r < 6; r++) x[r] = __shfl_sync(FULL, xr, r);
 }
 
 // symmetric 3x3 eigen-decomposition, cyclic Jacobi
@@ -138,12 +153,15 @@ __device__ void asv_m6_nearest_psd(const float M[6], float out[6])
 
 __device__ __forceinline__ float asv_round_half_up(float f) { return (float)floor((double)f + 0.5); }
 
-// matrix_slover (GPU-AS/Image.cpp:874-1009); returns the non-PSD flag
-__device__ int asv_metric_solve(const float2 *__restrict__ fwd, const float2 *__restrict__ bwd, int W,
-                                int H, int D, float sx, float sy, int frame, float M[6])
+// matrix_slover (GPU-AS/Image.cpp:874-1009) for one warp; returns the
+// non-PSD flag; M valid on every lane.  Rows are numbered in the
+// reference's order (neighbour y outer, x inner; forward row, then backward).
+__device__ int asv_metric_solve_warp(const float2 *__restrict__ fwd, const float2 *__restrict__ bwd,
+                                     int W, int H, int D, float sx, float sy, int frame, float M[6])
 {
+    const int lane = threadIdx.x & 31;
     const float expected_b[9] = { 3, 2, 3, 2, 1, 2, 3, 2, 3 };
-    double A[18][6], b[18];
+    double u[6] = { 0, 0, 0, 0, 0, 0 }, bl = 0.0;
     int m = 0, id_b = 0;
     for (int oy = -1; oy < 2; oy++)
         for (int ox = -1; ox < 2; ox++, id_b++) {
@@ -151,27 +169,36 @@ __device__ int asv_metric_solve(const float2 *__restrict__ fwd, const float2 *__
             if (!(nx >= 0 && nx < W && ny >= 0 && ny < H)) continue;
             long long o = ((long long)frame * H + ny) * W + nx;
             if (frame != D - 1) {
-                float2 f = __ldg(fwd + o);
-                float dx = (float)ox + asv_round_half_up(f.x);
-                float dy = (float)oy + asv_round_half_up(f.y);
-                A[m][0] = (double)(dx * dx); A[m][1] = (double)(2.0f * dx * dy);
-                A[m][2] = (double)(2.0f * dx); A[m][3] = (double)(dy * dy);
-                A[m][4] = (double)(2.0f * dy); A[m][5] = 1.0;
-                b[m++] = expected_b[id_b];
+                if (lane == m) {
+                    float2 f = __ldg(fwd + o);
+                    float dx = (float)ox + asv_round_half_up(f.x);
+                    float dy = (float)oy + asv_round_half_up(f.y);
+                    u[0] = (double)(dx * dx); u[1] = (double)(2.0f * dx * dy);
+                    u[2] = (double)(2.0f * dx); u[3] = (double)(dy * dy);
+                    u[4] = (double)(2.0f * dy); u[5] = 1.0;
+                    bl = expected_b[id_b];
+                }
+                m++;
             }
             if (frame != 0) {
-                float2 f = __ldg(bwd + o);
-                float dx = asv_round_half_up(f.x) + (float)ox;
-                float dy = asv_round_half_up(f.y) + (float)oy;
-                A[m][0] = (double)(dx * dx); A[m][1] = (double)(2.0f * dx * dy);
-                A[m][2] = (double)(-2.0f * dx); A[m][3] = (double)(dy * dy);
-                A[m][4] = (double)(-2.0f * dy); A[m][5] = 1.0;
-                b[m++] = expected_b[id_b];
+                if (lane == m) {
+                    float2 f = __ldg(bwd + o);
+                    float dx = asv_round_half_up(f.x) + (float)ox;
+                    float dy = asv_round_half_up(f.y) + (float)oy;
+                    u[0] = (double)(dx * dx); u[1] = (double)(2.0f * dx * dy);
+                    u[2] = (double)(-2.0f * dx); u[3] = (double)(dy * dy);
+                    u[4] = (double)(-2.0f * dy); u[5] = 1.0;
+                    bl = expected_b[id_b];
+                }
+                m++;
             }
         }
     double x[6];
-    if (m == 0) { for (int k = 0; k < 6; k++) x[k] = 0.0; }
-    else asv_lsq_minnorm(m, A, b, x);
+    if (m == 0) {
+        for (int k = 0; k < 6; k++) x[k] = 0.0;
+    } else {
+        asv_lsq_minnorm_warp(m, u, bl, x);
+    }
     for (int k = 0; k < 6; k++) M[k] = (float)x[k];
     return asv_m6_negative(M);
 }
@@ -215,45 +242,48 @@ __device__ __forceinline__ bool asv_seed_ref(const AsvDev &d, int g, SeedRef &r)
 }
 
 // which seed positions: reseed 0 -> pos0 (seed_matrix), 1 -> pos (reseed)
-__global__ void k_metric_self(AsvDev d, int reseed)
+__global__ void __launch_bounds__(128) k_metric_self(AsvDev d, int reseed)
 {
+    const int lane = threadIdx.x & 31;
     SeedRef r;
-    if (!asv_seed_ref(d, blockIdx.x * blockDim.x + threadIdx.x, r)) return;
+    if (!asv_seed_ref(d, (blockIdx.x * blockDim.x + threadIdx.x) >> 5, r)) return;   // warp-uniform
     const SegDesc &S = d.segs[r.si];
     float4 p = reseed ? d.pos[r.g] : d.pos0[r.g];
     float fx = floorf(p.x), fy = floorf(p.y);
     int frame = min(max((int)p.z, 0), S.D - 1);   // positions are inside; keep reads in bounds
     float M[6];
-    int neg = asv_metric_solve(d.fwd + S.vox_off, d.bwd + S.vox_off, S.W, S.H, S.D, fx, fy, frame, M);
-    for (int e = 0; e < 6; e++) d.Mself[8 * r.g + e] = M[e];
-    d.neg[r.g] = neg;
+    int neg = asv_metric_solve_warp(d.fwd + S.vox_off, d.bwd + S.vox_off, S.W, S.H, S.D, fx, fy,
+                                    frame, M);
+    if (lane < 6) d.Mself[8 * r.g + lane] = M[lane];
+    if (lane == 0) d.neg[r.g] = neg;
 }
 
-__global__ void k_metric_ring(AsvDev d, int reseed)
+__global__ void __launch_bounds__(128) k_metric_ring(AsvDev d, int reseed)
 {
-    int gid = blockIdx.x * blockDim.x + threadIdx.x;
-    int g = gid / ASV_RING, t = gid - g * ASV_RING;
+    const int lane = threadIdx.x & 31;
+    int task = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int g = task / ASV_RING, t = task - g * ASV_RING;
     SeedRef r;
     if (!asv_seed_ref(d, g, r)) return;
     int *ok = d.ringok + ASV_RING * g + t;
-    if (!d.neg[g]) { *ok = 0; return; }
+    if (!d.neg[g]) { if (lane == 0) *ok = 0; return; }
     const SegDesc &S = d.segs[r.si];
     float4 p = reseed ? d.pos[g] : d.pos0[g];
     float fx = floorf(p.x), fy = floorf(p.y);
     int frame = min(max((int)p.z, 0), S.D - 1);
     float nx = fx + (float)c_ringx[t], ny = fy + (float)c_ringy[t];
-    if (!(nx >= 0 && nx < S.W && ny >= 0 && ny < S.H)) { *ok = 0; return; }
+    if (!(nx >= 0 && nx < S.W && ny >= 0 && ny < S.H)) { if (lane == 0) *ok = 0; return; }
     const float2 *fwd = d.fwd + S.vox_off, *bwd = d.bwd + S.vox_off;
     if (reseed && S.angle_filter &&
         !asv_angle_ok(fwd, S.W, S.H, S.D, frame, (int)fx, (int)fy, (int)nx, (int)ny)) {
-        *ok = 0;
+        if (lane == 0) *ok = 0;
         return;
     }
     float M[6];
-    int neg = asv_metric_solve(fwd, bwd, S.W, S.H, S.D, nx, ny, frame, M);
+    int neg = asv_metric_solve_warp(fwd, bwd, S.W, S.H, S.D, nx, ny, frame, M);
     float *dst = d.Mring + 8 * (ASV_RING * g + t);
-    for (int e = 0; e < 6; e++) dst[e] = M[e];
-    *ok = neg ? 0 : 1;
+    if (lane < 6) dst[lane] = M[lane];
+    if (lane == 0) *ok = neg ? 0 : 1;
 }
 
 // writes M0 (reseed 0) or M (reseed 1)
@@ -291,9 +321,9 @@ __global__ void k_metric_combine(AsvDev d, int reseed)
 
 void asv_launch_metric(const AsvDev &d, int reseed, cudaStream_t st)
 {
-    int nb = (d.total_seeds + 63) / 64;
-    k_metric_self<<<nb, 64, 0, st>>>(d, reseed);
-    long long nr = (long long)d.total_seeds * ASV_RING;
-    k_metric_ring<<<(int)((nr + 63) / 64), 64, 0, st>>>(d, reseed);
-    k_metric_combine<<<nb, 64, 0, st>>>(d, reseed);
+    long long warps = d.total_seeds;
+    k_metric_self<<<(int)((warps * 32 + 127) / 128), 128, 0, st>>>(d, reseed);
+    long long rw = (long long)d.total_seeds * ASV_RING;
+    k_metric_ring<<<(int)((rw * 32 + 127) / 128), 128, 0, st>>>(d, reseed);
+    k_metric_combine<<<(d.total_seeds + 63) / 64, 64, 0, st>>>(d, reseed);
 }

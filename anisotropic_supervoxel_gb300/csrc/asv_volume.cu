@@ -30,6 +30,17 @@ __global__ void k_srgb_table(float *__restrict__ tab)
     tab[c] = t;
 }
 
+// distance of x + 0.5 to the nearest integer (where floor(x + 0.5) can flip)
+__device__ __forceinline__ float asv_tie_gap(float x)
+{
+    float y = x + 0.5f;
+    return fabsf(y - rintf(y));
+}
+
+// The cube root f = r^(1/3) is first taken in FP32 (exp2/log2, error below
+// 1e-6 relative, i.e. below 6e-4 on the scaled L, a, b); only when a scaled
+// value lies within 4e-3 of a rounding boundary is the voxel recomputed with
+// the correctly rounded FP64 path, so the bytes equal the exact ones.
 __device__ __forceinline__ uchar4 asv_lab_of(const float *__restrict__ tab, unsigned r, unsigned g,
                                              unsigned b)
 {
@@ -39,15 +50,27 @@ __device__ __forceinline__ uchar4 asv_lab_of(const float *__restrict__ tab, unsi
     float Z = (t0 * 0.019334f + t1 * 0.119193f) + t2 * 0.950227f;
     float rr[3] = { X / 0.950456f, Y / 1.0f, Z / 1.088754f };        // fs:54-55
     float f[3];
+    bool cube[3];
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-        if (rr[k] > 0.008856f) f[k] = asv_pow_cr(rr[k], 1.0f / 3.0f); // fs:57-70
+        cube[k] = rr[k] > 0.008856f;                                   // fs:57-70
+        if (cube[k]) f[k] = exp2f(log2f(rr[k]) * (1.0f / 3.0f));
         else f[k] = (903.3f * rr[k] + 16.0f) / 116.0f;
     }
     float L = 116.0f * f[1] - 16.0f;                                  // fs:72
     float A = 500.0f * (f[0] - f[1]);
     float B = 200.0f * (f[1] - f[2]);
     L = L * 2.55f; A = A + 128.0f; B = B + 128.0f;                    // fs:74-76
+    if ((cube[0] || cube[1] || cube[2]) &&
+        fminf(asv_tie_gap(L), fminf(asv_tie_gap(A), asv_tie_gap(B))) < 4e-3f) {
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+            if (cube[k]) f[k] = asv_pow_cr(rr[k], 1.0f / 3.0f);
+        L = 116.0f * f[1] - 16.0f;
+        A = 500.0f * (f[0] - f[1]);
+        B = 200.0f * (f[1] - f[2]);
+        L = L * 2.55f; A = A + 128.0f; B = B + 128.0f;
+    }
     float v0 = floorf(L + 0.5f), v1 = floorf(A + 0.5f), v2 = floorf(B + 0.5f);
     v0 = fminf(fmaxf(v0, 0.0f), 255.0f);
     v1 = fminf(fmaxf(v1, 0.0f), 255.0f);
@@ -151,24 +174,30 @@ __global__ void __launch_bounds__(256) k_density(AsvDev d)
 }
 
 // 1-D redistribution of the seeds along the cells (Image.cpp:549-616).  One
-// thread per segment: the prefix sums are sequential float sums in the
-// reference.  `scratch` holds Kp floats per segment.
-__global__ void k_density_adjust(AsvDev d, float *scratch)
+// block per segment: the densities are formed in parallel, the prefix sums
+// (sequential float sums in the reference) and the walk by one thread, on
+// shared memory when Kp <= ASV_ADJ_SMEM, else on `scratch` (Kp floats).
+#define ASV_ADJ_SMEM 12288
+
+__global__ void __launch_bounds__(256) k_density_adjust(AsvDev d, float *scratch)
 {
+    extern __shared__ float sh_len[];
     int si = blockIdx.x;
-    if (threadIdx.x != 0 || si >= d.nseg) return;
+    if (si >= d.nseg) return;
     const SegDesc &S = d.segs[si];
     const int Kp = S.Kp;
     const unsigned long long *acc = d.dacc + S.seed_off;
     const int *xl = d.cells + S.cell_off + S.W + S.H + S.D, *xr = xl + S.wNum;
     const float4 *grid = d.grid + S.seed_off;
-    float *len = scratch + S.seed_off;
-    for (int i = 0; i < Kp; i++) {
+    float *len = Kp <= ASV_ADJ_SMEM ? sh_len : scratch + S.seed_off;
+    for (int i = threadIdx.x; i < Kp; i += blockDim.x) {
         unsigned long long tot = acc[i] + (3ull << 24);               // cleared to 3.0 (:506-507)
         float res = __ull2float_rn(tot) * 0x1p-24f;
-        float dens = (float)(0.001 * (double)res);                    // :554
-        len[i] = i == 0 ? dens : dens + len[i - 1];                   // :558-569
+        len[i] = (float)(0.001 * (double)res);                        // :554
     }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    for (int i = 1; i < Kp; i++) len[i] = len[i] + len[i - 1];        // :558-569
     float interval = len[Kp - 1] / (float)(Kp + 1);                   // :570
     int i = 0, j1 = 0, n = 0;
     while (i < Kp) {                                                  // :586-616
@@ -246,40 +275,52 @@ __global__ void k_draw(AsvDev d)
 // 32x8-voxel tiles of one slice, persistent grid-stride over the tiles of
 // all segments (z-major, so the resident tiles share their +-step slices in
 // L2).  27 candidates in the shader's order: slices z, z-step, z+step; rows
-// y-step..y+step; columns x-step..x+step; clamp to edge.  A candidate whose
-// seed id equals the current best or the previously evaluated id is skipped:
-// its distance is identical and the test is strict `<`.
+// y-step..y+step; columns x-step..x+step; clamp to edge.
+//
+// The candidates are first reduced to a list of ids in first-occurrence
+// order (a candidate equal to one of the three most recently listed ids is
+// dropped), kept in shared memory, and the list is evaluated in one loop: a
+// warp pays for its longest list instead of for every candidate position
+// where some lane meets a new id.  A dropped or repeated id has the same
+// distance as its first occurrence and the test is strict `<`, so the result
+// is the shader's.
 // ---------------------------------------------------------------------------
+#define ASV_JFA_THREADS 256
+
 __device__ __forceinline__ void asv_jfa_voxel(const int32_t *__restrict__ in, int32_t *__restrict__ out,
                                               const uchar4 *__restrict__ lab,
                                               const float4 *__restrict__ tab, int W, int H, int D,
-                                              int Kp, int x, int y, int z, int step, float ratio)
+                                              int Kp, int x, int y, int z, int step, float ratio,
+                                              int *__restrict__ list)
 {
-    const long long sl = (long long)W * H;
+    const int sl = W * H;                       // segments hold < 2^31 voxels
     const float vx = (float)x + 0.5f, vy = (float)y + 0.5f, vz = (float)z + 0.5f;
-    uchar4 c = __ldg(lab + z * sl + (long long)y * W + x);
-    const float cL = (float)c.x, ca = (float)c.y, cb = (float)c.z;
-    const int xs0 = max(x - step, 0), xs2 = min(x + step, W - 1);
-    const int ys0 = max(y - step, 0), ys2 = min(y + step, H - 1);
-    const int zs[3] = { z, max(z - step, 0), min(z + step, D - 1) };
-    const int xs[3] = { xs0, x, xs2 };
-    const int ys[3] = { ys0, y, ys2 };
+    const int xs[3] = { max(x - step, 0), x, min(x + step, W - 1) };
+    const int ys[3] = { max(y - step, 0) * W, y * W, min(y + step, H - 1) * W };
+    const int zs[3] = { z * sl, max(z - step, 0) * sl, min(z + step, D - 1) * sl };
     int32_t cand[27];
 #pragma unroll
     for (int s = 0; s < 3; s++)
 #pragma unroll
-        for (int oy = 0; oy < 3; oy++) {
-            const int32_t *row = in + zs[s] * sl + (long long)ys[oy] * W;
+        for (int oy = 0; oy < 3; oy++)
 #pragma unroll
-            for (int ox = 0; ox < 3; ox++) cand[(s * 3 + oy) * 3 + ox] = __ldg(row + xs[ox]);
-        }
-    float mind = 100000000.0f;                                        // flood.gs:63
-    int32_t best = -1, last = -1;
+            for (int ox = 0; ox < 3; ox++) cand[(s * 3 + oy) * 3 + ox] = __ldg(in + zs[s] + ys[oy] + xs[ox]);
+    const uchar4 c = __ldg(lab + z * sl + y * W + x);
+    int n = 0, r1 = -1, r2 = -1, r3 = -1;
 #pragma unroll
     for (int k = 0; k < 27; k++) {
         const int32_t l = cand[k];
-        if (l < 0 || l >= Kp || l == best || l == last) continue;
-        last = l;
+        if ((unsigned)l < (unsigned)Kp && l != r1 && l != r2 && l != r3) {
+            list[n * ASV_JFA_THREADS] = l;
+            n++;
+            r3 = r2; r2 = r1; r1 = l;
+        }
+    }
+    const float cL = (float)c.x, ca = (float)c.y, cb = (float)c.z;
+    float mind = 100000000.0f;                                        // flood.gs:63
+    int32_t best = -1;
+    for (int i = 0; i < n; i++) {
+        const int32_t l = list[i * ASV_JFA_THREADS];
         const float4 t0 = __ldg(tab + 3 * l), t1 = __ldg(tab + 3 * l + 1), t2 = __ldg(tab + 3 * l + 2);
         const float dx = vx - t0.x, dy = vy - t0.y, dz = vz - t0.z;
         float p1 = (dx * dx) * t1.z + (dx * dy) * t1.w;              // flood.gs:85
@@ -294,12 +335,14 @@ __device__ __forceinline__ void asv_jfa_voxel(const int32_t *__restrict__ in, in
         const float dist = ratio * pos + col;                          // flood.gs:94
         if (dist < mind) { mind = dist; best = l; }                    // flood.gs:95-99
     }
-    out[z * sl + (long long)y * W + x] = best;
+    out[z * sl + y * W + x] = best;
 }
 
-__global__ void __launch_bounds__(256) k_jfa(AsvDev d, int pass, const int32_t *__restrict__ in,
-                                             int32_t *__restrict__ out)
+__global__ void __launch_bounds__(ASV_JFA_THREADS) k_jfa(AsvDev d, int pass,
+                                                         const int32_t *__restrict__ in,
+                                                         int32_t *__restrict__ out)
 {
+    __shared__ int list[27 * ASV_JFA_THREADS];
     const int lx = threadIdx.x & (ASV_TILE_X - 1), ly = threadIdx.x >> 5;
     for (int t = blockIdx.x; t < d.total_tiles; t += gridDim.x) {
         const int si = asv_find_seg(d.tile_prefix, d.nseg, t);
@@ -311,14 +354,16 @@ __global__ void __launch_bounds__(256) k_jfa(AsvDev d, int pass, const int32_t *
         const int x = tx * ASV_TILE_X + lx, y = ty * ASV_TILE_Y + ly;
         if (x >= S.W || y >= S.H) continue;
         asv_jfa_voxel(in + S.vox_off, out + S.vox_off, d.lab + S.vox_off, d.jtab + 3 * S.seed_off,
-                      S.W, S.H, S.D, S.Kp, x, y, z, S.steps[pass], S.ratio[pass]);
+                      S.W, S.H, S.D, S.Kp, x, y, z, S.steps[pass], S.ratio[pass], list + threadIdx.x);
     }
 }
 
 // single-segment pass with explicit step and ratio (test entry point)
-__global__ void __launch_bounds__(256) k_jfa_single(AsvDev d, const int32_t *__restrict__ in,
-                                                    int32_t *__restrict__ out, int step, float ratio)
+__global__ void __launch_bounds__(ASV_JFA_THREADS) k_jfa_single(AsvDev d, const int32_t *__restrict__ in,
+                                                                int32_t *__restrict__ out, int step,
+                                                                float ratio)
 {
+    __shared__ int list[27 * ASV_JFA_THREADS];
     const SegDesc &S = d.segs[0];
     const int lx = threadIdx.x & (ASV_TILE_X - 1), ly = threadIdx.x >> 5;
     const int ntiles = S.tiles_x * S.tiles_y * S.D;
@@ -328,7 +373,7 @@ __global__ void __launch_bounds__(256) k_jfa_single(AsvDev d, const int32_t *__r
         const int x = tx * ASV_TILE_X + lx, y = ty * ASV_TILE_Y + ly;
         if (x >= S.W || y >= S.H) continue;
         asv_jfa_voxel(in, out, d.lab + S.vox_off, d.jtab + 3 * S.seed_off, S.W, S.H, S.D, S.Kp,
-                      x, y, z, step, ratio);
+                      x, y, z, step, ratio, list + threadIdx.x);
     }
 }
 
@@ -667,7 +712,10 @@ static inline int seed_blocks(const AsvDev &d) { return (d.total_seeds + 127) / 
 void asv_launch_srgb_table(const AsvDev &d, cudaStream_t st) { k_srgb_table<<<1, 256, 0, st>>>(d.srgb); }
 void asv_launch_rgb2lab(const AsvDev &d, cudaStream_t st) { k_rgb2lab<<<d.total_chunks, 256, 0, st>>>(d); }
 void asv_launch_density(const AsvDev &d, cudaStream_t st) { k_density<<<d.total_chunks, 256, 0, st>>>(d); }
-void asv_launch_density_adjust(const AsvDev &d, cudaStream_t st) { k_density_adjust<<<d.nseg, 32, 0, st>>>(d, d.Mring); }
+void asv_launch_density_adjust(const AsvDev &d, cudaStream_t st)
+{
+    k_density_adjust<<<d.nseg, 256, ASV_ADJ_SMEM * sizeof(float), st>>>(d, d.Mring);
+}
 void asv_launch_first_init(const AsvDev &d, cudaStream_t st) { k_first_init<<<seed_blocks(d), 128, 0, st>>>(d); }
 void asv_launch_draw(const AsvDev &d, cudaStream_t st) { k_draw<<<seed_blocks(d), 128, 0, st>>>(d); }
 

@@ -1,0 +1,343 @@
+#!/usr/bin/env python3
+"""Throughput of the supervoxel JFA+Lloyd loop on GB300 (one JSON line).
+
+step      one full Lloyd loop (all iterations: metric solves, reseeding, every
+          JFA pass, centroid sums, post-processing) over one synthetic clip.
+value     Mvoxel-iterations/s = W*H*D*iters*steps / device time, inputs
+          resident in HBM; L2 flushed (512 MiB write) before every step.
+e2e       the same metric through the public C ABI with pinned host buffers:
+          RGB + flow upload, seed placement, metric, LAB, loop, labels back.
+--impl reference
+          the CPU restatement of the reference's path (the reference's own
+          GLSL/OpenGL pipeline cannot run here) on all host cores.
+Multi-GPU: replicas only (independent clips per rank, no collective on the
+data path); value = all ranks' voxel-iterations / max rank time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("Mvoxel-iterations/s (JFA+Lloyd) and p50/p99 window latency vs plain form at "
+          "≥99.9% agreement")
+UNIT = "Mvoxel-iterations/s"
+PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+TRAFFIC = os.path.join(ROOT, "profiles", "k_jfa_320x240x85.md")
+# algorithmic bytes per voxel of one JFA pass: label in 4 + label out 4 + LAB 3
+JFA_BYTES_PER_VOXEL = 11
+# nominal FP32 work per voxel of one JFA pass: 27 candidates x 33 operations
+JFA_FLOP_PER_VOXEL = 27 * 33
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="clip_320x240x85",
+                    choices=["clip_320x240x85", "clip_240x160x30"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload(name):
+    from anisotropic_supervoxel_gb300 import workloads
+    return {"clip_320x240x85": workloads.CLIP_320x240x85,
+            "clip_240x160x30": workloads.CLIP_240x160x30}[name]
+
+
+def dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi samples (200 ms) during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev):
+        self.dev = dev
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.p.terminate()
+        self.p.wait()
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as fh:
+            for line in fh:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 7:
+                    rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
+
+
+def peaks():
+    try:
+        with open(PEAKS) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def jfa_traffic_per_voxel():
+    """DRAM bytes per voxel of one JFA pass from the committed ncu summary."""
+    try:
+        with open(TRAFFIC) as f:
+            for line in f:
+                if line.startswith("dram_bytes_per_voxel:"):
+                    return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_baseline(w, rgb, fwd, bwd, iters):
+    from oracle import oracle
+    n = os.cpu_count() or 1
+    t = time.perf_counter()
+    oracle.run_clip(rgb, fwd, bwd, w["K"], iters=iters, nthreads=n)
+    dt = time.perf_counter() - t
+    vox = rgb.shape[0] * rgb.shape[1] * rgb.shape[2]
+    return {"value": vox * iters / dt / 1e6, "unit": UNIT, "cores": n, "kind": "port",
+            "sample": f"{rgb.shape[2]}x{rgb.shape[1]}x{rgb.shape[0]} clip, K={w['K']}, "
+                      f"{iters} Lloyd iterations (whole run incl. seed placement and LAB), "
+                      f"OpenMP over {n} threads, {dt:.1f} s"}
+
+
+def config_of(w, name, N):
+    return {"workload": f"{name}_K{w['K']}_I{w['iters']}", "W": w["W"], "H": w["H"], "D": w["D"],
+            "K": w["K"], "lloyd_iters": w["iters"], "ellipses": w["n_ellipses"],
+            "noise_sigma": w["noise_sigma"], "jitter": w["jitter"], "jfa_ladder": "reference",
+            "variant": "plain", "parallelism": f"replicas{N}",
+            "l2": "flushed before every step (512 MiB write)"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist()
+    if rank != 0:
+        return
+    w = workload(args.workload)
+    from anisotropic_supervoxel_gb300 import workloads
+    rgb, fwd, bwd = workloads.make_clip(w)
+    iters = 3
+    for _ in range(args.warmup):
+        cpu_baseline(w, rgb, fwd, bwd, iters)
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(w, rgb, fwd, bwd, iters))
+    wall = time.perf_counter() - t0
+    v = statistics.mean(x["value"] for x in vals)
+    cb = dict(vals[-1])
+    cb["value"] = v
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded ellipse video, exact generating flow)",
+        "config": config_of(w, args.workload, args.gpus),
+        "cpu_baseline": cb,
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference's own pipeline is GLSL over OpenGL (no graphics stack here); "
+                "this arm runs the C restatement of its shader maths and Image.cpp host logic",
+    }), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    import anisotropic_supervoxel_gb300 as asv
+    from anisotropic_supervoxel_gb300 import workloads
+
+    ws, rank, local = dist()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))
+    w = workload(args.workload)
+    I, K = w["iters"], w["K"]
+    rgb, fwd, bwd = workloads.make_clip(w)
+    D, H, W, _ = rgb.shape
+    nvox = W * H * D
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+
+    # --- device-resident value ----------------------------------------------
+    img = asv.Image(lloyd_iters=I, device=local)
+    img.init_gpu(rgb, K)
+    img.upload_flow(fwd, bwd)
+    img.initialization()
+    img.seed_matrix()
+    img.RGB2LAB()
+    img.synchronize()
+    st = torch.cuda.ExternalStream(img.stream(), device=torch.device("cuda", local))
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    for _ in range(args.warmup):
+        img.run_lloyd()
+    img.synchronize()
+    launches = img.stats().launches
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    clocks = Clocks(local)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    for k in range(args.steps):
+        with torch.cuda.stream(st):
+            flush.fill_(k & 255)
+        ev[k][0].record(st)
+        img.run_lloyd()
+        ev[k][1].record(st)
+    st.synchronize()
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    tot_ms = sum(step_ms)
+    if ws > 1:
+        t = torch.tensor([tot_ms], device=f"cuda:{local}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        tot_ms = float(t.item())
+    value = nvox * I * args.steps * ws / (tot_ms / 1e3) / 1e6
+    info = img.info()
+
+    # --- JFA kernel: per-launch device time (CUDA events around each pass) ----
+    prof = asv.Image(lloyd_iters=I, device=local, instrument=1, use_graph=0)
+    prof.init_gpu(rgb, K)
+    prof.upload_flow(fwd, bwd)
+    prof.initialization()
+    prof.seed_matrix()
+    prof.RGB2LAB()
+    prof.run_lloyd()
+    jfa_ms, jfa_n, loop_ms = 0.0, 0, 0.0
+    for _ in range(max(1, args.steps)):
+        prof.run_lloyd()
+        s = prof.stats()
+        jfa_ms += s.jfa_ms
+        jfa_n += s.jfa_launches
+        loop_ms += s.total_ms
+    prof.close()
+    jfa_launch_s = jfa_ms / jfa_n / 1e3
+    peak, peak_kind = peaks()
+    achieved = JFA_BYTES_PER_VOXEL * nvox / jfa_launch_s / 1e9
+    tpv = jfa_traffic_per_voxel()
+
+    # --- end to end through the C ABI with pinned host buffers ----------------
+    def pinned(a):
+        t = torch.empty(a.shape, dtype=getattr(torch, str(a.dtype)), pin_memory=True)
+        t.numpy()[...] = a
+        return t.numpy()
+
+    prgb, pfwd, pbwd = pinned(rgb), pinned(fwd), pinned(bwd)
+    plab = torch.empty((D, H, W), dtype=torch.int32, pin_memory=True).numpy()
+    e2e = asv.Image(lloyd_iters=I, device=local)
+
+    def e2e_step():
+        e2e.init_gpu(prgb, K)
+        e2e.upload_flow(pfwd, pbwd)
+        e2e.initialization()
+        e2e.seed_matrix()
+        e2e.RGB2LAB()
+        e2e.run_lloyd()
+        e2e.lib.asv_get_labels(e2e.h, plab.ctypes.data)
+
+    for _ in range(args.warmup):
+        e2e_step()
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if ws > 1:
+        t = torch.tensor([e2e_s], device=f"cuda:{local}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_val = nvox * I * args.steps * ws / e2e_s / 1e6
+    ok_labels = bool((plab == img.labels()).all())
+    e2e.close()
+
+    cb = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        cb = cpu_baseline(w, rgb, fwd, bwd, 5)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": tot_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded ellipse video, exact generating flow)",
+            "config": config_of(w, args.workload, ws),
+            "e2e": {"value": e2e_val, "unit": UNIT,
+                    "h2d_bytes_per_step": int(rgb.nbytes + fwd.nbytes + bwd.nbytes),
+                    "d2h_bytes_per_step": int(plab.nbytes),
+                    "labels_match_device_run": ok_labels},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind,
+                         "kernel": "k_jfa", "bytes_per_launch": JFA_BYTES_PER_VOXEL * nvox,
+                         "launch_ms": jfa_launch_s * 1e3,
+                         "traffic": tpv * nvox if tpv is not None else None,
+                         "fp32_nominal_tflops": JFA_FLOP_PER_VOXEL * nvox / jfa_launch_s / 1e12,
+                         "jfa_share_of_loop": jfa_ms / loop_ms if loop_ms else None},
+            "clocks": clk,
+            "gpu_launches": int(launches * args.steps),
+            "kp": info.Kp, "jfa_passes_per_iteration": info.passes,
+        }
+        if cb is not None:
+            line["cpu_baseline"] = cb
+        print(json.dumps(line), flush=True)
+    img.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()
