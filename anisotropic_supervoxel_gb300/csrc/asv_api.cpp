@@ -297,6 +297,7 @@ asv_status asv_build_layout(asv_ctx *ctx)
     AL(d.jtab, (size_t)seeds * 3);
     AL(d.sums, (size_t)seeds * 8);
     AL(d.Mself, (size_t)seeds * 8); AL(d.neg, seeds);
+    AL(d.Mmemo, (size_t)seeds * 8); AL(d.mkey, seeds);
     AL(d.Mring, (size_t)seeds * ASV_RING * 8); AL(d.ringok, (size_t)seeds * ASV_RING);
     AL(d.grid, seeds);
     AL(d.dacc, seeds);
@@ -782,6 +783,7 @@ asv_status asv_set_seeds(asv_ctx *ctx, const float *in, int Kp)
     CK(cudaMemcpyAsync(ctx->d.pos + off, p.data(), sizeof(float4) * Kp, cudaMemcpyHostToDevice, ctx->st));
     CK(cudaMemcpyAsync(ctx->d.slab + off, c.data(), sizeof(float4) * Kp, cudaMemcpyHostToDevice, ctx->st));
     CK(cudaMemcpyAsync(ctx->d.M + 8 * (size_t)off, m.data(), sizeof(float) * 8 * Kp, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemsetAsync(ctx->d.mkey + off, 0xff, sizeof(int) * Kp, ctx->st));   // drop the reseed memo
     asv_launch_draw(ctx->d, ctx->st);   // packs the JFA table (the label write is ignored here)
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(ctx->st));

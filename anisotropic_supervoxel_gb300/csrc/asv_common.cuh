@@ -82,6 +82,7 @@ struct AsvDev {
     float4 *jtab;                // JFA seed table, 3 float4 / seed
     unsigned long long *sums;    // 8 u64 / slot
     float *Mself; int *neg;      // metric scratch
+    float *Mmemo; int *mkey;     // reseed memo: metric of the voxel key of the last solve
     float *Mring; int *ringok;
     float4 *grid;                // grid seeds
     unsigned long long *dacc;    // density accumulators (2^-24 units)

@@ -5,9 +5,10 @@
 // round trip every Lloyd iteration.  For each seed, the 3x3 neighbourhood of
 // its voxel gives up to 18 rows d^T M d = b (forward rows d = (dx, dy, 1),
 // backward rows d = (dx, dy, -1), b = n^2 + m^2 + 1); M is the min-norm
-// least-squares solution (FP64 one-sided Jacobi SVD, rank rule of Eigen's
-// SVD solve: keep sigma >= max(sigma_max * min(rows,6) * FLT_EPSILON,
-// FLT_MIN)).  A non-PSD M falls back to the mean of the PSD metrics of the
+// least-squares solution in FP32 like the reference's Eigen float solve
+// (one-sided Jacobi SVD, rank rule of Eigen's SVD solve: keep
+// sigma >= max(sigma_max * min(rows,6) * FLT_EPSILON, FLT_MIN)); the 3x3
+// PSD test and the nearest-PSD projection run in FP64.  A non-PSD M falls back to the mean of the PSD metrics of the
 // 1-ring, then 2-ring neighbours, then to the nearest PSD matrix.
 //
 // One warp per solve: lane i holds row i of the system; column dot products
@@ -15,74 +16,77 @@
 // same scalars with the same operation sequence as a sequential solver.
 // Launches: k_metric_self (a warp per seed), k_metric_ring (a warp per seed
 // and neighbour, only for non-PSD seeds), k_metric_combine (a thread per
-// seed).  Compiled with -fmad=false.
+// seed).  A reseed solve is skipped when the seed's voxel is the one of its
+// previous reseed solve in this Lloyd run: the metric is a function of that
+// voxel and the flow only, so the stored result is the solve's result.
+// Compiled with -fmad=false.
 #include "asv_common.cuh"
 
 #include <float.h>
 
-#define SVD_SWEEPS 40
+#define SVD_SWEEPS 30
 #define FULL 0xffffffffu
 
 // sequential sum over rows 0..m-1 of a per-lane value
-__device__ __forceinline__ double asv_row_sum(double v, int m)
+__device__ __forceinline__ float asv_row_sum(float v, int m)
 {
-    double a = 0.0;
+    float a = 0.0f;
     for (int i = 0; i < m; i++) a = a + __shfl_sync(FULL, v, i);
     return a;
 }
 
-// min-norm least squares; u = this lane's row (zero beyond m), bl = its rhs.
-// Returns x[0..5] on every lane.
-__device__ void asv_lsq_minnorm_warp(int m, double u[6], double bl, double x[6])
+// min-norm least squares in FP32; u = this lane's row (zero beyond m),
+// bl = its rhs.  Returns x[0..5] on every lane.
+__device__ void asv_lsq_minnorm_warp(int m, float u[6], float bl, float x[6])
 {
     const int lane = threadIdx.x & 31;
-    double v[6];
+    float v[6];
 #pragma unroll
-    for (int c = 0; c < 6; c++) v[c] = lane == c ? 1.0 : 0.0;   // lane r < 6 holds row r of V
+    for (int c = 0; c < 6; c++) v[c] = lane == c ? 1.0f : 0.0f;   // lane r < 6 holds row r of V
     for (int sw = 0; sw < SVD_SWEEPS; sw++) {
         int rot = 0;
 #pragma unroll
         for (int p = 0; p < 5; p++)
 #pragma unroll
             for (int q = p + 1; q < 6; q++) {
-                const double pa = u[p] * u[p], pb = u[q] * u[q], pg = u[p] * u[q];
-                double al = 0.0, be = 0.0, ga = 0.0;
+                const float pa = u[p] * u[p], pb = u[q] * u[q], pg = u[p] * u[q];
+                float al = 0.0f, be = 0.0f, ga = 0.0f;
                 for (int i = 0; i < m; i++) {
                     al = al + __shfl_sync(FULL, pa, i);
                     be = be + __shfl_sync(FULL, pb, i);
                     ga = ga + __shfl_sync(FULL, pg, i);
                 }
-                if (ga == 0.0) continue;
-                if (fabs(ga) <= 1e-15 * sqrt(al * be)) continue;
-                double zeta = (be - al) / (2.0 * ga);
-                double t = 1.0 / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-                if (zeta < 0.0) t = -t;
-                double c = 1.0 / sqrt(1.0 + t * t);
-                double s = c * t;
-                double up = u[p], uq = u[q];
+                if (ga == 0.0f) continue;
+                if (fabsf(ga) <= FLT_EPSILON * sqrtf(al * be)) continue;
+                float zeta = (be - al) / (2.0f * ga);
+                float t = 1.0f / (fabsf(zeta) + sqrtf(1.0f + zeta * zeta));
+                if (zeta < 0.0f) t = -t;
+                float c = 1.0f / sqrtf(1.0f + t * t);
+                float s = c * t;
+                float up = u[p], uq = u[q];
                 u[p] = c * up - s * uq;
                 u[q] = s * up + c * uq;
-                double vp = v[p], vq = v[q];
+                float vp = v[p], vq = v[q];
                 v[p] = c * vp - s * vq;
                 v[q] = s * vp + c * vq;
                 rot++;
             }
         if (!rot) break;
     }
-    double sig[6], smax = 0.0;
+    float sig[6], smax = 0.0f;
 #pragma unroll
     for (int j = 0; j < 6; j++) {
-        sig[j] = sqrt(asv_row_sum(u[j] * u[j], m));
+        sig[j] = sqrtf(asv_row_sum(u[j] * u[j], m));
         if (sig[j] > smax) smax = sig[j];
     }
-    double thr = smax * ((double)(m < 6 ? m : 6) * (double)FLT_EPSILON);
-    if (thr < (double)FLT_MIN) thr = (double)FLT_MIN;
-    double xr = 0.0;   // lane r < 6 accumulates x[r]
+    float thr = smax * ((float)(m < 6 ? m : 6) * FLT_EPSILON);
+    if (thr < FLT_MIN) thr = FLT_MIN;
+    float xr = 0.0f;   // lane r < 6 accumulates x[r]
 #pragma unroll
     for (int j = 0; j < 6; j++) {
         if (!(sig[j] >= thr)) continue;
-        double ub = asv_row_sum(u[j] * bl, m);
-        double coef = ub / (sig[j] * sig[j]);
+        float ub = asv_row_sum(u[j] * bl, m);
+        float coef = (ub / sig[j]) / sig[j];
         xr = xr + v[j] * coef;
     }
 #pragma unroll
@@ -161,7 +165,7 @@ __device__ int asv_metric_solve_warp(const float2 *__restrict__ fwd, const float
 {
     const int lane = threadIdx.x & 31;
     const float expected_b[9] = { 3, 2, 3, 2, 1, 2, 3, 2, 3 };
-    double u[6] = { 0, 0, 0, 0, 0, 0 }, bl = 0.0;
+    float u[6] = { 0, 0, 0, 0, 0, 0 }, bl = 0.0f;
     int m = 0, id_b = 0;
     for (int oy = -1; oy < 2; oy++)
         for (int ox = -1; ox < 2; ox++, id_b++) {
@@ -173,9 +177,9 @@ __device__ int asv_metric_solve_warp(const float2 *__restrict__ fwd, const float
                     float2 f = __ldg(fwd + o);
                     float dx = (float)ox + asv_round_half_up(f.x);
                     float dy = (float)oy + asv_round_half_up(f.y);
-                    u[0] = (double)(dx * dx); u[1] = (double)(2.0f * dx * dy);
-                    u[2] = (double)(2.0f * dx); u[3] = (double)(dy * dy);
-                    u[4] = (double)(2.0f * dy); u[5] = 1.0;
+                    u[0] = dx * dx; u[1] = 2.0f * dx * dy;
+                    u[2] = 2.0f * dx; u[3] = dy * dy;
+                    u[4] = 2.0f * dy; u[5] = 1.0f;
                     bl = expected_b[id_b];
                 }
                 m++;
@@ -185,21 +189,21 @@ __device__ int asv_metric_solve_warp(const float2 *__restrict__ fwd, const float
                     float2 f = __ldg(bwd + o);
                     float dx = asv_round_half_up(f.x) + (float)ox;
                     float dy = asv_round_half_up(f.y) + (float)oy;
-                    u[0] = (double)(dx * dx); u[1] = (double)(2.0f * dx * dy);
-                    u[2] = (double)(-2.0f * dx); u[3] = (double)(dy * dy);
-                    u[4] = (double)(-2.0f * dy); u[5] = 1.0;
+                    u[0] = dx * dx; u[1] = 2.0f * dx * dy;
+                    u[2] = -2.0f * dx; u[3] = dy * dy;
+                    u[4] = -2.0f * dy; u[5] = 1.0f;
                     bl = expected_b[id_b];
                 }
                 m++;
             }
         }
-    double x[6];
+    float x[6];
     if (m == 0) {
-        for (int k = 0; k < 6; k++) x[k] = 0.0;
+        for (int k = 0; k < 6; k++) x[k] = 0.0f;
     } else {
         asv_lsq_minnorm_warp(m, u, bl, x);
     }
-    for (int k = 0; k < 6; k++) M[k] = (float)x[k];
+    for (int k = 0; k < 6; k++) M[k] = x[k];
     return asv_m6_negative(M);
 }
 
@@ -241,6 +245,15 @@ __device__ __forceinline__ bool asv_seed_ref(const AsvDev &d, int g, SeedRef &r)
     return r.i < d.segs[r.si].Kp;
 }
 
+// voxel key of a seed position (the memo key of the reseed solve)
+__device__ __forceinline__ int asv_seed_key(const SegDesc &S, float4 p)
+{
+    int frame = min(max((int)p.z, 0), S.D - 1);
+    int x = min(max((int)floorf(p.x), 0), S.W - 1), y = min(max((int)floorf(p.y), 0), S.H - 1);
+    return (frame * S.H + y) * S.W + x;
+}
+
+// neg[g]: 0 = PSD, 1 = non-PSD (fallbacks run), 2 = memo hit (reseed only)
 // which seed positions: reseed 0 -> pos0 (seed_matrix), 1 -> pos (reseed)
 __global__ void __launch_bounds__(128) k_metric_self(AsvDev d, int reseed)
 {
@@ -249,6 +262,10 @@ __global__ void __launch_bounds__(128) k_metric_self(AsvDev d, int reseed)
     if (!asv_seed_ref(d, (blockIdx.x * blockDim.x + threadIdx.x) >> 5, r)) return;   // warp-uniform
     const SegDesc &S = d.segs[r.si];
     float4 p = reseed ? d.pos[r.g] : d.pos0[r.g];
+    if (reseed && d.mkey[r.g] == asv_seed_key(S, p)) {
+        if (lane == 0) d.neg[r.g] = 2;
+        return;
+    }
     float fx = floorf(p.x), fy = floorf(p.y);
     int frame = min(max((int)p.z, 0), S.D - 1);   // positions are inside; keep reads in bounds
     float M[6];
@@ -266,7 +283,7 @@ __global__ void __launch_bounds__(128) k_metric_ring(AsvDev d, int reseed)
     SeedRef r;
     if (!asv_seed_ref(d, g, r)) return;
     int *ok = d.ringok + ASV_RING * g + t;
-    if (!d.neg[g]) { if (lane == 0) *ok = 0; return; }
+    if (d.neg[g] != 1) { if (lane == 0) *ok = 0; return; }
     const SegDesc &S = d.segs[r.si];
     float4 p = reseed ? d.pos[g] : d.pos0[g];
     float fx = floorf(p.x), fy = floorf(p.y);
@@ -286,20 +303,27 @@ __global__ void __launch_bounds__(128) k_metric_ring(AsvDev d, int reseed)
     if (lane == 0) *ok = neg ? 0 : 1;
 }
 
-// writes M0 (reseed 0) or M (reseed 1)
+// writes M0 (reseed 0) or M (reseed 1, and the memo)
 __global__ void k_metric_combine(AsvDev d, int reseed)
 {
     SeedRef r;
     if (!asv_seed_ref(d, blockIdx.x * blockDim.x + threadIdx.x, r)) return;
     const int g = r.g;
     float *out = (reseed ? d.M : d.M0) + 8 * g;
-    float self[6];
-    for (int e = 0; e < 6; e++) self[e] = d.Mself[8 * g + e];
-    if (!d.neg[g]) {
-        for (int e = 0; e < 6; e++) out[e] = self[e];
+    const int neg = d.neg[g];
+    if (neg == 2) {
+        for (int e = 0; e < 6; e++) out[e] = d.Mmemo[8 * g + e];
         return;
     }
-    for (int ring = 0; ring < 2; ring++) {
+    float res[6];
+    float self[6];
+    for (int e = 0; e < 6; e++) self[e] = d.Mself[8 * g + e];
+    bool done = false;
+    if (!neg) {
+        for (int e = 0; e < 6; e++) res[e] = self[e];
+        done = true;
+    }
+    for (int ring = 0; ring < 2 && !done; ring++) {
         int t0 = ring == 0 ? 0 : 8, t1 = ring == 0 ? 8 : ASV_RING;
         float sum[6] = { 0, 0, 0, 0, 0, 0 };
         int n = 0;
@@ -310,13 +334,16 @@ __global__ void k_metric_combine(AsvDev d, int reseed)
             for (int e = 0; e < 6; e++) sum[e] = sum[e] + m[e];
         }
         if (n > 0) {
-            for (int e = 0; e < 6; e++) out[e] = sum[e] / (float)n;
-            return;
+            for (int e = 0; e < 6; e++) res[e] = sum[e] / (float)n;
+            done = true;
         }
     }
-    float o[6];
-    asv_m6_nearest_psd(self, o);
-    for (int e = 0; e < 6; e++) out[e] = o[e];
+    if (!done) asv_m6_nearest_psd(self, res);
+    for (int e = 0; e < 6; e++) out[e] = res[e];
+    if (reseed) {
+        for (int e = 0; e < 6; e++) d.Mmemo[8 * g + e] = res[e];
+        d.mkey[g] = asv_seed_key(d.segs[r.si], d.pos[g]);
+    }
 }
 
 void asv_launch_metric(const AsvDev &d, int reseed, cudaStream_t st)

@@ -240,6 +240,7 @@ __global__ void k_first_init(AsvDev d)
     if (i >= S.Kp) return;
     float4 p = d.pos0[g];
     d.pos[g] = p;
+    d.mkey[g] = -1;   // a new Lloyd run starts without reseed memo
 #pragma unroll
     for (int e = 0; e < 8; e++) d.M[8 * g + e] = d.M0[8 * g + e];
     int x = min(max((int)floorf(p.x), 0), S.W - 1);

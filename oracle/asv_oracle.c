@@ -293,40 +293,41 @@ int orc_density_adjust(const uint8_t *rgb, int W, int H, int D, const float *gri
 
 /* ======================================================================
  * Metric tensor from flow: GPU-AS/Image.cpp:874-1009 (matrix_slover).
- * Min-norm least squares (the reference calls Eigen BDCSVD::solve) is
- * computed here with a one-sided Jacobi SVD in FP64 and Eigen's rank rule:
- * keep singular values >= max(sigma_max * min(m,6) * FLT_EPSILON, FLT_MIN).
+ * Min-norm least squares in FP32, the reference's precision (it calls
+ * Eigen's float BDCSVD::solve, :946-961), computed here with a one-sided
+ * Jacobi SVD and Eigen's rank rule: keep singular values
+ * >= max(sigma_max * min(m,6) * FLT_EPSILON, FLT_MIN).
  * ==================================================================== */
-#define SVD_SWEEPS 40
+#define SVD_SWEEPS 30
 
-static void lsq_minnorm(int m, double U[18][6], const double *b, double x[6])
+static void lsq_minnorm(int m, float U[18][6], const float *b, float x[6])
 {
-    double V[6][6];
-    for (int r = 0; r < 6; r++) for (int c = 0; c < 6; c++) V[r][c] = r == c ? 1.0 : 0.0;
+    float V[6][6];
+    for (int r = 0; r < 6; r++) for (int c = 0; c < 6; c++) V[r][c] = r == c ? 1.0f : 0.0f;
     for (int sw = 0; sw < SVD_SWEEPS; sw++) {
         int rot = 0;
         for (int p = 0; p < 5; p++)
             for (int q = p + 1; q < 6; q++) {
-                double al = 0.0, be = 0.0, ga = 0.0;
+                float al = 0.0f, be = 0.0f, ga = 0.0f;
                 for (int i = 0; i < m; i++) {
                     al = al + U[i][p] * U[i][p];
                     be = be + U[i][q] * U[i][q];
                     ga = ga + U[i][p] * U[i][q];
                 }
-                if (ga == 0.0) continue;
-                if (fabs(ga) <= 1e-15 * sqrt(al * be)) continue;
-                double zeta = (be - al) / (2.0 * ga);
-                double t = 1.0 / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-                if (zeta < 0.0) t = -t;
-                double c = 1.0 / sqrt(1.0 + t * t);
-                double s = c * t;
+                if (ga == 0.0f) continue;
+                if (fabsf(ga) <= FLT_EPSILON * sqrtf(al * be)) continue;
+                float zeta = (be - al) / (2.0f * ga);
+                float t = 1.0f / (fabsf(zeta) + sqrtf(1.0f + zeta * zeta));
+                if (zeta < 0.0f) t = -t;
+                float c = 1.0f / sqrtf(1.0f + t * t);
+                float s = c * t;
                 for (int i = 0; i < m; i++) {
-                    double up = U[i][p], uq = U[i][q];
+                    float up = U[i][p], uq = U[i][q];
                     U[i][p] = c * up - s * uq;
                     U[i][q] = s * up + c * uq;
                 }
                 for (int i = 0; i < 6; i++) {
-                    double vp = V[i][p], vq = V[i][q];
+                    float vp = V[i][p], vq = V[i][q];
                     V[i][p] = c * vp - s * vq;
                     V[i][q] = s * vp + c * vq;
                 }
@@ -334,21 +335,21 @@ static void lsq_minnorm(int m, double U[18][6], const double *b, double x[6])
             }
         if (!rot) break;
     }
-    double sig[6], smax = 0.0;
+    float sig[6], smax = 0.0f;
     for (int j = 0; j < 6; j++) {
-        double a = 0.0;
+        float a = 0.0f;
         for (int i = 0; i < m; i++) a = a + U[i][j] * U[i][j];
-        sig[j] = sqrt(a);
+        sig[j] = sqrtf(a);
         if (sig[j] > smax) smax = sig[j];
     }
-    double thr = smax * ((double)(m < 6 ? m : 6) * (double)FLT_EPSILON);
-    if (thr < (double)FLT_MIN) thr = (double)FLT_MIN;
-    for (int r = 0; r < 6; r++) x[r] = 0.0;
+    float thr = smax * ((float)(m < 6 ? m : 6) * FLT_EPSILON);
+    if (thr < FLT_MIN) thr = FLT_MIN;
+    for (int r = 0; r < 6; r++) x[r] = 0.0f;
     for (int j = 0; j < 6; j++) {
         if (!(sig[j] >= thr)) continue;
-        double ub = 0.0;
+        float ub = 0.0f;
         for (int i = 0; i < m; i++) ub = ub + U[i][j] * b[i];
-        double coef = ub / (sig[j] * sig[j]);
+        float coef = (ub / sig[j]) / sig[j];
         for (int r = 0; r < 6; r++) x[r] = x[r] + V[r][j] * coef;
     }
 }
@@ -432,7 +433,7 @@ int orc_metric_solve(const float *fwd, const float *bwd, int W, int H, int D, fl
                      int frame, float M[6])
 {
     static const float expected_b[9] = { 3, 2, 3, 2, 1, 2, 3, 2, 3 };      /* :884 */
-    double A[18][6], b[18];
+    float A[18][6], b[18];
     int m = 0, id_b = 0;
     for (int oy = -1; oy < 2; oy++)
         for (int ox = -1; ox < 2; ox++, id_b++) {
@@ -442,24 +443,24 @@ int orc_metric_solve(const float *fwd, const float *bwd, int W, int H, int D, fl
             if (frame != D - 1) {                                            /* :898-913 */
                 float dx = (float)ox + round_half_up(fwd[o]);
                 float dy = (float)oy + round_half_up(fwd[o + 1]);
-                A[m][0] = (double)(dx * dx); A[m][1] = (double)(2.0f * dx * dy);
-                A[m][2] = (double)(2.0f * dx); A[m][3] = (double)(dy * dy);
-                A[m][4] = (double)(2.0f * dy); A[m][5] = 1.0;
+                A[m][0] = dx * dx; A[m][1] = 2.0f * dx * dy;
+                A[m][2] = 2.0f * dx; A[m][3] = dy * dy;
+                A[m][4] = 2.0f * dy; A[m][5] = 1.0f;
                 b[m++] = expected_b[id_b];
             }
             if (frame != 0) {                                                /* :915-930 */
                 float dx = round_half_up(bwd[o]) + (float)ox;
                 float dy = round_half_up(bwd[o + 1]) + (float)oy;
-                A[m][0] = (double)(dx * dx); A[m][1] = (double)(2.0f * dx * dy);
-                A[m][2] = (double)(-2.0f * dx); A[m][3] = (double)(dy * dy);
-                A[m][4] = (double)(-2.0f * dy); A[m][5] = 1.0;
+                A[m][0] = dx * dx; A[m][1] = 2.0f * dx * dy;
+                A[m][2] = -2.0f * dx; A[m][3] = dy * dy;
+                A[m][4] = -2.0f * dy; A[m][5] = 1.0f;
                 b[m++] = expected_b[id_b];
             }
         }
-    double x[6];
-    if (m == 0) { for (int k = 0; k < 6; k++) x[k] = 0.0; }
+    float x[6];
+    if (m == 0) { for (int k = 0; k < 6; k++) x[k] = 0.0f; }
     else lsq_minnorm(m, A, b, x);
-    for (int k = 0; k < 6; k++) M[k] = (float)x[k];
+    for (int k = 0; k < 6; k++) M[k] = x[k];
     return m6_negative(M);
 }
 
