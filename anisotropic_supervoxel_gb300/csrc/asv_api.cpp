@@ -274,7 +274,7 @@ asv_status asv_build_layout(asv_ctx *ctx)
         int nchunk = (int)((n + ASV_CHUNK - 1) / ASV_CHUNK);
         vox += (long long)nchunk * ASV_CHUNK;
         chunks += nchunk;
-        tiles += s.tiles_x * s.tiles_y * h.D;
+        tiles += s.tiles_x * s.tiles_y * ((h.D + ASV_TILE_Z - 1) / ASV_TILE_Z);
         seeds += ((h.Kp + 64 + 31) / 32) * 32;
         cells += h.W + h.H + h.D + 2 * h.g.wNum;
         ctx->maxpass = std::max(ctx->maxpass, h.npass);

@@ -13,8 +13,9 @@
 
 #define ASV_MAXP 32          // max JFA passes per Lloyd iteration
 #define ASV_CHUNK 2048       // voxels per block in the per-voxel kernels
-#define ASV_TILE_X 32        // JFA tile: 32 x 8 voxels of one slice
-#define ASV_TILE_Y 8
+#define ASV_TILE_X 16        // JFA tile: 16 x 16 voxels x ASV_TILE_Z slices (a warp
+#define ASV_TILE_Y 16        // covers 16 x 2 voxels: fewer distinct candidates per warp)
+#define ASV_TILE_Z 8
 #define ASV_RING 24          // 8 one-ring + 16 two-ring neighbours of the metric fallback
 #define ASV_POST_WORDS 16    // per-segment post-processing record
 

@@ -279,7 +279,7 @@ __global__ void k_draw(AsvDev d)
 // y-step..y+step; columns x-step..x+step; clamp to edge.
 //
 // The candidates are first reduced to a list of ids in first-occurrence
-// order (a candidate equal to one of the three most recently listed ids is
+// order (a candidate equal to one of the five most recently listed ids is
 // dropped), kept in shared memory, and the list is evaluated in one loop: a
 // warp pays for its longest list instead of for every candidate position
 // where some lane meets a new id.  A dropped or repeated id has the same
@@ -307,14 +307,14 @@ __device__ __forceinline__ void asv_jfa_voxel(const int32_t *__restrict__ in, in
 #pragma unroll
             for (int ox = 0; ox < 3; ox++) cand[(s * 3 + oy) * 3 + ox] = __ldg(in + zs[s] + ys[oy] + xs[ox]);
     const uchar4 c = __ldg(lab + z * sl + y * W + x);
-    int n = 0, r1 = -1, r2 = -1, r3 = -1;
+    int n = 0, r1 = -1, r2 = -1, r3 = -1, r4 = -1, r5 = -1;
 #pragma unroll
     for (int k = 0; k < 27; k++) {
         const int32_t l = cand[k];
-        if ((unsigned)l < (unsigned)Kp && l != r1 && l != r2 && l != r3) {
+        if ((unsigned)l < (unsigned)Kp && l != r1 && l != r2 && l != r3 && l != r4 && l != r5) {
             list[n * ASV_JFA_THREADS] = l;
             n++;
-            r3 = r2; r2 = r1; r1 = l;
+            r5 = r4; r4 = r3; r3 = r2; r2 = r1; r1 = l;
         }
     }
     const float cL = (float)c.x, ca = (float)c.y, cb = (float)c.z;
@@ -339,23 +339,29 @@ __device__ __forceinline__ void asv_jfa_voxel(const int32_t *__restrict__ in, in
     out[z * sl + y * W + x] = best;
 }
 
+// tile = ASV_TILE_X x ASV_TILE_Y voxels x ASV_TILE_Z slices; the tile
+// coordinates are derived once per tile, the slices walked inside it
 __global__ void __launch_bounds__(ASV_JFA_THREADS) k_jfa(AsvDev d, int pass,
                                                          const int32_t *__restrict__ in,
                                                          int32_t *__restrict__ out)
 {
     __shared__ int list[27 * ASV_JFA_THREADS];
-    const int lx = threadIdx.x & (ASV_TILE_X - 1), ly = threadIdx.x >> 5;
+    const int lx = threadIdx.x % ASV_TILE_X, ly = threadIdx.x / ASV_TILE_X;
     for (int t = blockIdx.x; t < d.total_tiles; t += gridDim.x) {
         const int si = asv_find_seg(d.tile_prefix, d.nseg, t);
         const SegDesc &S = d.segs[si];
         if (pass >= S.npass) continue;
         const int lt = t - d.tile_prefix[si];
         const int tx = lt % S.tiles_x, rest = lt / S.tiles_x;
-        const int ty = rest % S.tiles_y, z = rest / S.tiles_y;
+        const int ty = rest % S.tiles_y, z0 = (rest / S.tiles_y) * ASV_TILE_Z;
         const int x = tx * ASV_TILE_X + lx, y = ty * ASV_TILE_Y + ly;
         if (x >= S.W || y >= S.H) continue;
-        asv_jfa_voxel(in + S.vox_off, out + S.vox_off, d.lab + S.vox_off, d.jtab + 3 * S.seed_off,
-                      S.W, S.H, S.D, S.Kp, x, y, z, S.steps[pass], S.ratio[pass], list + threadIdx.x);
+        const int z1 = min(z0 + ASV_TILE_Z, S.D);
+        const int step = S.steps[pass];
+        const float ratio = S.ratio[pass];
+        for (int z = z0; z < z1; z++)
+            asv_jfa_voxel(in + S.vox_off, out + S.vox_off, d.lab + S.vox_off, d.jtab + 3 * S.seed_off,
+                          S.W, S.H, S.D, S.Kp, x, y, z, step, ratio, list + threadIdx.x);
     }
 }
 
@@ -366,15 +372,18 @@ __global__ void __launch_bounds__(ASV_JFA_THREADS) k_jfa_single(AsvDev d, const 
 {
     __shared__ int list[27 * ASV_JFA_THREADS];
     const SegDesc &S = d.segs[0];
-    const int lx = threadIdx.x & (ASV_TILE_X - 1), ly = threadIdx.x >> 5;
-    const int ntiles = S.tiles_x * S.tiles_y * S.D;
+    const int lx = threadIdx.x % ASV_TILE_X, ly = threadIdx.x / ASV_TILE_X;
+    const int tiles_z = (S.D + ASV_TILE_Z - 1) / ASV_TILE_Z;
+    const int ntiles = S.tiles_x * S.tiles_y * tiles_z;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int tx = t % S.tiles_x, rest = t / S.tiles_x;
-        const int ty = rest % S.tiles_y, z = rest / S.tiles_y;
+        const int ty = rest % S.tiles_y, z0 = (rest / S.tiles_y) * ASV_TILE_Z;
         const int x = tx * ASV_TILE_X + lx, y = ty * ASV_TILE_Y + ly;
         if (x >= S.W || y >= S.H) continue;
-        asv_jfa_voxel(in, out, d.lab + S.vox_off, d.jtab + 3 * S.seed_off, S.W, S.H, S.D, S.Kp,
-                      x, y, z, step, ratio, list + threadIdx.x);
+        const int z1 = min(z0 + ASV_TILE_Z, S.D);
+        for (int z = z0; z < z1; z++)
+            asv_jfa_voxel(in, out, d.lab + S.vox_off, d.jtab + 3 * S.seed_off, S.W, S.H, S.D, S.Kp,
+                          x, y, z, step, ratio, list + threadIdx.x);
     }
 }
 
