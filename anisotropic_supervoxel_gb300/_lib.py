@@ -84,6 +84,8 @@ SIGNATURES = {
     "asv_get_stream": (c_int, [c_void_p, P(c_void_p)]),
     "asv_synchronize": (c_int, [c_void_p]),
     "asv_clip_bytes": (c_size_t, [c_int, c_int, c_int, c_int]),
+    "asv_check_dead_seeds_noalloc": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int,
+                                             c_void_p]),
     # include/asv_host.h
     "asv_synth_clip": (c_int, [P(SynthParams), c_void_p, c_void_p, c_void_p]),
     "asv_preprocess_frame": (c_int, [c_void_p, c_int, c_int, c_void_p]),

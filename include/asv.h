@@ -173,6 +173,27 @@ asv_status asv_synchronize(asv_ctx *ctx);
 /* bytes of device memory a clip of this size needs (admission control) */
 size_t asv_clip_bytes(int W, int H, int D, int K);
 
+/* ---- post-processing without device allocation ------------------------- */
+
+/* No counterpart in the reference.  The same dead-seed relabel and -1 fill
+ * as asv_check_dead_seeds, for callers that cannot let a library allocate
+ * device memory: hosts that give out every device byte from their own pool,
+ * or latency-bound stages where cudaMalloc/cudaFree would synchronize the
+ * device mid-pipeline.  The caller passes device buffers (d_raw: W*H*D
+ * int32 raw labels in [-1, Kp); d_out: W*H*D int32) and an optional stream;
+ * no context is needed.  Scratch is a fixed array of about 320 KiB inside
+ * the library's device image, held by every device the library is loaded on
+ * until the process exits.  Limits: W*H*D <= 2^25 voxels, Kp <= 32767
+ * (ASV_ERR_BAD_ARG beyond).  The first call on a device resolves the
+ * scratch address (make it before any stream capture).  All calls on a
+ * device share the scratch and leave it holding their data; calls whose
+ * work overlaps on the GPU race, so serialize them.  Run with the buffers'
+ * device current. */
+#define ASV_NOALLOC_MAX_VOXELS (1LL << 25)
+#define ASV_NOALLOC_MAX_SEEDS 32767
+asv_status asv_check_dead_seeds_noalloc(const int32_t *d_raw, int32_t *d_out, int W, int H, int D,
+                                        int Kp, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
