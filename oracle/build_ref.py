@@ -1,0 +1,284 @@
+"""Compiles the reference's own GLSL shaders as C++ (with the glm copy the
+reference vendors) into oracle/_ref/libref_shaders.so, the checker of the
+CPU restatement's shader maths.
+
+TEST INFRASTRUCTURE ONLY.  The shader files are read where they lie under
+the reference tree; the transformed C++ and the library go to oracle/_ref/
+(git-ignored, never committed).  The transform is textual and mechanical:
+drop `#version` and `layout(...)` qualifiers, turn `in`/`out`/`uniform`
+declarations into namespace globals, interface blocks into structs, and
+`main` into `shader_main`.  The harness below (this project's code) supplies
+GL's builtins: `texture()` as nearest-texel sampling with clamp-to-edge,
+`gl_Position`, `gl_Layer`, `gl_in`, `EmitVertex`, `EndPrimitive`.  GLSL
+float literals are single precision: compiled with -fsingle-precision-constant;
+no FMA contraction (-ffp-contract=off); pow() is taken correctly rounded.
+"""
+import os
+import re
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(HERE, "_ref")
+LIB = os.path.join(OUT, "libref_shaders.so")
+REF = os.environ.get("ASV_REFERENCE_ROOT", "/root/reference")
+SHADERS = os.path.join(REF, "GPU-AS", "shaders")
+GLM = os.path.join(REF, "includes")
+
+PROGRAMS = {
+    "rgb2lab": ["RGB2LAB.vs", "RGB2LAB.gs", "RGB2LAB.fs"],
+    "derivative": ["derivative_t.vs", "derivative_t.gs"],
+    "flood": ["flood.vs", "flood.gs"],
+    "centroids": ["centroids.vs"],
+    "aver": ["aver_exception.vs"],
+    "label_replace": ["label_replace.vs", "label_replace.gs"],
+}
+
+
+def glsl_to_cpp(src, stage):
+    s = re.sub(r"//[^\n]*", "", src)
+    s = re.sub(r"/\*.*?\*/", "", s, flags=re.S)
+    s = re.sub(r"#version[^\n]*", "", s)
+    s = re.sub(r"layout\s*\([^)]*\)\s*(in|out)\s*;", "", s)
+    s = re.sub(r"layout\s*\([^)]*\)\s*", "", s)
+
+    def block(m):
+        kind, name, body, inst, arr = m.group(1), m.group(2), m.group(3), m.group(4), m.group(5)
+        t = f"{name}_{kind}"
+        return f"struct {t} {{{body}}}; {t} {inst}{'[1]' if arr else ''};"
+
+    s = re.sub(r"\b(in|out)\s+(\w+)\s*\{([^}]*)\}\s*(\w+)\s*(\[\s*\])?\s*;", block, s)
+    s = re.sub(r"\bflat\s+", "", s)
+    s = re.sub(r"\buniform\s+sampler3D\b", "Sampler3D", s)
+    s = re.sub(r"\buniform\s+", "", s)
+    s = re.sub(r"^(\s*)(in|out)\s+(?=\w+\s+\w+\s*;)", r"\1", s, flags=re.M)
+    s = re.sub(r"\bvoid\s+main\s*\(\s*\)", "void shader_main()", s)
+    s = re.sub(r"\.(xyz|rgb|xy)\b(?!\s*\()", r".\1()", s)
+    return s
+
+
+HARNESS = r"""
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+
+// GLSL float vectors: non-template operators, so int operands convert to
+// float as GLSL's implicit conversion does; swizzles .xy/.xyz/.rgb are
+// accessor proxies (the transform rewrites `.xyz` as `.xyz()`).
+struct vec2 {
+    union { float x; float r; };
+    union { float y; float g; };
+    vec2() : x(0), y(0) {}
+    vec2(float a, float b) : x(a), y(b) {}
+};
+struct vec3 {
+    union { float x; float r; };
+    union { float y; float g; };
+    union { float z; float b; };
+    vec3() : x(0), y(0), z(0) {}
+    vec3(float a, float b, float c) : x(a), y(b), z(c) {}
+    vec3 &operator+=(vec3 o) { x = x + o.x; y = y + o.y; z = z + o.z; return *this; }
+    vec3 &operator+=(float o) { x = x + o; y = y + o; z = z + o; return *this; }
+    vec3 &operator-=(float o) { x = x - o; y = y - o; z = z - o; return *this; }
+    vec3 &operator*=(float o) { x = x * o; y = y * o; z = z * o; return *this; }
+    vec3 &operator/=(float o) { x = x / o; y = y / o; z = z / o; return *this; }
+    struct Swz2 xy();
+};
+struct ivec3 { int x, y, z; ivec3() : x(0), y(0), z(0) {} ivec3(int a, int b, int c) : x(a), y(b), z(c) {} };
+struct Swz2 { float &a, &b; operator vec2() const { return vec2(a, b); } };
+struct Swz3 {
+    float &a, &b, &c;
+    operator vec3() const { return vec3(a, b, c); }
+    Swz3 &operator=(vec3 v) { a = v.x; b = v.y; c = v.z; return *this; }
+    Swz3 &operator/=(float o) { a = a / o; b = b / o; c = c / o; return *this; }
+    Swz3 &operator*=(float o) { a = a * o; b = b * o; c = c * o; return *this; }
+};
+struct vec4 {
+    union { float x; float r; };
+    union { float y; float g; };
+    union { float z; float b; };
+    union { float w; float a; };
+    vec4() : x(0), y(0), z(0), w(0) {}
+    vec4(float p, float q, float s, float t) : x(p), y(q), z(s), w(t) {}
+    vec4(vec2 v, float s, float t) : x(v.x), y(v.y), z(s), w(t) {}
+    vec4(vec3 v, float t) : x(v.x), y(v.y), z(v.z), w(t) {}
+    Swz3 xyz() { return Swz3{x, y, z}; }
+    Swz3 rgb() { return Swz3{x, y, z}; }
+    Swz2 xy() { return Swz2{x, y}; }
+};
+inline Swz2 vec3::xy() { return Swz2{x, y}; }
+static inline vec2 operator*(float s, vec2 v) { return vec2(s * v.x, s * v.y); }
+static inline vec2 operator-(vec2 v, float s) { return vec2(v.x - s, v.y - s); }
+static inline vec3 operator+(vec3 a, vec3 b) { return vec3(a.x + b.x, a.y + b.y, a.z + b.z); }
+static inline vec3 operator-(vec3 a, vec3 b) { return vec3(a.x - b.x, a.y - b.y, a.z - b.z); }
+static inline vec3 operator*(vec3 a, vec3 b) { return vec3(a.x * b.x, a.y * b.y, a.z * b.z); }
+static inline vec3 operator+(vec3 a, float s) { return vec3(a.x + s, a.y + s, a.z + s); }
+static inline vec3 operator-(vec3 a, float s) { return vec3(a.x - s, a.y - s, a.z - s); }
+static inline vec3 operator*(vec3 a, float s) { return vec3(a.x * s, a.y * s, a.z * s); }
+static inline vec3 operator*(float s, vec3 a) { return vec3(s * a.x, s * a.y, s * a.z); }
+static inline vec3 operator/(vec3 a, float s) { return vec3(a.x / s, a.y / s, a.z / s); }
+static inline float dot(vec3 a, vec3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+static inline float floor(float v) { return std::floor(v); }
+static inline vec3 floor(vec3 v) { return vec3(std::floor(v.x), std::floor(v.y), std::floor(v.z)); }
+static inline vec3 abs(vec3 v) { return vec3(std::fabs(v.x), std::fabs(v.y), std::fabs(v.z)); }
+
+struct Sampler3D { const float *data = nullptr; int W = 1, H = 1, D = 1, C = 4; };
+
+static inline vec4 texture(const Sampler3D &s, vec3 uv)
+{
+    int x = (int)std::floor(uv.x * (float)s.W), y = (int)std::floor(uv.y * (float)s.H),
+        z = (int)std::floor(uv.z * (float)s.D);
+    x = x < 0 ? 0 : (x >= s.W ? s.W - 1 : x);
+    y = y < 0 ? 0 : (y >= s.H ? s.H - 1 : y);
+    z = z < 0 ? 0 : (z >= s.D ? s.D - 1 : z);
+    const float *p = s.data + (((size_t)z * s.H + y) * s.W + x) * s.C;
+    return vec4(p[0], s.C > 1 ? p[1] : 0.0f, s.C > 2 ? p[2] : 0.0f, s.C > 3 ? p[3] : 1.0f);
+}
+
+#define GL_BUILTINS                                                                 \
+    struct gl_PerVertex { vec4 gl_Position; };                                      \
+    static gl_PerVertex gl_in[1];                                                   \
+    static vec4 gl_Position;                                                        \
+    static int gl_Layer;                                                            \
+    static inline void EmitVertex() {}                                              \
+    static inline void EndPrimitive() {}                                            \
+    static inline float pow(float a, float b) { return (float)std::pow((double)a, (double)b); }
+"""
+
+WRAPPERS = r"""
+static float wr_of(int n) { return (float)(1.0 / (float)n); }   // width_ratio = 1.0 / width_f (Image.cpp:329-331)
+
+extern "C" void ref_rgb2lab(const uint8_t *rgb, long n, float *out3)
+{
+    for (long i = 0; i < n; i++) {
+        rgb2lab_fs::f_color = vec3((float)rgb[3 * i] / 255.0f, (float)rgb[3 * i + 1] / 255.0f,
+                                   (float)rgb[3 * i + 2] / 255.0f);
+        rgb2lab_fs::shader_main();
+        out3[3 * i] = rgb2lab_fs::FragColor.x;
+        out3[3 * i + 1] = rgb2lab_fs::FragColor.y;
+        out3[3 * i + 2] = rgb2lab_fs::FragColor.z;
+    }
+}
+
+// rgbf: unorm texel values (c / 255), 3 per voxel
+extern "C" void ref_derivative(const float *rgbf, int W, int H, int D, float *out)
+{
+    Sampler3D s; s.data = rgbf; s.W = W; s.H = H; s.D = D; s.C = 3;
+    derivative_vs::width_ratio = derivative_gs::width_ratio = wr_of(W);
+    derivative_vs::height_ratio = derivative_gs::height_ratio = wr_of(H);
+    derivative_vs::depth_ratio = derivative_gs::depth_ratio = wr_of(D);
+    derivative_gs::texels = s;
+    for (int z = 0; z < D; z++) for (int y = 0; y < H; y++) for (int x = 0; x < W; x++) {
+        derivative_vs::aPos = ivec3(x, y, z);
+        derivative_vs::shader_main();
+        derivative_gs::gs_in[0].gLayer = derivative_vs::vs_out.gLayer;
+        derivative_gs::gs_in[0].gTex = derivative_vs::vs_out.gTex;
+        derivative_gs::shader_main();
+        out[((size_t)z * H + y) * W + x] = derivative_gs::gradient_t;
+    }
+}
+
+// labels, scolor, mf3, ml3: RGBA32F volumes (4 floats / voxel); image: LAB, 3 floats / voxel
+extern "C" void ref_flood(const float *labels, const float *scolor, const float *mf3, const float *ml3,
+                          const float *image, int W, int H, int D, float step, float ratio, float *out4)
+{
+    Sampler3D t; t.W = W; t.H = H; t.D = D;
+    flood_gs::texels = t; flood_gs::texels.data = labels;
+    flood_gs::sColorImage = t; flood_gs::sColorImage.data = scolor;
+    flood_gs::seedMatrixFirst3 = t; flood_gs::seedMatrixFirst3.data = mf3;
+    flood_gs::seedMatrixLast3 = t; flood_gs::seedMatrixLast3.data = ml3;
+    flood_gs::image = t; flood_gs::image.data = image; flood_gs::image.C = 3;
+    flood_vs::width_ratio = flood_gs::width_ratio = wr_of(W);
+    flood_vs::height_ratio = flood_gs::height_ratio = wr_of(H);
+    flood_vs::depth_ratio = flood_gs::depth_ratio = wr_of(D);
+    flood_gs::step = step;
+    flood_gs::ratio = ratio;
+    for (int z = 0; z < D; z++) for (int y = 0; y < H; y++) for (int x = 0; x < W; x++) {
+        flood_vs::aPos = ivec3(x, y, z);
+        flood_vs::shader_main();
+        flood_gs::gs_in[0].gPos = flood_vs::vs_out.gPos;
+        flood_gs::gs_in[0].gTex = flood_vs::vs_out.gTex;
+        flood_gs::shader_main();
+        float *o = out4 + 4 * (((size_t)z * H + y) * W + x);
+        o[0] = flood_gs::f_color.x; o[1] = flood_gs::f_color.y; o[2] = flood_gs::f_color.z; o[3] = flood_gs::f_color.w;
+    }
+}
+
+// the render-target texel a voxel labelled `id` adds into (id < 0 -> the slot after the seeds)
+extern "C" void ref_centroid_target(float id, int W, int H, float ac_seeds_num, int *tx, int *ty)
+{
+    static float lab[4];
+    lab[0] = lab[1] = lab[2] = 0.5f; lab[3] = id;
+    static float img[3] = {0, 0, 0};
+    Sampler3D t; t.data = lab; t.W = t.H = t.D = 1;
+    centroids_vs::texels = t;
+    centroids_vs::image = t; centroids_vs::image.data = img; centroids_vs::image.C = 3;
+    centroids_vs::width_ratio = wr_of(W);
+    centroids_vs::height_ratio = wr_of(H);
+    centroids_vs::depth_ratio = 1.0f;
+    centroids_vs::ac_seeds_num = ac_seeds_num;
+    centroids_vs::aPos = ivec3(0, 0, 0);
+    centroids_vs::shader_main();
+    vec4 p = centroids_vs::gl_Position;
+    *tx = (int)std::floor((p.x + 1.0f) * 0.5f * (float)W);   // viewport transform
+    *ty = (int)std::floor((p.y + 1.0f) * 0.5f * (float)H);
+}
+
+// sum_pos, sum_color: RGBA32F W x H x D volumes (slice 0 holds the sums);
+// image: LAB 3 floats / voxel.  For seed `id`: centroid position (x, y, z, id)
+// and colour.
+extern "C" void ref_aver_exception(const float *sum_pos, const float *sum_color, const float *image,
+                                   int W, int H, int D, int id, float *pos4, float *col3)
+{
+    Sampler3D t; t.W = W; t.H = H; t.D = D;
+    aver_vs::sum_pos = t; aver_vs::sum_pos.data = sum_pos;
+    aver_vs::sum_color = t; aver_vs::sum_color.data = sum_color;
+    aver_vs::image = t; aver_vs::image.data = image; aver_vs::image.C = 3;
+    aver_vs::width = (float)W; aver_vs::height = (float)H; aver_vs::depth = (float)D;
+    // seeds_index vertex attributes (Image.cpp:108-125)
+    int slice = W * H;
+    float tex_x = (float)((float)(id % W) + 0.5), tex_y = (float)((float)(id / W) + 0.5),
+          tex_z = (float)((float)(id / slice) + 0.5);
+    aver_vs::texPos = vec3(tex_x * wr_of(W), tex_y * wr_of(H), tex_z * wr_of(D));
+    aver_vs::seedId = (float)id;
+    aver_vs::shader_main();
+    vec4 c = aver_vs::vs_out.gCentroidPos;
+    pos4[0] = c.x; pos4[1] = c.y; pos4[2] = c.z; pos4[3] = c.w;
+    vec3 k = aver_vs::vs_out.gCentroidColor;
+    col3[0] = k.x; col3[1] = k.y; col3[2] = k.z;
+}
+"""
+
+
+def build(force=False):
+    """Transforms and compiles the reference shaders; returns the library path,
+    or None when the reference tree is not present."""
+    if not os.path.isdir(SHADERS):
+        return None
+    srcs = [os.path.join(SHADERS, f) for p in PROGRAMS.values() for f in p]
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(
+            [os.path.getmtime(f) for f in srcs] + [os.path.getmtime(__file__)]):
+        return LIB
+    os.makedirs(OUT, exist_ok=True)
+    parts = [HARNESS]
+    for prog, files in PROGRAMS.items():
+        for f in files:
+            stage = f.rsplit(".", 1)[1]
+            ns = f"{prog}_{stage}"
+            body = glsl_to_cpp(open(os.path.join(SHADERS, f)).read(), stage)
+            parts.append(f"namespace {ns} {{\nGL_BUILTINS\n{body}\n}}\n")
+    parts.append(WRAPPERS)
+    cpp = os.path.join(OUT, "ref_shaders.cpp")
+    with open(cpp, "w") as fh:
+        fh.write("\n".join(parts))
+    tmp = LIB + ".tmp"
+    cmd = ["g++", "-std=c++17", "-O1", "-fPIC", "-shared", "-fsingle-precision-constant",
+           "-ffp-contract=off", "-w", "-o", tmp, cpp]
+    p = subprocess.run(cmd, capture_output=True, text=True)
+    if p.returncode != 0:
+        raise RuntimeError("reference shader build failed:\n" + p.stderr[-6000:])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force=True))

@@ -1,0 +1,93 @@
+"""Generates the golden fixtures of tests/golden/ from the reference's own
+shaders compiled as C++ (oracle/build_ref.py; needs the reference tree).
+
+    python tests/golden/make_golden.py
+
+Fixtures (npz): inputs plus the compiled reference shaders' outputs for
+RGB2LAB.fs (a seeded sample of RGB values), derivative_t.gs, flood.gs (one
+pass at several steps) and aver_exception.vs.  tests/test_golden.py checks
+the CPU restatement and the CUDA path against them.
+"""
+import ctypes
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.dirname(HERE))
+
+
+def main():
+    from oracle import build_ref, oracle
+    import test_ref_pin as pin
+    import anisotropic_supervoxel_gb300 as asv
+
+    path = build_ref.build()
+    if path is None:
+        raise SystemExit("reference tree not present")
+    lib = ctypes.CDLL(path)
+    V = ctypes.c_void_p
+    lib.ref_rgb2lab.argtypes = [V, ctypes.c_long, V]
+    lib.ref_derivative.argtypes = [V, ctypes.c_int, ctypes.c_int, ctypes.c_int, V]
+    lib.ref_flood.argtypes = [V, V, V, V, V, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                              ctypes.c_float, ctypes.c_float, V]
+    lib.ref_aver_exception.argtypes = [V, V, V, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_int, V, V]
+    P = pin.P
+    rng = np.random.default_rng(20240610)
+
+    rgb = rng.integers(0, 256, (16384, 3), dtype=np.uint8)
+    np.savez_compressed(os.path.join(HERE, "rgb2lab_sample.npz"), rgb=rgb, lab=pin.ref_lab(lib, rgb))
+
+    clip = asv.synth_clip(24, 18, 6, n_ellipses=4, noise_sigma=6.0, seed=77)[0]
+    D, H, W, _ = clip.shape
+    rgbf = np.ascontiguousarray(clip.astype(np.float32) / np.float32(255.0))
+    g = np.zeros((D, H, W), np.float32)
+    lib.ref_derivative(P(rgbf), W, H, D, P(g))
+    np.savez_compressed(os.path.join(HERE, "derivative.npz"), rgb=clip, gradient=g)
+
+    lab4 = oracle.rgb2lab(clip)
+    assert np.array_equal(lab4[..., :3].astype(np.float32), pin.ref_lab(lib, clip))
+    k = 20
+    for step, psd in ((1, True), (3, False), (7, True)):
+        seeds = pin._flood_case(rng, W, H, D, k, psd)
+        labels = rng.integers(-1, k, (D, H, W)).astype(np.int32)
+        ratio = np.float32(0.125)
+        lt, sc, f3, l3, img = pin._textures(seeds, labels, lab4)
+        out = np.zeros((D, H, W, 4), np.float32)
+        lib.ref_flood(P(lt), P(sc), P(f3), P(l3), P(img), W, H, D, float(step), float(ratio), P(out))
+        np.savez_compressed(os.path.join(HERE, f"flood_step{step}.npz"), rgb=clip, seeds=seeds,
+                            labels=labels, step=step, ratio=ratio, out=out[..., 3].astype(np.int32))
+
+    kp = 20
+    sums = np.zeros((kp + 1, 7), np.int64)
+    cnt = rng.integers(1, 60, kp + 1)
+    cnt[[0, 3, kp - 1]] = 0
+    for i in range(kp + 1):
+        c = int(cnt[i])
+        if c:
+            xs, ys, zs = rng.integers(0, W, c), rng.integers(0, H, c), rng.integers(0, D, c)
+            sums[i, :4] = [(2 * xs + 1).sum(), (2 * ys + 1).sum(), (2 * zs + 1).sum(), c]
+            sums[i, 4:] = rng.integers(0, 256, (c, 3)).sum(0)
+    sp = np.zeros((D, H, W, 4), np.float32)
+    scol = np.zeros((D, H, W, 4), np.float32)
+    for i in range(kp + 1):
+        y, x = divmod(i, W)
+        sp[0, y, x] = [np.float32(sums[i, 0]) * np.float32(0.5), np.float32(sums[i, 1]) * np.float32(0.5),
+                       np.float32(sums[i, 2]) * np.float32(0.5), np.float32(sums[i, 3])]
+        scol[0, y, x] = [np.float32(sums[i, 4]), np.float32(sums[i, 5]), np.float32(sums[i, 6]),
+                         np.float32(sums[i, 3])]
+    img = np.ascontiguousarray(lab4[..., :3].astype(np.float32))
+    pos = np.zeros((kp, 4), np.float32)
+    col = np.zeros((kp, 3), np.float32)
+    for i in range(kp):
+        lib.ref_aver_exception(P(sp), P(scol), P(img), W, H, D, i, P(pos[i]), P(col[i]))
+    np.savez_compressed(os.path.join(HERE, "aver_exception.npz"), rgb=clip, sums=sums, pos=pos, col=col)
+    print("fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,160 @@
+"""Pins the CPU restatement to the reference's own shader code.
+
+oracle/build_ref.py compiles the reference's GLSL files (read where they lie
+in the reference tree) as C++ with a harness that supplies GL's sampling and
+builtins; these tests compare the restatement with those compiled shaders.
+They need the reference tree, so they skip where it is absent; the golden
+fixtures under tests/golden/ carry the same answers everywhere.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from conftest import small_clip
+
+
+@pytest.fixture(scope="module")
+def ref():
+    from oracle import build_ref
+    path = build_ref.build()
+    if path is None:
+        pytest.skip("reference tree not present")
+    lib = ctypes.CDLL(path)
+    V = ctypes.c_void_p
+    lib.ref_rgb2lab.argtypes = [V, ctypes.c_long, V]
+    lib.ref_derivative.argtypes = [V, ctypes.c_int, ctypes.c_int, ctypes.c_int, V]
+    lib.ref_flood.argtypes = [V, V, V, V, V, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                              ctypes.c_float, ctypes.c_float, V]
+    lib.ref_centroid_target.argtypes = [ctypes.c_float, ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                        V, V]
+    lib.ref_aver_exception.argtypes = [V, V, V, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_int, V, V]
+    return lib
+
+
+def P(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def ref_lab(ref, rgb):
+    rgb = np.ascontiguousarray(rgb, np.uint8)
+    out = np.zeros(rgb.shape[:-1] + (3,), np.float32)
+    ref.ref_rgb2lab(P(rgb), rgb.size // 3, P(out))
+    return out
+
+
+def test_rgb2lab_all_2e24(ref, orc):
+    v = np.arange(1 << 24, dtype=np.uint32)
+    rgb = np.stack([(v >> 16) & 255, (v >> 8) & 255, v & 255], -1).astype(np.uint8)
+    want = ref_lab(ref, rgb)
+    assert np.array_equal(want, np.floor(want))          # the shader writes integers
+    got = orc.rgb2lab(rgb)[:, :3].astype(np.float32)
+    bad = np.nonzero((got != want).any(-1))[0]
+    assert bad.size == 0, f"{bad.size} RGB values differ, first {bad[:8]}"
+
+
+def test_derivative(ref, orc, asv):
+    for rgb in (small_clip(asv, 23, 17, 6, seed=2)[0],
+                np.random.default_rng(3).integers(0, 256, (5, 11, 13, 3), dtype=np.uint8)):
+        D, H, W, _ = rgb.shape
+        rgbf = np.ascontiguousarray(rgb.astype(np.float32) / np.float32(255.0))
+        g = np.zeros((D, H, W), np.float32)
+        ref.ref_derivative(P(rgbf), W, H, D, P(g))
+        assert np.array_equal(orc.gradient_half(rgb), g.astype(np.float16).view(np.uint16))
+
+
+def _flood_case(rng, W, H, D, k, psd=True):
+    seeds = np.zeros((k, 12), np.float32)
+    vox = rng.choice(W * H * D, k, replace=False)          # distinct seed voxels
+    seeds[:, 0] = vox % W + 0.5
+    seeds[:, 1] = (vox // W) % H + 0.5
+    seeds[:, 2] = vox // (W * H) + 0.5
+    seeds[:, 3:6] = rng.uniform(0, 255, (k, 3)).astype(np.float32)
+    A = rng.normal(0, 0.7, (k, 3, 3)).astype(np.float32)
+    M = np.einsum("kij,kil->kjl", A, A) + (np.eye(3, dtype=np.float32) * 0.2)
+    seeds[:, 6:12] = M[:, [0, 0, 0, 1, 1, 2], [0, 1, 2, 1, 2, 2]]
+    if not psd:
+        seeds[: k // 4, 6:12] *= -1.0
+    return seeds
+
+
+def _textures(seeds, labels, lab4):
+    D, H, W = labels.shape
+    k = seeds.shape[0]
+    ids = np.arange(k, dtype=np.float32)
+    rec = np.concatenate([seeds[:, :3], ids[:, None]], 1)
+    lt = np.where(labels[..., None] >= 0, rec[np.clip(labels, 0, None)], np.float32(-1)).astype(np.float32)
+    sc = np.full((D, H, W, 4), -1, np.float32)
+    f3 = np.full((D, H, W, 4), -1, np.float32)
+    l3 = np.full((D, H, W, 4), -1, np.float32)
+    x, y, z = seeds[:, 0].astype(int), seeds[:, 1].astype(int), seeds[:, 2].astype(int)
+    sc[z, y, x] = np.concatenate([seeds[:, 3:6], ids[:, None]], 1)
+    f3[z, y, x] = np.concatenate([seeds[:, 6:9], ids[:, None]], 1)
+    l3[z, y, x] = np.concatenate([seeds[:, 9:12], ids[:, None]], 1)
+    img = np.ascontiguousarray(lab4[..., :3].astype(np.float32))
+    return [np.ascontiguousarray(a) for a in (lt, sc, f3, l3)] + [img]
+
+
+@pytest.mark.parametrize("step,psd", [(1, True), (2, True), (3, False), (6, True), (11, False)])
+def test_flood(ref, orc, asv, step, psd):
+    W, H, D, k = 29, 21, 9, 40
+    rgb = small_clip(asv, W, H, D, seed=step)[0]
+    lab4 = orc.rgb2lab(rgb)
+    rng = np.random.default_rng(step)
+    seeds = _flood_case(rng, W, H, D, k, psd)
+    labels = rng.integers(-1, k, (D, H, W)).astype(np.int32)
+    ratio = np.float32(0.0873)
+    lt, sc, f3, l3, img = _textures(seeds, labels, lab4)
+    out = np.zeros((D, H, W, 4), np.float32)
+    ref.ref_flood(P(lt), P(sc), P(f3), P(l3), P(img), W, H, D, float(step), float(ratio), P(out))
+    want = out[..., 3].astype(np.int32)
+    got = orc.jfa_pass(labels, lab4, seeds, step, ratio)
+    assert np.array_equal(got, want)
+
+
+def test_centroid_slot_mapping(ref):
+    for W, H in ((240, 160), (320, 240), (146, 120), (640, 480), (1280, 720)):
+        for kp in (187, 936, 1947, 2000):
+            for i in list(range(0, kp, 7)) + [kp - 1, -1]:
+                tx, ty = ctypes.c_int(), ctypes.c_int()
+                ref.ref_centroid_target(float(i), W, H, float(kp), ctypes.byref(tx), ctypes.byref(ty))
+                slot = kp if i < 0 else i
+                assert (tx.value, ty.value) == (slot % W, slot // W)
+
+
+def test_aver_exception(ref, orc, asv):
+    W, H, D, kp = 37, 13, 7, 60
+    rgb = small_clip(asv, W, H, D, seed=9)[0]
+    lab4 = orc.rgb2lab(rgb)
+    rng = np.random.default_rng(4)
+    sums = np.zeros((kp + 1, 7), np.int64)
+    cnt = rng.integers(1, 400, kp + 1)
+    dead = [0, 1, 5, 6, 30, kp - 1]              # includes seed 0 (reads texel W-1) and the last seed
+    cnt[dead] = 0
+    for i in range(kp + 1):
+        c = int(cnt[i])
+        if c == 0:
+            continue
+        xs = rng.integers(0, W, c); ys = rng.integers(0, H, c); zs = rng.integers(0, D, c)
+        sums[i, :4] = [(2 * xs + 1).sum(), (2 * ys + 1).sum(), (2 * zs + 1).sum(), c]
+        sums[i, 4:] = rng.integers(0, 256, (c, 3)).sum(0)
+    pos0 = np.zeros((kp, 3), np.float32)
+    slab0 = np.zeros((kp, 3), np.float32)
+    got_pos, got_col = orc.finalize((D, H, W), sums, lab4, pos0, slab0)
+    sp = np.zeros((D, H, W, 4), np.float32)
+    scol = np.zeros((D, H, W, 4), np.float32)
+    for i in range(kp + 1):                         # texels of slice 0 hold the sums (slot i at (i % W, i // W))
+        y, x = divmod(i, W)
+        sp[0, y, x] = [np.float32(sums[i, 0]) * np.float32(0.5), np.float32(sums[i, 1]) * np.float32(0.5),
+                       np.float32(sums[i, 2]) * np.float32(0.5), np.float32(sums[i, 3])]
+        scol[0, y, x] = [np.float32(sums[i, 4]), np.float32(sums[i, 5]), np.float32(sums[i, 6]),
+                         np.float32(sums[i, 3])]
+    img = np.ascontiguousarray(lab4[..., :3].astype(np.float32))
+    for i in range(kp):
+        p4 = np.zeros(4, np.float32)
+        c3 = np.zeros(3, np.float32)
+        ref.ref_aver_exception(P(sp), P(scol), P(img), W, H, D, i, P(p4), P(c3))
+        assert np.array_equal(p4[:3], got_pos[i]), i
+        assert np.array_equal(c3, got_col[i]), i
+        assert p4[3] == i
