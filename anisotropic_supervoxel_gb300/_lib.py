@@ -43,6 +43,11 @@ class Stats(ctypes.Structure):
                 ("total_ms", ctypes.c_double), ("launches", c_int)]
 
 
+class StreamInfo(ctypes.Structure):
+    _fields_ = [(n, c_int) for n in ("blocks", "next_block", "block_start", "block_end",
+                                     "frames_needed", "seeds_placed", "block_Kp")]
+
+
 class SynthParams(ctypes.Structure):
     _fields_ = [("W", c_int), ("H", c_int), ("frame0", c_int), ("nframes", c_int),
                 ("n_ellipses", c_int), ("noise_sigma", c_float), ("vmax", c_float),
@@ -86,6 +91,9 @@ SIGNATURES = {
     "asv_clip_bytes": (c_size_t, [c_int, c_int, c_int, c_int]),
     "asv_check_dead_seeds_noalloc": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int,
                                              c_void_p]),
+    "asv_stream_begin": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_int, c_int]),
+    "asv_stream_info_get": (c_int, [c_void_p, c_void_p]),
+    "asv_stream_push": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, P(c_int)]),
     # include/asv_host.h
     "asv_synth_clip": (c_int, [P(SynthParams), c_void_p, c_void_p, c_void_p]),
     "asv_preprocess_frame": (c_int, [c_void_p, c_int, c_int, c_void_p]),

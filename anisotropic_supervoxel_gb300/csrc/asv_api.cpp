@@ -6,6 +6,7 @@
 #include "asv.h"
 #include "asv_common.cuh"
 #include "asv_internal.h"
+#include "asv_stream.cuh"
 
 #include <cuda_runtime.h>
 
@@ -155,6 +156,15 @@ struct asv_ctx {
     asv_stats stats{};
     std::vector<cudaEvent_t> ev;
     int launches = 0;
+    // streaming form (asv_stream_*)
+    struct Stream {
+        bool on = false;
+        int W = 0, H = 0, D_all = 0, bs = 30, seeds100 = 0, nb = 0, next = 0, prev_Db = 0;
+        int Kcap = 0, Dcap = 0;
+        std::vector<int> iv;   // block intervals [start, end)
+        StreamDev s{};
+        int placed = 0, kept = 0, last_Kp = 0;
+    } sm;
 };
 
 static asv_status fail(asv_ctx *c, asv_status s, const std::string &m)
@@ -183,6 +193,7 @@ static void free_layout(asv_ctx *ctx)
     ctx->d = AsvDev{};
     ctx->have_rgb = ctx->have_flow = ctx->have_pos0 = ctx->have_M0 = ctx->have_lab = false;
     ctx->seeded = ctx->ran = false;
+    ctx->sm.on = false;
 }
 
 template <typename T>
@@ -360,8 +371,10 @@ static void do_first_init(asv_ctx *ctx)
     ctx->launches += 2;
 }
 
+// the JFA ladder; the last pass of each segment also forms its centroid sums
 static void do_flood(asv_ctx *ctx, int evbase)
 {
+    cudaMemsetAsync(ctx->d.sums, 0, sizeof(unsigned long long) * 8 * (size_t)ctx->d.total_seeds, ctx->st);
     for (int p = 0; p < ctx->maxpass; p++) {
         if (evbase >= 0) rec_begin(ctx, evbase + 2 * p);
         asv_launch_jfa(ctx->d, p, ctx->jfa_blocks, ctx->st);
@@ -370,12 +383,18 @@ static void do_flood(asv_ctx *ctx, int evbase)
     }
 }
 
+// the reseed of centroids_next_seeds (the sums came with the flood)
 static void do_centroids(asv_ctx *ctx, bool reseed)
+{
+    if (reseed) { asv_launch_finalize(ctx->d, ctx->st); ctx->launches++; }
+}
+
+// per-label sums of the labels in the final buffers (caller-supplied labels)
+static void do_sums_from_labels(asv_ctx *ctx)
 {
     cudaMemsetAsync(ctx->d.sums, 0, sizeof(unsigned long long) * 8 * (size_t)ctx->d.total_seeds, ctx->st);
     asv_launch_centroids(ctx->d, ctx->st);
     ctx->launches++;
-    if (reseed) { asv_launch_finalize(ctx->d, ctx->st); ctx->launches++; }
 }
 
 static void do_next_seeds(asv_ctx *ctx)
@@ -824,7 +843,7 @@ asv_status asv_check_dead_seeds_host(asv_ctx *ctx, const int32_t *raw_in, int32_
         if (raw_in[v] < -1 || raw_in[v] >= s.Kp) return fail(ctx, ASV_ERR_BAD_ARG, "label outside [-1, Kp)");
     int32_t *fin = (s.final_buf ? ctx->d.labB : ctx->d.labA) + s.vox_off;
     CK(cudaMemcpyAsync(fin, raw_in, 4 * (size_t)s.nvox, cudaMemcpyHostToDevice, ctx->st));
-    do_centroids(ctx, false);
+    do_sums_from_labels(ctx);
     do_post(ctx);
     CK(cudaGetLastError());
     ctx->ran = true;
@@ -868,6 +887,215 @@ asv_status asv_synchronize(asv_ctx *ctx)
     if (!ctx) return ASV_ERR_BAD_ARG;
     CK(cudaStreamSynchronize(ctx->st));
     CK(cudaGetLastError());
+    return ASV_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Streaming form (streamGPU-AS/Render.cpp:100-569)
+// ---------------------------------------------------------------------------
+
+// block intervals (Render.cpp:199-241)
+static int stream_blocks(int D_all, int bs, std::vector<int> *iv)
+{
+    int one_third = bs / 3, two_third = 2 * bs / 3;
+    int last_end = bs;
+    bool done = false;
+    iv->clear();
+    if (D_all < bs + one_third) {
+        iv->push_back(0); iv->push_back(D_all);
+    } else {
+        iv->push_back(0); iv->push_back(last_end);
+        while (last_end + two_third < D_all) {
+            if (D_all - last_end - two_third < one_third) {
+                iv->push_back(last_end - one_third); iv->push_back(D_all);
+                done = true;
+            } else {
+                iv->push_back(last_end - one_third); iv->push_back(last_end + two_third);
+            }
+            last_end += two_third;
+        }
+        if (!done) { iv->push_back(last_end - one_third); iv->push_back(D_all); }
+    }
+    return (int)iv->size() / 2;
+}
+
+// new seeds requested for block b (Render.cpp:351-356, :394)
+static int stream_seeds_num(const asv_ctx *ctx, int b)
+{
+    const auto &m = ctx->sm;
+    int Db = m.iv[2 * b + 1] - m.iv[2 * b];
+    if (b == 0) return m.nb > 1 ? m.seeds100 * (Db - 10) / 100 : m.seeds100 * Db / 100;
+    return m.seeds100 * (Db - 10) / 100;
+}
+
+asv_status asv_stream_begin(asv_ctx *ctx, int W, int H, int D_all, int K_video, int seeds_num_100,
+                            int block_size)
+{
+    if (!ctx) return ASV_ERR_BAD_ARG;
+    if (block_size <= 0) block_size = 30;
+    if (W < 1 || H < 1 || D_all < 2 || block_size < 6 || (K_video < 1 && seeds_num_100 < 1))
+        return fail(ctx, ASV_ERR_BAD_ARG, "need W,H >= 1, D_all >= 2, block_size >= 6 and seeds");
+    cudaSetDevice(ctx->cfg.device);
+    free_layout(ctx);
+    ctx->cfg.variant = ASV_VARIANT_STREAM;          // compactness 6, no angle filter
+    auto &m = ctx->sm;
+    m = asv_ctx::Stream{};
+    m.W = W; m.H = H; m.D_all = D_all; m.bs = block_size;
+    m.seeds100 = seeds_num_100 > 0 ? seeds_num_100 : K_video * 100 / D_all;   // Render.cpp:157
+    m.nb = stream_blocks(D_all, block_size, &m.iv);
+    int kn_max = 0, wmax = 1, hmax = 1, dmax = 1;
+    for (int b = 0; b < m.nb; b++) {
+        int Db = m.iv[2 * b + 1] - m.iv[2 * b];
+        if (Db < 2) return fail(ctx, ASV_ERR_BAD_ARG, "a block shorter than 2 frames");
+        SegHost h;
+        asv_status s = asv_prepare_segment(ctx, W, H, Db, stream_seeds_num(ctx, b), &h);
+        if (s != ASV_OK) return s;
+        kn_max = std::max(kn_max, h.Kp);
+        wmax = std::max(wmax, h.g.wNum); hmax = std::max(hmax, h.g.hNum); dmax = std::max(dmax, h.g.dNum);
+        m.Dcap = std::max(m.Dcap, Db);
+    }
+    m.Kcap = std::min(3 * kn_max + 256, 32767);
+    SegHost cap;
+    cap.W = W; cap.H = H; cap.D = m.Dcap; cap.Kp = m.Kcap; cap.npass = 1;
+    cap.g.wNum = wmax; cap.g.hNum = hmax; cap.g.dNum = dmax; cap.g.Kp = m.Kcap;
+    cap.cells.assign((size_t)W + H + m.Dcap + 2 * wmax, -1);
+    cap.grid.assign((size_t)4 * m.Kcap, 0.f);
+    ctx->seg.assign(1, cap);
+    asv_status s = asv_build_layout(ctx);
+    if (s != ASV_OK) return s;
+    StreamDev &sd = m.s;
+    AL(sd.kept_pos, m.Kcap); AL(sd.kept_next, m.Kcap);
+    AL(sd.gmap_prev, m.Kcap); AL(sd.gmap_cur, m.Kcap);
+    AL(sd.ctr, STREAM_CTR_WORDS);
+    AL(sd.lab_out, (size_t)W * H * m.Dcap);
+    CK(cudaMemsetAsync(sd.ctr, 0, sizeof(int) * STREAM_CTR_WORDS, ctx->st));
+    m.on = true;
+    return ASV_OK;
+}
+
+asv_status asv_stream_info_get(asv_ctx *ctx, asv_stream_info *info)
+{
+    if (!ctx || !info) return ASV_ERR_BAD_ARG;
+    const auto &m = ctx->sm;
+    if (!m.on) return fail(ctx, ASV_ERR_STATE, "no stream: call asv_stream_begin first");
+    std::memset(info, 0, sizeof(*info));
+    info->blocks = m.nb;
+    info->next_block = m.next;
+    info->seeds_placed = m.placed;
+    info->block_Kp = m.last_Kp;
+    if (m.next < m.nb) {
+        info->block_start = m.iv[2 * m.next];
+        info->block_end = m.iv[2 * m.next + 1];
+        info->frames_needed = info->block_end - info->block_start - (m.next == 0 ? 0 : 10);
+    }
+    return ASV_OK;
+}
+
+asv_status asv_stream_push(asv_ctx *ctx, const uint8_t *rgb, const float *fwd, const float *bwd,
+                           int32_t *labels_out, int *done_frames)
+{
+    if (!ctx) return ASV_ERR_BAD_ARG;
+    auto &m = ctx->sm;
+    if (!m.on) return fail(ctx, ASV_ERR_STATE, "no stream: call asv_stream_begin first");
+    if (m.next >= m.nb) return fail(ctx, ASV_ERR_STATE, "the stream is finished");
+    if (!rgb || !fwd || !bwd || !labels_out) return fail(ctx, ASV_ERR_BAD_ARG, "NULL buffer");
+    cudaSetDevice(ctx->cfg.device);
+    const int b = m.next;
+    const int Db = m.iv[2 * b + 1] - m.iv[2 * b];
+    const int one_third = m.bs / 3, two_third = m.bs - one_third;   // Render.cpp:515-516
+    const int z0 = b == 0 ? 0 : 10;                                 // overlap frames kept on the device
+    const size_t WH = (size_t)m.W * m.H;
+    AsvDev &d = ctx->d;
+    cudaStream_t st = ctx->st;
+    if (b > 0) {                                                    // Render.cpp:405-412, :545-556
+        size_t src = (size_t)(m.prev_Db - 10) * WH, n = 10 * WH;
+        CK(cudaMemcpyAsync(d.rgb, d.rgb + 3 * src, 3 * n, cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemcpyAsync(d.lab, d.lab + src, 4 * n, cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemcpyAsync(d.fwd, d.fwd + src, 8 * n, cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemcpyAsync(d.bwd, d.bwd + src, 8 * n, cudaMemcpyDeviceToDevice, st));
+    }
+    const size_t nnew = (size_t)(Db - z0) * WH;
+    CK(cudaMemcpyAsync(d.rgb + 3 * z0 * WH, rgb, 3 * nnew, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d.fwd + z0 * WH, fwd, 8 * nnew, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d.bwd + z0 * WH, bwd, 8 * nnew, cudaMemcpyHostToDevice, st));
+
+    // new seeds of the block: grid + density placement (Render.cpp:376-379, :429-432)
+    SegHost h;
+    asv_status s = asv_prepare_segment(ctx, m.W, m.H, Db, stream_seeds_num(ctx, b), &h);
+    if (s != ASV_OK) return s;
+    const int Kn = h.Kp;
+    SegDesc &sd = ctx->sd[0];
+    const int seed_cap = d.total_seeds;
+    sd.W = m.W; sd.H = m.H; sd.D = Db; sd.Kp = Kn;
+    sd.vox_off = 0; sd.nvox = (long long)WH * Db; sd.seed_off = 0;
+    sd.npass = h.npass;
+    for (int p = 0; p < h.npass; p++) { sd.steps[p] = h.steps[p]; sd.ratio[p] = h.rmul[p] * h.ratio; }
+    sd.tiles_x = (m.W + ASV_TILE_X - 1) / ASV_TILE_X;
+    sd.tiles_y = (m.H + ASV_TILE_Y - 1) / ASV_TILE_Y;
+    sd.angle_filter = 0;
+    sd.wNum = h.g.wNum; sd.hNum = h.g.hNum; sd.dNum = h.g.dNum;
+    sd.cell_off = 0;
+    sd.final_buf = h.npass & 1;
+    sd.lab_from = (long long)z0 * WH;
+    const int tiles = sd.tiles_x * sd.tiles_y * ((Db + ASV_TILE_Z - 1) / ASV_TILE_Z);
+    const int chunks = (int)((sd.nvox + ASV_CHUNK - 1) / ASV_CHUNK);
+    d.total_tiles = tiles;
+    d.total_chunks = chunks;
+    int tp[2] = { 0, tiles }, cp[2] = { 0, chunks }, sp[2] = { 0, seed_cap };
+    CK(cudaMemcpyAsync((void *)d.tile_prefix, tp, sizeof(tp), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync((void *)d.chunk_prefix, cp, sizeof(cp), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync((void *)d.seed_prefix, sp, sizeof(sp), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync((void *)d.segs, &sd, sizeof(SegDesc), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d.cells, h.cells.data(), sizeof(int) * h.cells.size(), cudaMemcpyHostToDevice, st));
+    std::vector<float4> grid((size_t)Kn);
+    for (int k = 0; k < Kn; k++)
+        grid[k] = make_float4(h.grid[4 * k], h.grid[4 * k + 1], h.grid[4 * k + 2], h.grid[4 * k + 3]);
+    CK(cudaMemcpyAsync(d.grid, grid.data(), sizeof(float4) * Kn, cudaMemcpyHostToDevice, st));
+    ctx->maxpass = h.npass;
+    ctx->jfa_blocks = asv_jfa_grid_blocks(tiles);
+
+    asv_launch_rgb2lab(d, st);                                   // new frames only (lab_from)
+    CK(cudaMemsetAsync(d.dacc, 0, sizeof(unsigned long long) * d.total_seeds, st));
+    asv_launch_density(d, st);
+    asv_launch_density_adjust(d, st);
+    asv_launch_stream_compose(d, m.s, Kn, m.Kcap, st);          // kept seeds first, then the new ones
+    CK(cudaGetLastError());
+    int ctr[STREAM_CTR_WORDS], post[ASV_POST_WORDS];
+    CK(cudaMemcpyAsync(ctr, m.s.ctr, sizeof(ctr), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(post, d.post, sizeof(post), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (post[POST_VALID] != Kn) return fail(ctx, ASV_ERR_CUDA, "density placement produced fewer seeds than the grid");
+    if (ctr[STREAM_KP] < 0) return fail(ctx, ASV_ERR_OVER_BUDGET, "kept + new seeds exceed the stream's seed capacity");
+    const int Kp = ctr[STREAM_KP];
+    sd.Kp = Kp;
+    CK(cudaMemcpyAsync((void *)d.segs, &sd, sizeof(SegDesc), cudaMemcpyHostToDevice, st));
+    h.Kp = Kp;
+    ctx->seg[0] = h;
+    ctx->seg[0].vox_off = 0;
+    ctx->seg[0].seed_off = 0;
+
+    // seed_matrix, RGB2LAB (above), Lloyd loop, check_dead_seeds (Render.cpp:470-512)
+    ctx->launches = 0;
+    asv_launch_metric(d, 0, st);
+    enqueue_lloyd(ctx, false);
+    const int keep = b < m.nb - 1;
+    asv_launch_stream_next(d, m.s, (float)(m.bs - one_third), (float)two_third, keep, st);
+    const int done = keep ? Db - one_third : Db;
+    asv_launch_stream_map(d, m.s, (long long)WH * done, st);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(labels_out, m.s.lab_out, sizeof(int32_t) * WH * done, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(ctr, m.s.ctr, sizeof(ctr), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    std::swap(m.s.kept_pos, m.s.kept_next);
+    std::swap(m.s.gmap_prev, m.s.gmap_cur);
+    m.placed = ctr[STREAM_PLACED];
+    m.kept = ctr[STREAM_KEPT];
+    m.last_Kp = Kp;
+    m.prev_Db = Db;
+    m.next++;
+    ctx->have_rgb = ctx->have_flow = ctx->have_pos0 = ctx->have_M0 = ctx->have_lab = true;
+    ctx->seeded = ctx->ran = true;
+    if (done_frames) *done_frames = done;
     return ASV_OK;
 }
 

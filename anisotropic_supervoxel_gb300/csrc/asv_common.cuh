@@ -32,6 +32,8 @@ struct SegDesc {
     int wNum, hNum, dNum;    // seed grid (density placement)
     int cell_off;            // x cells at cell_off, y at +W, z at +W+H
     int final_buf;           // 0: last pass wrote buffer A, 1: buffer B
+    long long lab_from;      // first voxel whose LAB must be computed (streaming windows keep
+                             // the LAB of their overlap frames)
 };
 
 // post-processing record per segment (ints), written by k_post_stats

@@ -87,6 +87,7 @@ __global__ void __launch_bounds__(256) k_rgb2lab(AsvDev d)
     const SegDesc &S = d.segs[si];
     long long base = (long long)(blockIdx.x - d.chunk_prefix[si]) * ASV_CHUNK;
     long long n = S.nvox;
+    if (base + ASV_CHUNK <= S.lab_from) return;
     for (int i = 0; i < ASV_CHUNK / 256; i++) {
         long long v = base + i * 256 + threadIdx.x;
         if (v >= n) break;
@@ -288,7 +289,7 @@ __global__ void k_draw(AsvDev d)
 // ---------------------------------------------------------------------------
 #define ASV_JFA_THREADS 256
 
-__device__ __forceinline__ void asv_jfa_voxel(const int32_t *__restrict__ in, int32_t *__restrict__ out,
+__device__ __forceinline__ int asv_jfa_voxel(const int32_t *__restrict__ in, int32_t *__restrict__ out,
                                               const uchar4 *__restrict__ lab,
                                               const float4 *__restrict__ tab, int W, int H, int D,
                                               int Kp, int x, int y, int z, int step, float ratio,
@@ -337,6 +338,30 @@ __device__ __forceinline__ void asv_jfa_voxel(const int32_t *__restrict__ in, in
         if (dist < mind) { mind = dist; best = l; }                    // flood.gs:95-99
     }
     out[z * sl + y * W + x] = best;
+    return best;
+}
+
+// Centroid sums of one voxel, fused into the last JFA pass of a Lloyd
+// iteration (centroids.vs:19-54): the lanes that run together are grouped by
+// label, reduced in the warp, and one u64 atomic per group and component is
+// issued.  Grouping over whichever lanes are active keeps the sums exact.
+__device__ __forceinline__ void asv_accumulate(unsigned long long *__restrict__ sums,
+                                               const uchar4 *__restrict__ lab, int W, int H, int Kp,
+                                               int x, int y, int z, int best)
+{
+    const uchar4 c = __ldg(lab + (z * H + y) * W + x);
+    const int key = best < 0 ? Kp : best;
+    const unsigned act = __activemask();
+    const unsigned grp = __match_any_sync(act, key);
+    const unsigned q[7] = { 2u * x + 1u, 2u * y + 1u, 2u * z + 1u, 1u, c.x, c.y, c.z };
+    unsigned s[7];
+#pragma unroll
+    for (int k = 0; k < 7; k++) s[k] = __reduce_add_sync(grp, q[k]);
+    if ((int)(threadIdx.x & 31) == __ffs(grp) - 1) {
+        unsigned long long *dst = sums + 8ull * key;
+#pragma unroll
+        for (int k = 0; k < 7; k++) atomicAdd(dst + k, (unsigned long long)s[k]);
+    }
 }
 
 // tile = ASV_TILE_X x ASV_TILE_Y voxels x ASV_TILE_Z slices; the tile
@@ -359,9 +384,15 @@ __global__ void __launch_bounds__(ASV_JFA_THREADS) k_jfa(AsvDev d, int pass,
         const int z1 = min(z0 + ASV_TILE_Z, S.D);
         const int step = S.steps[pass];
         const float ratio = S.ratio[pass];
-        for (int z = z0; z < z1; z++)
-            asv_jfa_voxel(in + S.vox_off, out + S.vox_off, d.lab + S.vox_off, d.jtab + 3 * S.seed_off,
-                          S.W, S.H, S.D, S.Kp, x, y, z, step, ratio, list + threadIdx.x);
+        const bool last = pass == S.npass - 1;     // the iteration's labels: sum them
+        for (int z = z0; z < z1; z++) {
+            const int best = asv_jfa_voxel(in + S.vox_off, out + S.vox_off, d.lab + S.vox_off,
+                                           d.jtab + 3 * S.seed_off, S.W, S.H, S.D, S.Kp, x, y, z, step,
+                                           ratio, list + threadIdx.x);
+            if (last)
+                asv_accumulate(d.sums + 8ull * S.seed_off, d.lab + S.vox_off, S.W, S.H, S.Kp, x, y, z,
+                               best);
+        }
     }
 }
 

@@ -188,6 +188,38 @@ class Image:
         return self.labels()
 
 
+class Stream(Image):
+    """The reference's streaming form (streamGPU-AS/Render.cpp:100-569) on the
+    device: `push` takes a block's new frames and returns the video-wide labels
+    of the frames that block finishes."""
+
+    def __init__(self, W, H, D_all, K_video=0, seeds_num_100=0, block_size=30, **kw):
+        super().__init__(**kw)
+        self._ck(self.lib.asv_stream_begin(self.h, W, H, D_all, K_video, seeds_num_100, block_size))
+        self.W, self.H = W, H
+
+    def info(self):
+        i = _lib.StreamInfo()
+        self._ck(self.lib.asv_stream_info_get(self.h, ctypes.byref(i)))
+        return i
+
+    def push(self, rgb, fwd, bwd):
+        """rgb [n,H,W,3] uint8, fwd/bwd [n,H,W,2] float32: the next block's new frames.
+        Returns (first frame index, labels [done,H,W] int32)."""
+        inf = self.info()
+        rgb = np.ascontiguousarray(rgb, np.uint8)
+        fwd = np.ascontiguousarray(fwd, np.float32)
+        bwd = np.ascontiguousarray(bwd, np.float32)
+        if rgb.shape[0] != inf.frames_needed:
+            raise ValueError(f"block {inf.next_block} needs {inf.frames_needed} new frames")
+        D = inf.block_end - inf.block_start
+        out = np.empty((D, self.H, self.W), np.int32)
+        done = ctypes.c_int()
+        self._ck(self.lib.asv_stream_push(self.h, _ptr(rgb), _ptr(fwd), _ptr(bwd), _ptr(out),
+                                          ctypes.byref(done)))
+        return inf.block_start, out[:done.value]
+
+
 def write_labels_txt(path, labels):
     D, H, W = labels.shape
     lab = np.ascontiguousarray(labels, np.int32)

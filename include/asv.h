@@ -173,6 +173,44 @@ asv_status asv_synchronize(asv_ctx *ctx);
 /* bytes of device memory a clip of this size needs (admission control) */
 size_t asv_clip_bytes(int W, int H, int D, int K);
 
+/* ---- streaming form ---------------------------------------------------- */
+
+/* The reference's streamGPU-AS form (streamGPU-AS/Render.cpp:100-569): a
+ * long video segmented in blocks of `block_size` frames (30) that overlap by
+ * block_size/3 (10); each block places its new seeds (grid + gradient
+ * density) after the seeds carried from the previous block (final centroids
+ * with z > block_size - block_size/3, shifted back), runs the Lloyd loop
+ * with compactness 6 and no flow-angle filter, and maps its labels to
+ * video-wide ids (block2all).  Here the overlap frames (RGB, LAB, flow), the
+ * carried seeds and the id maps stay on the device between blocks; each push
+ * uploads only the frames the block does not have yet. */
+typedef struct asv_stream_info {
+    int blocks;          /* blocks of the video */
+    int next_block;      /* the block the next asv_stream_push processes */
+    int block_start;     /* its frame range [block_start, block_end) */
+    int block_end;
+    int frames_needed;   /* new frames the next push must carry */
+    int seeds_placed;    /* seeds_num_placed after the last processed block */
+    int block_Kp;        /* seeds (carried + new) of the last processed block */
+} asv_stream_info;
+
+/* Replaces the block scheduling of Render::run (streamGPU-AS/Render.cpp:
+ * 149-241).  seeds_num_100 (new seeds per 100 frames) is K_video*100/D_all
+ * when given as 0 (:156-158); block_size 0 means 30.  Sets the context's
+ * variant to ASV_VARIANT_STREAM. */
+asv_status asv_stream_begin(asv_ctx *ctx, int W, int H, int D_all, int K_video, int seeds_num_100,
+                            int block_size);
+asv_status asv_stream_info_get(asv_ctx *ctx, asv_stream_info *info);
+
+/* prepare_data_seeds + block_segment + post_and_next for the next block
+ * (streamGPU-AS/Render.cpp:348-569).  rgb / fwd / bwd: the block's new
+ * frames (frames_needed of them, same layouts as asv_init_gpu and
+ * asv_upload_flow; fwd of a frame is its flow to the next frame of the
+ * video).  labels_out: the video-wide labels of the block's finished frames
+ * [block_start, block_start + *done_frames), W*H*done_frames int32. */
+asv_status asv_stream_push(asv_ctx *ctx, const uint8_t *rgb, const float *fwd, const float *bwd,
+                           int32_t *labels_out, int *done_frames);
+
 /* ---- post-processing without device allocation ------------------------- */
 
 /* No counterpart in the reference.  The same dead-seed relabel and -1 fill

@@ -1,0 +1,36 @@
+"""Streaming form on the GPU (asv_stream_*) against the CPU restatement of
+streamGPU-AS's block scheduler: video-wide labels must be identical."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _run_stream(asv, rgb, fwd, bwd, seeds100, iters, bs=30):
+    D_all, H, W, _ = rgb.shape
+    st = asv.Stream(W, H, D_all, seeds_num_100=seeds100, block_size=bs, lloyd_iters=iters)
+    out = np.full((D_all, H, W), -7, np.int32)
+    info = st.info()
+    nb = info.blocks
+    for b in range(nb):
+        inf = st.info()
+        z0 = inf.block_end - inf.block_start - inf.frames_needed
+        a, e = inf.block_start + z0, inf.block_end
+        f0, lab = st.push(rgb[a:e], fwd[a:e], bwd[a:e])
+        out[f0:f0 + lab.shape[0]] = lab
+    info = st.info()
+    st.close()
+    return out, nb, info.seeds_placed
+
+
+@pytest.mark.parametrize("W,H,D,seeds100,iters", [(48, 40, 75, 200, 4), (64, 48, 95, 120, 6),
+                                                  (40, 32, 36, 300, 3)])
+def test_stream_matches_oracle(asv, orc, W, H, D, seeds100, iters):
+    rgb, fwd, bwd = asv.synth_clip(W, H, D, n_ellipses=6, noise_sigma=5.0, vmax=2.0, jitter=0.3,
+                                   drift_amp=2.0, drift_period=40.0, seed=W + D)
+    got, nb, placed = _run_stream(asv, rgb, fwd, bwd, seeds100, iters)
+    want, info = orc.run_stream(rgb, fwd, bwd, seeds_num_100=seeds100, iters=iters, nthreads=8)
+    assert nb == info["blocks"]
+    assert placed == info["placed"]
+    assert (got != -7).all()
+    assert np.array_equal(got, want)
