@@ -20,6 +20,8 @@ ASV_ERR_TIMEOUT = 4
 ASV_ERR_CUDA = 5
 ASV_ERR_STATE = 6
 ASV_ERR_NO_DEVICE = 7
+REQ_CLIP = 0
+REQ_WINDOW = 1
 VARIANT_PLAIN = 0
 VARIANT_STREAM = 1
 
@@ -28,7 +30,7 @@ class Config(ctypes.Structure):
     _fields_ = [("variant", c_int), ("lloyd_iters", c_int), ("full_ladder", c_int),
                 ("middlebury", c_int), ("density_adjust", c_int), ("device", c_int),
                 ("stream", c_void_p), ("hbm_budget", c_size_t), ("use_graph", c_int),
-                ("instrument", c_int)]
+                ("instrument", c_int), ("jfa_zrun", c_int)]
 
 
 class Info(ctypes.Structure):
@@ -46,6 +48,19 @@ class Stats(ctypes.Structure):
 class StreamInfo(ctypes.Structure):
     _fields_ = [(n, c_int) for n in ("blocks", "next_block", "block_start", "block_end",
                                      "frames_needed", "seeds_placed", "block_Kp")]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("kind", c_int), ("session", c_int), ("W", c_int), ("H", c_int), ("D", c_int),
+                ("K", c_int), ("rgb", c_void_p), ("fwd", c_void_p), ("bwd", c_void_p),
+                ("labels_out", c_void_p)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_longlong), ("completed", ctypes.c_longlong),
+                ("failed", ctypes.c_longlong), ("queued", ctypes.c_longlong),
+                ("running", ctypes.c_longlong), ("bytes_in_use", c_size_t), ("budget", c_size_t),
+                ("slots", c_int), ("sessions", c_int)]
 
 
 class SynthParams(ctypes.Structure):
@@ -74,6 +89,7 @@ SIGNATURES = {
     "asv_ld_next_seeds_matrix": (c_int, [c_void_p, c_int]),
     "asv_check_dead_seeds": (c_int, [c_void_p, c_void_p]),
     "asv_run_lloyd": (c_int, [c_void_p]),
+    "asv_autotune": (c_int, [c_void_p, P(c_int)]),
     "asv_segment_clip": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_int,
                                  c_int, c_void_p]),
     "asv_get_info": (c_int, [c_void_p, P(Info)]),
@@ -91,6 +107,19 @@ SIGNATURES = {
     "asv_clip_bytes": (c_size_t, [c_int, c_int, c_int, c_int]),
     "asv_check_dead_seeds_noalloc": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int,
                                              c_void_p]),
+    "asv_batch_init": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "asv_batch_upload": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
+    "asv_batch_get_labels": (c_int, [c_void_p, c_int, c_void_p]),
+    "asv_batch_get_info": (c_int, [c_void_p, c_int, P(Info)]),
+    "asv_batch_bytes": (c_size_t, [c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "asv_server_create": (c_int, [P(Config), c_int, c_size_t, P(c_void_p)]),
+    "asv_server_destroy": (c_int, [c_void_p]),
+    "asv_server_open_session": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_int, c_int, P(c_int)]),
+    "asv_server_submit": (c_int, [c_void_p, c_void_p, P(ctypes.c_longlong)]),
+    "asv_server_wait": (c_int, [c_void_p, ctypes.c_longlong, P(ctypes.c_double), P(ctypes.c_double),
+                                P(c_int)]),
+    "asv_server_poll": (c_int, [c_void_p, ctypes.c_longlong, P(c_int)]),
+    "asv_server_get_stats": (c_int, [c_void_p, c_void_p]),
     "asv_stream_begin": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_int, c_int]),
     "asv_stream_info_get": (c_int, [c_void_p, c_void_p]),
     "asv_stream_push": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, P(c_int)]),

@@ -156,6 +156,8 @@ struct asv_ctx {
     asv_stats stats{};
     std::vector<cudaEvent_t> ev;
     int launches = 0;
+    // batched form: which clips have their inputs on the device
+    std::vector<uint8_t> up_rgb, up_flow;
     // streaming form (asv_stream_*)
     struct Stream {
         bool on = false;
@@ -166,6 +168,8 @@ struct asv_ctx {
         int placed = 0, kept = 0, last_Kp = 0;
     } sm;
 };
+
+size_t asv::ctx_bytes(const asv_ctx *c) { return c ? c->bytes : 0; }
 
 static asv_status fail(asv_ctx *c, asv_status s, const std::string &m)
 {
@@ -250,9 +254,32 @@ size_t asv_layout_bytes(const std::vector<SegHost> &seg)
         seeds += (size_t)((s.Kp + 64 + 31) / 32) * 32;
         cells += s.W + s.H + s.D + 2 * s.g.wNum;
     }
+    // rgb 3 + lab 4 + fwd/bwd 16 + two label buffers 8
     size_t per_vox = 3 + 4 + 8 + 8 + 4 + 4;
-    size_t per_seed = 16 * 4 + 4 * 8 * 2 + 3 * 16 + 8 * 8 + 8 * 4 + 4 + ASV_RING * (32 + 4) + 16 + 8 + 4;
-    return vox * per_vox + seeds * per_seed + cells * 4 + chunks * 4 + 4096 + seg.size() * 1024;
+    // float4 pos0/pos/slab/grid, 8-float M0/M/Mself/Mmemo, jtab 3 float4, 8 u64
+    // sums, int neg/mkey/rank, u64 dacc, the metric ring
+    size_t per_seed = 4 * 16 + 4 * 32 + 3 * 16 + 8 * 8 + 3 * 4 + 8 + ASV_RING * (32 + 4);
+    // each of the ~30 allocations rounds up to 256 bytes
+    size_t fixed = 32 * 256 + 256 * 4 + 16;
+    size_t per_seg = sizeof(SegDesc) + 3 * 4 + ASV_POST_WORDS * 4;
+    return vox * per_vox + seeds * per_seed + cells * 4 + chunks * 4 + fixed + seg.size() * per_seg;
+}
+
+// JFA tile depth for a set of segments: the configured one, else the
+// deepest of 32/16/8 that still gives every resident block two tiles (deeper
+// runs share more slice lists; shallower ones fill the GPU), else 4.
+static int pick_zrun(const asv_ctx *ctx, const std::vector<SegHost> &seg)
+{
+    if (ctx->cfg.jfa_zrun > 0) return std::min(ctx->cfg.jfa_zrun, 256);
+    const long long want = 2LL * asv_jfa_resident_blocks();
+    for (int z : { 32, 16, 8 }) {
+        long long tiles = 0;
+        for (const SegHost &h : seg)
+            tiles += (long long)((h.W + ASV_TILE_X - 1) / ASV_TILE_X) * ((h.H + ASV_TILE_Y - 1) / ASV_TILE_Y)
+                     * ((h.D + z - 1) / z);
+        if (tiles >= want) return z;
+    }
+    return 4;
 }
 
 // Allocates the packed device arrays for the segments in ctx->seg.
@@ -265,6 +292,7 @@ asv_status asv_build_layout(asv_ctx *ctx)
     int tiles = 0, chunks = 0, seeds = 0, cells = 0;
     ctx->sd.assign(nseg, SegDesc{});
     ctx->maxpass = 0;
+    const int zrun = pick_zrun(ctx, ctx->seg);
     for (int i = 0; i < nseg; i++) {
         SegHost &h = ctx->seg[i];
         SegDesc &s = ctx->sd[i];
@@ -276,6 +304,7 @@ asv_status asv_build_layout(asv_ctx *ctx)
         for (int p = 0; p < h.npass; p++) { s.steps[p] = h.steps[p]; s.ratio[p] = h.rmul[p] * h.ratio; }
         s.tiles_x = (h.W + ASV_TILE_X - 1) / ASV_TILE_X;
         s.tiles_y = (h.H + ASV_TILE_Y - 1) / ASV_TILE_Y;
+        s.zrun = zrun;
         s.angle_filter = ctx->cfg.variant == ASV_VARIANT_PLAIN ? 1 : 0;
         s.wNum = h.g.wNum; s.hNum = h.g.hNum; s.dNum = h.g.dNum;
         s.cell_off = cells;
@@ -285,7 +314,7 @@ asv_status asv_build_layout(asv_ctx *ctx)
         int nchunk = (int)((n + ASV_CHUNK - 1) / ASV_CHUNK);
         vox += (long long)nchunk * ASV_CHUNK;
         chunks += nchunk;
-        tiles += s.tiles_x * s.tiles_y * ((h.D + ASV_TILE_Z - 1) / ASV_TILE_Z);
+        tiles += s.tiles_x * s.tiles_y * ((h.D + zrun - 1) / zrun);
         seeds += ((h.Kp + 64 + 31) / 32) * 32;
         cells += h.W + h.H + h.D + 2 * h.g.wNum;
         ctx->maxpass = std::max(ctx->maxpass, h.npass);
@@ -718,6 +747,64 @@ asv_status asv_run_lloyd(asv_ctx *ctx)
     return ASV_OK;
 }
 
+// re-tiles every segment's JFA passes to depth z (tile prefix, grid size);
+// the captured graph holds the old launch shapes and is dropped
+static asv_status set_zrun(asv_ctx *ctx, int z)
+{
+    const int nseg = (int)ctx->sd.size();
+    std::vector<int> tp(nseg + 1);
+    int tiles = 0;
+    for (int i = 0; i < nseg; i++) {
+        SegDesc &sd = ctx->sd[i];
+        sd.zrun = z;
+        tp[i] = tiles;
+        tiles += sd.tiles_x * sd.tiles_y * ((sd.D + z - 1) / z);
+    }
+    tp[nseg] = tiles;
+    CK(cudaMemcpyAsync((void *)ctx->d.segs, ctx->sd.data(), sizeof(SegDesc) * nseg, cudaMemcpyHostToDevice,
+                       ctx->st));
+    CK(cudaMemcpyAsync((void *)ctx->d.tile_prefix, tp.data(), sizeof(int) * (nseg + 1), cudaMemcpyHostToDevice,
+                       ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->d.total_tiles = tiles;
+    ctx->jfa_blocks = asv_jfa_grid_blocks(std::max(tiles, 1));
+    if (ctx->gexec) { cudaGraphExecDestroy(ctx->gexec); ctx->gexec = nullptr; }
+    return ASV_OK;
+}
+
+asv_status asv_autotune(asv_ctx *ctx, int *zrun_out)
+{
+    if (!ctx) return ASV_ERR_BAD_ARG;
+    if (ctx->sm.on) return fail(ctx, ASV_ERR_STATE, "autotune applies to clip and batch contexts");
+    asv_status s = check_ready(ctx);
+    if (s != ASV_OK) return s;
+    cudaSetDevice(ctx->cfg.device);
+    s = ensure_events(ctx, 2);
+    if (s != ASV_OK) return s;
+    int best = 0;
+    float best_ms = 0.f;
+    for (int z : { 4, 8, 16, 32 }) {
+        if ((s = set_zrun(ctx, z)) != ASV_OK) return s;
+        enqueue_lloyd(ctx, false);                        // warm-up at this depth
+        CK(cudaEventRecord(ctx->ev[0], ctx->st));
+        enqueue_lloyd(ctx, false);
+        CK(cudaEventRecord(ctx->ev[1], ctx->st));
+        CK(cudaGetLastError());
+        CK(cudaEventSynchronize(ctx->ev[1]));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]));
+        if (!best || ms < best_ms) { best = z; best_ms = ms; }
+    }
+    if ((s = set_zrun(ctx, best)) != ASV_OK) return s;
+    ctx->cfg.jfa_zrun = best;                             // later layouts keep it
+    enqueue_lloyd(ctx, false);                            // labels of the final depth (identical)
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->seeded = ctx->ran = true;
+    if (zrun_out) *zrun_out = best;
+    return ASV_OK;
+}
+
 asv_status asv_segment_clip(asv_ctx *ctx, const uint8_t *rgb, const float *fwd, const float *bwd,
                             int W, int H, int D, int K, int32_t *labels_out)
 {
@@ -891,6 +978,93 @@ asv_status asv_synchronize(asv_ctx *ctx)
 }
 
 // ---------------------------------------------------------------------------
+// Batched form: many clips, one launch per stage
+// ---------------------------------------------------------------------------
+static asv_status batch_segments(asv_ctx *ctx, int n, const int *W, const int *H, const int *D,
+                                 const int *K, std::vector<SegHost> *v)
+{
+    if (n < 1 || n > 4096 || !W || !H || !D || !K) return fail(ctx, ASV_ERR_BAD_ARG, "bad batch description");
+    v->clear();
+    for (int i = 0; i < n; i++) {
+        SegHost h;
+        asv_status s = asv_prepare_segment(ctx, W[i], H[i], D[i], K[i], &h);
+        if (s != ASV_OK) return s;
+        v->push_back(h);
+    }
+    return ASV_OK;
+}
+
+size_t asv_batch_bytes(int n, const int *W, const int *H, const int *D, const int *K)
+{
+    asv_ctx tmp;
+    asv_config_default(&tmp.cfg);
+    std::vector<SegHost> v;
+    if (batch_segments(&tmp, n, W, H, D, K, &v) != ASV_OK) return 0;
+    return asv_layout_bytes(v);
+}
+
+asv_status asv_batch_init(asv_ctx *ctx, int n, const int *W, const int *H, const int *D, const int *K)
+{
+    if (!ctx) return ASV_ERR_BAD_ARG;
+    cudaSetDevice(ctx->cfg.device);
+    std::vector<SegHost> v;
+    asv_status s = batch_segments(ctx, n, W, H, D, K, &v);
+    if (s != ASV_OK) return s;
+    if (ctx->cfg.hbm_budget && asv_layout_bytes(v) > ctx->cfg.hbm_budget)
+        return fail(ctx, ASV_ERR_OVER_BUDGET, "batch exceeds the configured HBM budget");
+    ctx->seg = v;
+    s = asv_build_layout(ctx);
+    if (s != ASV_OK) return s;
+    ctx->up_rgb.assign(n, 0);
+    ctx->up_flow.assign(n, 0);
+    return ASV_OK;
+}
+
+asv_status asv_batch_upload(asv_ctx *ctx, int clip, const uint8_t *rgb, const float *fwd, const float *bwd)
+{
+    if (!ctx) return ASV_ERR_BAD_ARG;
+    if (clip < 0 || clip >= (int)ctx->seg.size() || ctx->up_rgb.size() != ctx->seg.size())
+        return fail(ctx, ASV_ERR_BAD_ARG, "no such clip in the batch");
+    if (!rgb || !fwd || !bwd) return fail(ctx, ASV_ERR_BAD_ARG, "NULL buffer");
+    const SegDesc &s = ctx->sd[clip];
+    size_t n = (size_t)s.nvox;
+    CK(cudaMemcpyAsync(ctx->d.rgb + 3 * s.vox_off, rgb, 3 * n, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ctx->d.fwd + s.vox_off, fwd, 8 * n, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ctx->d.bwd + s.vox_off, bwd, 8 * n, cudaMemcpyHostToDevice, ctx->st));
+    ctx->up_rgb[clip] = ctx->up_flow[clip] = 1;
+    bool all = true;
+    for (auto u : ctx->up_rgb) all = all && u;
+    ctx->have_rgb = ctx->have_flow = all;
+    return ASV_OK;
+}
+
+asv_status asv_batch_get_labels(asv_ctx *ctx, int clip, int32_t *out)
+{
+    if (!ctx || !out) return ASV_ERR_BAD_ARG;
+    if (clip < 0 || clip >= (int)ctx->seg.size()) return fail(ctx, ASV_ERR_BAD_ARG, "no such clip");
+    if (!ctx->ran) return fail(ctx, ASV_ERR_STATE, "no labels: run the Lloyd loop first");
+    const SegDesc &s = ctx->sd[clip];
+    const int32_t *src = (s.final_buf ? ctx->d.labA : ctx->d.labB) + s.vox_off;
+    CK(cudaMemcpyAsync(out, src, sizeof(int32_t) * (size_t)s.nvox, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return ASV_OK;
+}
+
+asv_status asv_batch_get_info(asv_ctx *ctx, int clip, asv_info *info)
+{
+    if (!ctx || !info) return ASV_ERR_BAD_ARG;
+    if (clip < 0 || clip >= (int)ctx->seg.size()) return fail(ctx, ASV_ERR_BAD_ARG, "no such clip");
+    if (ctx->ran) { asv_status s = read_post(ctx); if (s != ASV_OK) return s; }
+    std::memset(info, 0, sizeof(*info));
+    const SegHost &h = ctx->seg[clip];
+    info->W = h.W; info->H = h.H; info->D = h.D; info->K = h.K; info->Kp = h.Kp; info->s = h.g.s;
+    info->ratio = h.ratio; info->passes = h.npass;
+    for (int p = 0; p < h.npass && p < 32; p++) info->steps[p] = h.steps[p];
+    info->dead = h.dead; info->neg_count = h.neg; info->final_label_num = h.valid;
+    return ASV_OK;
+}
+
+// ---------------------------------------------------------------------------
 // Streaming form (streamGPU-AS/Render.cpp:100-569)
 // ---------------------------------------------------------------------------
 
@@ -1032,12 +1206,13 @@ asv_status asv_stream_push(asv_ctx *ctx, const uint8_t *rgb, const float *fwd, c
     for (int p = 0; p < h.npass; p++) { sd.steps[p] = h.steps[p]; sd.ratio[p] = h.rmul[p] * h.ratio; }
     sd.tiles_x = (m.W + ASV_TILE_X - 1) / ASV_TILE_X;
     sd.tiles_y = (m.H + ASV_TILE_Y - 1) / ASV_TILE_Y;
+    sd.zrun = pick_zrun(ctx, std::vector<SegHost>(1, h));
     sd.angle_filter = 0;
     sd.wNum = h.g.wNum; sd.hNum = h.g.hNum; sd.dNum = h.g.dNum;
     sd.cell_off = 0;
     sd.final_buf = h.npass & 1;
     sd.lab_from = (long long)z0 * WH;
-    const int tiles = sd.tiles_x * sd.tiles_y * ((Db + ASV_TILE_Z - 1) / ASV_TILE_Z);
+    const int tiles = sd.tiles_x * sd.tiles_y * ((Db + sd.zrun - 1) / sd.zrun);
     const int chunks = (int)((sd.nvox + ASV_CHUNK - 1) / ASV_CHUNK);
     d.total_tiles = tiles;
     d.total_chunks = chunks;

@@ -13,9 +13,8 @@
 
 #define ASV_MAXP 32          // max JFA passes per Lloyd iteration
 #define ASV_CHUNK 2048       // voxels per block in the per-voxel kernels
-#define ASV_TILE_X 16        // JFA tile: 16 x 16 voxels x ASV_TILE_Z slices (a warp
-#define ASV_TILE_Y 16        // covers 16 x 2 voxels: fewer distinct candidates per warp)
-#define ASV_TILE_Z 8
+#define ASV_TILE_X 16        // JFA tile: 16 x 16 columns x SegDesc::zrun chain positions
+#define ASV_TILE_Y 16        // (a warp covers 16 x 2 columns: fewer distinct candidates)
 #define ASV_RING 24          // 8 one-ring + 16 two-ring neighbours of the metric fallback
 #define ASV_POST_WORDS 16    // per-segment post-processing record
 
@@ -28,6 +27,7 @@ struct SegDesc {
     int steps[ASV_MAXP];
     float ratio[ASV_MAXP];   // ratio of each pass (base ratio x 1 or x 2)
     int tiles_x, tiles_y;
+    int zrun;                // JFA tile depth: chain positions per column and tile
     int angle_filter;        // plain reseed flow-angle filter
     int wNum, hNum, dNum;    // seed grid (density placement)
     int cell_off;            // x cells at cell_off, y at +W, z at +W+H
@@ -111,3 +111,4 @@ void asv_launch_finalize(const AsvDev &d, cudaStream_t st);
 void asv_launch_post(const AsvDev &d, cudaStream_t st);
 void asv_launch_metric(const AsvDev &d, int reseed, cudaStream_t st);
 int asv_jfa_grid_blocks(int total_tiles);
+int asv_jfa_resident_blocks();

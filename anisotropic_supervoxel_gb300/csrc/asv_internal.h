@@ -1,6 +1,7 @@
 // asv_internal.h -- host-side helpers of libasv shared by the C ABI files.
 #pragma once
 
+#include "asv.h"
 #include "asv_common.cuh"
 
 #include <vector>
@@ -27,6 +28,7 @@ struct SegHost {
 };
 
 int grid_seeds(int W, int H, int D, int K, int middlebury, GridInfo *g, std::vector<float> *seeds4);
+size_t ctx_bytes(const asv_ctx *ctx);   // device bytes a context holds
 void cell_tables(int W, int H, int D, const GridInfo &g, const std::vector<float> &grid,
                  std::vector<int> *cells);
 float ratio_of(int s, float compactness);

@@ -273,84 +273,143 @@ __global__ void k_draw(AsvDev d)
 }
 
 // ---------------------------------------------------------------------------
-// One JFA pass (GPU-AS/shaders/flood.gs:26-182).  One thread per voxel,
-// 32x8-voxel tiles of one slice, persistent grid-stride over the tiles of
-// all segments (z-major, so the resident tiles share their +-step slices in
-// L2).  27 candidates in the shader's order: slices z, z-step, z+step; rows
-// y-step..y+step; columns x-step..x+step; clamp to edge.
+// One JFA pass (GPU-AS/shaders/flood.gs:26-182).  27 candidates per voxel in
+// the shader's order: slices z, z-step, z+step; in each slice rows
+// y-step..y+step, columns x-step..x+step; clamp to edge.  The winner is the
+// first candidate of least distance (strict `<` from 1e8), so any list that
+// holds every valid candidate id, each first listed in the order of its first
+// occurrence, gives the shader's label: a repeated id has the distance of its
+// first occurrence and never wins again.
 //
-// The candidates are first reduced to a list of ids in first-occurrence
-// order (a candidate equal to one of the five most recently listed ids is
-// dropped), kept in shared memory, and the list is evaluated in one loop: a
-// warp pays for its longest list instead of for every candidate position
-// where some lane meets a new id.  A dropped or repeated id has the same
-// distance as its first occurrence and the test is strict `<`, so the result
-// is the shader's.
+// Work layout: a block owns a tile of ASV_TILE_X x ASV_TILE_Y columns and a
+// run of `zrun` voxels of each column, taken in chain order for the
+// pass's step: z = r, r+step, r+2*step, ... (residue r = 0, 1, ...).  Along a
+// chain the slice z+step of one voxel is the centre slice of the next and its
+// centre the minus slice after that, so every slice's 9 labels are loaded
+// and reduced to a list of ids once and used by up to three voxels (about
+// 1.25 slice reductions per voxel instead of 3).  The voxel's list is the
+// centre list, then the ids of the minus and plus lists not already listed
+// (asv_merge_lists); a warp evaluates it in one loop, paying for its longest
+// list.
 // ---------------------------------------------------------------------------
 #define ASV_JFA_THREADS 256
+#define ASV_SLICE_MAX 9
+typedef int asv_list_t;      // candidate-list entry in shared memory (ids < 32768)
 
-__device__ __forceinline__ int asv_jfa_voxel(const int32_t *__restrict__ in, int32_t *__restrict__ out,
-                                              const uchar4 *__restrict__ lab,
-                                              const float4 *__restrict__ tab, int W, int H, int D,
-                                              int Kp, int x, int y, int z, int step, float ratio,
-                                              int *__restrict__ list)
+// chain order of the D slices for `step`: position p -> residue r, index j
+// in the chain, chain length len (z = r + j * step)
+__device__ __forceinline__ void asv_chain_pos(int p, int D, int step, int &r, int &j, int &len)
 {
-    const int sl = W * H;                       // segments hold < 2^31 voxels
-    const float vx = (float)x + 0.5f, vy = (float)y + 0.5f, vz = (float)z + 0.5f;
-    const int xs[3] = { max(x - step, 0), x, min(x + step, W - 1) };
-    const int ys[3] = { max(y - step, 0) * W, y * W, min(y + step, H - 1) * W };
-    const int zs[3] = { z * sl, max(z - step, 0) * sl, min(z + step, D - 1) * sl };
-    int32_t cand[27];
+    if (step >= D) { r = p; j = 0; len = 1; return; }
+    const int q = D / step, m = D - q * step;       // m chains of q+1 slices, the rest q
+    const int big = m * (q + 1);
+    if (p < big) { r = p / (q + 1); j = p - r * (q + 1); len = q + 1; }
+    else { const int pp = p - big; r = m + pp / q; j = pp - (r - m) * q; len = q; }
+}
+
+// valid ids among the 9 labels of one slice (offset zoff) around the
+// column, first-occurrence order; an id equal to one of the last four listed
+// is dropped.  Writes the list (stride ASV_JFA_THREADS), returns its length.
+__device__ __forceinline__ int asv_slice_list(const int32_t *__restrict__ in, int zoff, const int xs[3],
+                                              const int ys[3], int Kp, asv_list_t *__restrict__ lst)
+{
+    int n = 0, r1 = -1, r2 = -1, r3 = -1, r4 = -1;
 #pragma unroll
-    for (int s = 0; s < 3; s++)
+    for (int oy = 0; oy < 3; oy++)
 #pragma unroll
-        for (int oy = 0; oy < 3; oy++)
-#pragma unroll
-            for (int ox = 0; ox < 3; ox++) cand[(s * 3 + oy) * 3 + ox] = __ldg(in + zs[s] + ys[oy] + xs[ox]);
-    const uchar4 c = __ldg(lab + z * sl + y * W + x);
-    int n = 0, r1 = -1, r2 = -1, r3 = -1, r4 = -1, r5 = -1;
-#pragma unroll
-    for (int k = 0; k < 27; k++) {
-        const int32_t l = cand[k];
-        if ((unsigned)l < (unsigned)Kp && l != r1 && l != r2 && l != r3 && l != r4 && l != r5) {
-            list[n * ASV_JFA_THREADS] = l;
-            n++;
-            r5 = r4; r4 = r3; r3 = r2; r2 = r1; r1 = l;
+        for (int ox = 0; ox < 3; ox++) {
+            const int32_t l = __ldg(in + zoff + ys[oy] + xs[ox]);
+            if ((unsigned)l < (unsigned)Kp && l != r1 && l != r2 && l != r3 && l != r4) {
+                lst[n * ASV_JFA_THREADS] = l;
+                n++;
+                r4 = r3; r3 = r2; r2 = r1; r1 = l;
+            }
+        }
+    return n;
+}
+
+// The voxel's candidate list: the centre list A, then the ids of the minus
+// list B and the plus list C that are not among A's first four entries or
+// the last two ids appended (appended to X in order).  Returns X's length.
+__device__ __forceinline__ int asv_merge_lists(const asv_list_t *__restrict__ A, int na,
+                                               const asv_list_t *__restrict__ B, int nb,
+                                               const asv_list_t *__restrict__ C, int nc,
+                                               asv_list_t *__restrict__ X)
+{
+    const int h0 = na > 0 ? A[0] : -1, h1 = na > 1 ? A[ASV_JFA_THREADS] : -1;
+    const int h2 = na > 2 ? A[2 * ASV_JFA_THREADS] : -1, h3 = na > 3 ? A[3 * ASV_JFA_THREADS] : -1;
+    int nx = 0, r1 = -1, r2 = -1;
+    const int n = nb + nc;
+    for (int i = 0; i < n; i++) {
+        const int l = i < nb ? B[i * ASV_JFA_THREADS] : C[(i - nb) * ASV_JFA_THREADS];
+        if (l != h0 && l != h1 && l != h2 && l != h3 && l != r1 && l != r2) {
+            X[nx * ASV_JFA_THREADS] = l;
+            nx++;
+            r2 = r1; r1 = l;
         }
     }
+    return nx;
+}
+
+// flood.gs:72-94: anisotropic distance of the voxel centre (vx, vy, vz) with
+// LAB (cL, ca, cb) to seed l of the table, in the shader's operation order
+__device__ __forceinline__ float asv_jfa_dist(const float4 *__restrict__ tab, int l, float vx, float vy,
+                                              float vz, float cL, float ca, float cb, float ratio)
+{
+    const float4 t0 = __ldg(tab + 3 * l), t1 = __ldg(tab + 3 * l + 1), t2 = __ldg(tab + 3 * l + 2);
+    const float dx = vx - t0.x, dy = vy - t0.y, dz = vz - t0.z;
+    float p1 = (dx * dx) * t1.z + (dx * dy) * t1.w;                  // flood.gs:85
+    p1 = p1 + (dx * dz) * t2.x;
+    float p2 = (dy * dy) * t2.y + (dy * dz) * t2.z;
+    p2 = p2 + (dz * dz) * t2.w;
+    float pos = p1 + p2;
+    const float eL = cL - t0.w, ea = ca - t1.x, eb = cb - t1.y;
+    float col = eL * eL + ea * ea;                                     // flood.gs:89
+    col = col + eb * eb;
+    pos = (pos < 0.0f) ? 0.0f : pos;                                   // flood.gs:90-93
+    return ratio * pos + col;                                          // flood.gs:94
+}
+
+// distance loop over the concatenated lists A (na) and X (nx): the first
+// candidate of least distance wins (flood.gs:63, :95-99)
+__device__ __forceinline__ int32_t asv_jfa_eval(const asv_list_t *__restrict__ A, int na,
+                                                const asv_list_t *__restrict__ X, int nx,
+                                                const float4 *__restrict__ tab, uchar4 c, float vx, float vy,
+                                                float vz, float ratio)
+{
     const float cL = (float)c.x, ca = (float)c.y, cb = (float)c.z;
-    float mind = 100000000.0f;                                        // flood.gs:63
+    float mind = 100000000.0f;
     int32_t best = -1;
-    for (int i = 0; i < n; i++) {
-        const int32_t l = list[i * ASV_JFA_THREADS];
-        const float4 t0 = __ldg(tab + 3 * l), t1 = __ldg(tab + 3 * l + 1), t2 = __ldg(tab + 3 * l + 2);
-        const float dx = vx - t0.x, dy = vy - t0.y, dz = vz - t0.z;
-        float p1 = (dx * dx) * t1.z + (dx * dy) * t1.w;              // flood.gs:85
-        p1 = p1 + (dx * dz) * t2.x;
-        float p2 = (dy * dy) * t2.y + (dy * dz) * t2.z;
-        p2 = p2 + (dz * dz) * t2.w;
-        float pos = p1 + p2;
-        const float eL = cL - t0.w, ea = ca - t1.x, eb = cb - t1.y;
-        float col = eL * eL + ea * ea;                                 // flood.gs:89
-        col = col + eb * eb;
-        pos = (pos < 0.0f) ? 0.0f : pos;                               // flood.gs:90-93
-        const float dist = ratio * pos + col;                          // flood.gs:94
-        if (dist < mind) { mind = dist; best = l; }                    // flood.gs:95-99
+    const int n = na + nx;
+    int i = 0;
+    for (; i + 1 < n; i += 2) {          // two candidates per trip: their loads overlap
+        const int32_t la = i < na ? A[i * ASV_JFA_THREADS] : X[(i - na) * ASV_JFA_THREADS];
+        const int32_t lb = i + 1 < na ? A[(i + 1) * ASV_JFA_THREADS] : X[(i + 1 - na) * ASV_JFA_THREADS];
+        const float da = asv_jfa_dist(tab, la, vx, vy, vz, cL, ca, cb, ratio);
+        const float db = asv_jfa_dist(tab, lb, vx, vy, vz, cL, ca, cb, ratio);
+        if (da < mind) { mind = da; best = la; }     // compared in list order
+        if (db < mind) { mind = db; best = lb; }
     }
-    out[z * sl + y * W + x] = best;
+    if (i < n) {
+        const int32_t l = i < na ? A[i * ASV_JFA_THREADS] : X[(i - na) * ASV_JFA_THREADS];
+        const float dist = asv_jfa_dist(tab, l, vx, vy, vz, cL, ca, cb, ratio);
+        if (dist < mind) { mind = dist; best = l; }
+    }
     return best;
 }
 
 // Centroid sums of one voxel, fused into the last JFA pass of a Lloyd
 // iteration (centroids.vs:19-54): the lanes that run together are grouped by
-// label, reduced in the warp, and one u64 atomic per group and component is
-// issued.  Grouping over whichever lanes are active keeps the sums exact.
-__device__ __forceinline__ void asv_accumulate(unsigned long long *__restrict__ sums,
-                                               const uchar4 *__restrict__ lab, int W, int H, int Kp,
-                                               int x, int y, int z, int best)
+// destination slot, reduced in the warp, and one u64 atomic per group and
+// component is issued.  Lanes of one warp can be in different tiles at this
+// point (a lane that left its tile early runs ahead into the next one, which
+// may belong to another segment), so the group key is the global sum slot
+// `slot0 + label`, never the segment-local label; grouping over whichever
+// lanes are active keeps the sums exact.
+__device__ __forceinline__ void asv_accumulate(unsigned long long *__restrict__ sums, int slot0, uchar4 c,
+                                               int Kp, int x, int y, int z, int best)
 {
-    const uchar4 c = __ldg(lab + (z * H + y) * W + x);
-    const int key = best < 0 ? Kp : best;
+    const int key = slot0 + (best < 0 ? Kp : best);
     const unsigned act = __activemask();
     const unsigned grp = __match_any_sync(act, key);
     const unsigned q[7] = { 2u * x + 1u, 2u * y + 1u, 2u * z + 1u, 1u, c.x, c.y, c.z };
@@ -364,13 +423,62 @@ __device__ __forceinline__ void asv_accumulate(unsigned long long *__restrict__ 
     }
 }
 
-// tile = ASV_TILE_X x ASV_TILE_Y voxels x ASV_TILE_Z slices; the tile
-// coordinates are derived once per tile, the slices walked inside it
-__global__ void __launch_bounds__(ASV_JFA_THREADS) k_jfa(AsvDev d, int pass,
+// One column's run of zrun chain positions [p0, p0 + zrun).
+// `lists` is this thread's first entry of 3 slice-list rows of ASV_SLICE_MAX
+// entries and one merge row of 2 x ASV_SLICE_MAX.  A
+// chain continues while z + step < D; the next chain starts at the next
+// residue, whose minus slice is slice 0.
+template <bool SUMS>
+__device__ __forceinline__ void asv_jfa_run(const int32_t *__restrict__ in, int32_t *__restrict__ out,
+                                            const uchar4 *__restrict__ lab, const float4 *__restrict__ tab,
+                                            unsigned long long *__restrict__ sums, int slot0, int W, int H, int D,
+                                            int Kp, int x, int y, int p0, int zrun, int step,
+                                            float ratio, asv_list_t *__restrict__ lists)
+{
+    const int sl = W * H;                       // segments hold < 2^31 voxels
+    const int xs[3] = { max(x - step, 0), x, min(x + step, W - 1) };
+    const int ys[3] = { max(y - step, 0) * W, y * W, min(y + step, H - 1) * W };
+    const int col = y * W + x;
+    const float vx = (float)x + 0.5f, vy = (float)y + 0.5f;
+    const int row = ASV_SLICE_MAX * ASV_JFA_THREADS;
+    int r, j, len;
+    asv_chain_pos(p0, D, step, r, j, len);
+    int z = r + j * step;
+    int n = min(zrun, D - p0);
+    int sm = 0, sc = 1, sp = 2;                 // list rows of the minus / centre / plus slices
+    int nm = asv_slice_list(in, max(z - step, 0) * sl, xs, ys, Kp, lists + sm * row);
+    int nc = asv_slice_list(in, z * sl, xs, ys, Kp, lists + sc * row);
+    while (true) {
+        const bool more = z + step < D;         // the chain goes on
+        const int zp = more ? z + step : D - 1;
+        const int np = asv_slice_list(in, zp * sl, xs, ys, Kp, lists + sp * row);
+        const uchar4 c = __ldg(lab + z * sl + col);
+        const int nx = asv_merge_lists(lists + sc * row, nc, lists + sm * row, nm, lists + sp * row, np,
+                                       lists + 3 * row);
+        const int32_t best = asv_jfa_eval(lists + sc * row, nc, lists + 3 * row, nx, tab, c, vx, vy,
+                                          (float)z + 0.5f, ratio);
+        out[z * sl + col] = best;
+        if (SUMS) asv_accumulate(sums, slot0, c, Kp, x, y, z, best);
+        if (--n == 0) break;
+        if (more) {                             // next voxel of the chain: rotate the rows
+            z = zp;
+            const int t = sm;
+            sm = sc; sc = sp; sp = t;
+            nm = nc; nc = np;
+        } else {                                // next residue: a new chain
+            z = z - (z / step) * step + 1;
+            nm = asv_slice_list(in, 0, xs, ys, Kp, lists + sm * row);
+            nc = asv_slice_list(in, z * sl, xs, ys, Kp, lists + sc * row);
+        }
+    }
+}
+
+// tile = ASV_TILE_X x ASV_TILE_Y columns x S.zrun chain positions
+__global__ void __launch_bounds__(ASV_JFA_THREADS, 3) k_jfa(AsvDev d, int pass,
                                                          const int32_t *__restrict__ in,
                                                          int32_t *__restrict__ out)
 {
-    __shared__ int list[27 * ASV_JFA_THREADS];
+    __shared__ asv_list_t lists[5 * ASV_SLICE_MAX * ASV_JFA_THREADS];
     const int lx = threadIdx.x % ASV_TILE_X, ly = threadIdx.x / ASV_TILE_X;
     for (int t = blockIdx.x; t < d.total_tiles; t += gridDim.x) {
         const int si = asv_find_seg(d.tile_prefix, d.nseg, t);
@@ -378,21 +486,17 @@ __global__ void __launch_bounds__(ASV_JFA_THREADS) k_jfa(AsvDev d, int pass,
         if (pass >= S.npass) continue;
         const int lt = t - d.tile_prefix[si];
         const int tx = lt % S.tiles_x, rest = lt / S.tiles_x;
-        const int ty = rest % S.tiles_y, z0 = (rest / S.tiles_y) * ASV_TILE_Z;
+        const int ty = rest % S.tiles_y, p0 = (rest / S.tiles_y) * S.zrun;
         const int x = tx * ASV_TILE_X + lx, y = ty * ASV_TILE_Y + ly;
         if (x >= S.W || y >= S.H) continue;
-        const int z1 = min(z0 + ASV_TILE_Z, S.D);
-        const int step = S.steps[pass];
-        const float ratio = S.ratio[pass];
-        const bool last = pass == S.npass - 1;     // the iteration's labels: sum them
-        for (int z = z0; z < z1; z++) {
-            const int best = asv_jfa_voxel(in + S.vox_off, out + S.vox_off, d.lab + S.vox_off,
-                                           d.jtab + 3 * S.seed_off, S.W, S.H, S.D, S.Kp, x, y, z, step,
-                                           ratio, list + threadIdx.x);
-            if (last)
-                asv_accumulate(d.sums + 8ull * S.seed_off, d.lab + S.vox_off, S.W, S.H, S.Kp, x, y, z,
-                               best);
-        }
+        if (pass == S.npass - 1)                   // the iteration's labels: sum them
+            asv_jfa_run<true>(in + S.vox_off, out + S.vox_off, d.lab + S.vox_off, d.jtab + 3 * S.seed_off,
+                              d.sums, S.seed_off, S.W, S.H, S.D, S.Kp, x, y, p0, S.zrun,
+                              S.steps[pass], S.ratio[pass], lists + threadIdx.x);
+        else
+            asv_jfa_run<false>(in + S.vox_off, out + S.vox_off, d.lab + S.vox_off, d.jtab + 3 * S.seed_off,
+                               nullptr, 0, S.W, S.H, S.D, S.Kp, x, y, p0, S.zrun, S.steps[pass],
+                               S.ratio[pass], lists + threadIdx.x);
     }
 }
 
@@ -401,20 +505,18 @@ __global__ void __launch_bounds__(ASV_JFA_THREADS) k_jfa_single(AsvDev d, const 
                                                                 int32_t *__restrict__ out, int step,
                                                                 float ratio)
 {
-    __shared__ int list[27 * ASV_JFA_THREADS];
+    __shared__ asv_list_t lists[5 * ASV_SLICE_MAX * ASV_JFA_THREADS];
     const SegDesc &S = d.segs[0];
     const int lx = threadIdx.x % ASV_TILE_X, ly = threadIdx.x / ASV_TILE_X;
-    const int tiles_z = (S.D + ASV_TILE_Z - 1) / ASV_TILE_Z;
+    const int tiles_z = (S.D + S.zrun - 1) / S.zrun;
     const int ntiles = S.tiles_x * S.tiles_y * tiles_z;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int tx = t % S.tiles_x, rest = t / S.tiles_x;
-        const int ty = rest % S.tiles_y, z0 = (rest / S.tiles_y) * ASV_TILE_Z;
+        const int ty = rest % S.tiles_y, p0 = (rest / S.tiles_y) * S.zrun;
         const int x = tx * ASV_TILE_X + lx, y = ty * ASV_TILE_Y + ly;
         if (x >= S.W || y >= S.H) continue;
-        const int z1 = min(z0 + ASV_TILE_Z, S.D);
-        for (int z = z0; z < z1; z++)
-            asv_jfa_voxel(in, out, d.lab + S.vox_off, d.jtab + 3 * S.seed_off, S.W, S.H, S.D, S.Kp,
-                          x, y, z, step, ratio, list + threadIdx.x);
+        asv_jfa_run<false>(in, out, d.lab + S.vox_off, d.jtab + 3 * S.seed_off, nullptr, 0, S.W, S.H,
+                           S.D, S.Kp, x, y, p0, S.zrun, step, ratio, lists + threadIdx.x);
     }
 }
 
@@ -760,17 +862,24 @@ void asv_launch_density_adjust(const AsvDev &d, cudaStream_t st)
 void asv_launch_first_init(const AsvDev &d, cudaStream_t st) { k_first_init<<<seed_blocks(d), 128, 0, st>>>(d); }
 void asv_launch_draw(const AsvDev &d, cudaStream_t st) { k_draw<<<seed_blocks(d), 128, 0, st>>>(d); }
 
-int asv_jfa_grid_blocks(int total_tiles)
+// resident k_jfa blocks on the device (persistent grid size); computed once
+// per process (thread-safe static initialisation)
+int asv_jfa_resident_blocks()
 {
-    static int blocks = 0;
-    if (!blocks) {
+    static const int blocks = [] {
         int dev = 0, sms = 0, per = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_jfa, 256, 0);
-        blocks = sms * (per > 0 ? per : 1);
-        if (blocks <= 0) blocks = 1024;
-    }
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_jfa, ASV_JFA_THREADS, 0);
+        const int b = sms * (per > 0 ? per : 1);
+        return b > 0 ? b : 1024;
+    }();
+    return blocks;
+}
+
+int asv_jfa_grid_blocks(int total_tiles)
+{
+    const int blocks = asv_jfa_resident_blocks();
     return total_tiles < blocks ? total_tiles : blocks;
 }
 

@@ -33,12 +33,13 @@ def synth_clip(W, H, D, n_ellipses=12, noise_sigma=5.0, vmax=3.0, jitter=0.0, dr
 
 
 def config(variant=_lib.VARIANT_PLAIN, lloyd_iters=20, full_ladder=0, middlebury=0,
-           density_adjust=1, device=0, stream=None, hbm_budget=0, use_graph=1, instrument=0):
+           density_adjust=1, device=0, stream=None, hbm_budget=0, use_graph=1, instrument=0,
+           jfa_zrun=0):
     c = Config()
     _lib.load().asv_config_default(ctypes.byref(c))
     c.variant, c.lloyd_iters, c.full_ladder, c.middlebury = variant, lloyd_iters, full_ladder, middlebury
     c.density_adjust, c.device, c.stream, c.hbm_budget = density_adjust, device, stream, hbm_budget
-    c.use_graph, c.instrument = use_graph, instrument
+    c.use_graph, c.instrument, c.jfa_zrun = use_graph, instrument, jfa_zrun
     return c
 
 
@@ -117,6 +118,13 @@ class Image:
     def run_lloyd(self):
         self._ck(self.lib.asv_run_lloyd(self.h))
 
+    def autotune(self):
+        """asv_autotune: times the Lloyd loop at JFA tile depths 4..32, keeps the
+        fastest; returns it."""
+        z = ctypes.c_int()
+        self._ck(self.lib.asv_autotune(self.h, ctypes.byref(z)))
+        return z.value
+
     # --- state ---------------------------------------------------------------
     def info(self):
         i = Info()
@@ -188,6 +196,43 @@ class Image:
         return self.labels()
 
 
+class Batch(Image):
+    """Many clips of uneven size in one context: every stage one launch over all
+    clips, the Lloyd loop one CUDA graph (asv_batch_*)."""
+
+    def __init__(self, dims, **kw):
+        """dims: list of (W, H, D, K) per clip."""
+        super().__init__(**kw)
+        arr = [np.ascontiguousarray([d[i] for d in dims], np.int32) for i in range(4)]
+        self._dims = arr
+        self._ck(self.lib.asv_batch_init(self.h, len(dims), *[_ptr(a) for a in arr]))
+        self.shapes = [(int(d[2]), int(d[1]), int(d[0])) for d in dims]
+
+    def upload(self, i, rgb, fwd, bwd):
+        rgb = np.ascontiguousarray(rgb, np.uint8)
+        fwd = np.ascontiguousarray(fwd, np.float32)
+        bwd = np.ascontiguousarray(bwd, np.float32)
+        if rgb.shape[:3] != self.shapes[i]:
+            raise ValueError(f"clip {i} is {self.shapes[i]}, got {rgb.shape[:3]}")
+        self._ck(self.lib.asv_batch_upload(self.h, i, _ptr(rgb), _ptr(fwd), _ptr(bwd)))
+
+    def prepare(self):
+        """initialization + seed_matrix + RGB2LAB for every clip."""
+        self.initialization()
+        self.seed_matrix()
+        self.RGB2LAB()
+
+    def clip_labels(self, i):
+        out = np.empty(self.shapes[i], np.int32)
+        self._ck(self.lib.asv_batch_get_labels(self.h, i, _ptr(out)))
+        return out
+
+    def clip_info(self, i):
+        inf = Info()
+        self._ck(self.lib.asv_batch_get_info(self.h, i, ctypes.byref(inf)))
+        return inf
+
+
 class Stream(Image):
     """The reference's streaming form (streamGPU-AS/Render.cpp:100-569) on the
     device: `push` takes a block's new frames and returns the video-wide labels
@@ -218,6 +263,100 @@ class Stream(Image):
         self._ck(self.lib.asv_stream_push(self.h, _ptr(rgb), _ptr(fwd), _ptr(bwd), _ptr(out),
                                           ctypes.byref(done)))
         return inf.block_start, out[:done.value]
+
+
+class Server:
+    """Request pool on one GPU (asv_server_*): clip requests admitted first-fit
+    under an HBM budget, each on its own slot stream, plus streaming sessions
+    whose windows run in order.  `submit_*` returns a request id; `wait` gives
+    (labels, latency_ms, queue_ms)."""
+
+    def __init__(self, max_slots=4, hbm_budget=0, **kw):
+        self.lib = _lib.load()
+        self.cfg = config(**kw)
+        h = ctypes.c_void_p()
+        st = self.lib.asv_server_create(ctypes.byref(self.cfg), max_slots, hbm_budget, ctypes.byref(h))
+        if st != _lib.ASV_OK:
+            raise AsvError(st, self.lib.asv_status_string(st).decode())
+        self.h = h
+        self._live = {}      # id -> (arrays kept alive, labels out, session W/H)
+        self._sessions = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.asv_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _ck(self, st):
+        if st != _lib.ASV_OK:
+            raise AsvError(st, self.lib.asv_status_string(st).decode())
+
+    def open_session(self, W, H, D_all, K_video=0, seeds_num_100=0, block_size=30):
+        sid = ctypes.c_int()
+        self._ck(self.lib.asv_server_open_session(self.h, W, H, D_all, K_video, seeds_num_100,
+                                                  block_size, ctypes.byref(sid)))
+        self._sessions[sid.value] = (W, H, block_size or 30)
+        return sid.value
+
+    def _submit(self, req, keep, out):
+        rid = ctypes.c_longlong()
+        self._ck(self.lib.asv_server_submit(self.h, ctypes.byref(req), ctypes.byref(rid)))
+        self._live[rid.value] = (keep, out, req.kind == _lib.REQ_WINDOW)
+        return rid.value
+
+    def submit_clip(self, rgb, fwd, bwd, K):
+        rgb = np.ascontiguousarray(rgb, np.uint8)
+        fwd = np.ascontiguousarray(fwd, np.float32)
+        bwd = np.ascontiguousarray(bwd, np.float32)
+        D, H, W = rgb.shape[:3]
+        out = np.empty((D, H, W), np.int32)
+        req = _lib.Request(_lib.REQ_CLIP, 0, W, H, D, K, _ptr(rgb).value, _ptr(fwd).value,
+                           _ptr(bwd).value, _ptr(out).value)
+        return self._submit(req, (rgb, fwd, bwd), out)
+
+    def submit_window(self, session, rgb, fwd, bwd):
+        """the next block's new frames of a session (asv_stream_push semantics)"""
+        W, H, block = self._sessions[session]
+        rgb = np.ascontiguousarray(rgb, np.uint8)
+        fwd = np.ascontiguousarray(fwd, np.float32)
+        bwd = np.ascontiguousarray(bwd, np.float32)
+        # the last block of a video can reach block_size + block_size/3 - 1 frames
+        out = np.empty((block + block // 3, H, W), np.int32)
+        req = _lib.Request(_lib.REQ_WINDOW, session, W, H, rgb.shape[0], 0, _ptr(rgb).value,
+                           _ptr(fwd).value, _ptr(bwd).value, _ptr(out).value)
+        return self._submit(req, (rgb, fwd, bwd), out)
+
+    def wait(self, rid):
+        lat, qms, done = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
+        st = self.lib.asv_server_wait(self.h, rid, ctypes.byref(lat), ctypes.byref(qms),
+                                      ctypes.byref(done))
+        keep, out, window = self._live.pop(rid)
+        self._ck(st)
+        if window:
+            out = out[:done.value]
+        return out, lat.value, qms.value
+
+    def poll(self, rid):
+        d = ctypes.c_int()
+        self._ck(self.lib.asv_server_poll(self.h, rid, ctypes.byref(d)))
+        return bool(d.value)
+
+    def stats(self):
+        s = _lib.ServerStats()
+        self._ck(self.lib.asv_server_get_stats(self.h, ctypes.byref(s)))
+        return s
 
 
 def write_labels_txt(path, labels):

@@ -12,10 +12,12 @@ CLIP_240x160x30 = dict(W=240, H=160, D=30, n_ellipses=12, noise_sigma=5.0, vmax=
 # single clip: 320x240x85, 30 ellipses with +-0.5 px/frame jitter, sigma 8, K=1000, 15 iterations
 CLIP_320x240x85 = dict(W=320, H=240, D=85, n_ellipses=30, noise_sigma=8.0, vmax=3.0,
                        jitter=0.5, K=1000, iters=15, seed=20240602)
-# streaming 1280x720 video, 60 ellipses, sinusoidal background drift, windows 30/10
+# streaming 1280x720 video, 60 ellipses, sinusoidal background drift, windows 30/10;
+# K = 2000 new seeds per window of 20 new frames: seeds_num_100 = 2000 * 100 / 20
+# (the window also carries the seeds of its 10 overlap frames from the previous one)
 STREAM_720P = dict(W=1280, H=720, D_all=900, n_ellipses=60, noise_sigma=5.0, vmax=3.0,
-                   jitter=0.0, drift_amp=6.0, drift_period=90.0, K_window=2000, iters=20,
-                   block_size=30, seed=20240604)
+                   jitter=0.0, drift_amp=6.0, drift_period=90.0, K_window=2000,
+                   seeds_num_100=10000, iters=20, block_size=30, seed=20240604)
 
 
 def batch_clips(n=16, seed=20240603):

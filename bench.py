@@ -44,7 +44,10 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="clip_320x240x85",
-                    choices=["clip_320x240x85", "clip_240x160x30"])
+                    choices=["clip_320x240x85", "clip_240x160x30", "batch16", "stream_720p",
+                             "serve_mix"])
+    ap.add_argument("--requests", type=int, default=160, help="serve_mix: requests in the run")
+    ap.add_argument("--rate", type=float, default=40.0, help="serve_mix: mean arrivals per second")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 
@@ -151,6 +154,10 @@ def config_of(w, name, N):
 def run_reference(args):
     ws, rank, _ = dist()
     if rank != 0:
+        return
+    if args.workload not in ("clip_320x240x85", "clip_240x160x30"):
+        print(json.dumps({"impl": "reference", "unavailable": "the CPU arm covers the single-clip "
+                          "workloads; " + args.workload + " has no CPU counterpart"}), flush=True)
         return
     w = workload(args.workload)
     from anisotropic_supervoxel_gb300 import workloads
@@ -331,10 +338,287 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def _pct(v, q):
+    v = sorted(v)
+    if not v:
+        return None
+    k = min(len(v) - 1, max(0, int(round(q / 100.0 * (len(v) - 1)))))
+    return v[k]
+
+
+def _pinned(a):
+    import torch
+    t = torch.empty(a.shape, dtype=getattr(torch, str(a.dtype)), pin_memory=True)
+    t.numpy()[...] = a
+    return t.numpy()
+
+
+def _line(args, value, ms_per_step, config, extra):
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded ellipse video, exact generating flow)", "config": config}
+    line.update(extra)
+    print(json.dumps(line), flush=True)
+
+
+def run_batch16(args):
+    """16 clips of uneven size in one context (asv_batch_*): every stage one
+    launch over all clips, the Lloyd loop one graph.  Compared with the plain
+    per-clip form (one Image per clip, each its own graph) on the same clips."""
+    import numpy as np
+    import torch
+
+    import anisotropic_supervoxel_gb300 as asv
+    from anisotropic_supervoxel_gb300 import workloads
+    torch.cuda.set_device(0)
+    ws = workloads.batch_clips()
+    dims = [(w["W"], w["H"], w["D"], w["K"]) for w in ws]
+    clips = [workloads.make_clip(w) for w in ws]
+    I = ws[0]["iters"]
+    vox_it = sum(W * H * D for W, H, D, _ in dims) * I
+    b = asv.Batch(dims, lloyd_iters=I)
+    for i, c in enumerate(clips):
+        b.upload(i, *c)
+    b.prepare()
+    b.synchronize()
+    st = torch.cuda.ExternalStream(b.stream(), device=torch.device("cuda", 0))
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda:0")
+    for _ in range(args.warmup):
+        b.run_lloyd()
+    b.synchronize()
+    launches = b.stats().launches
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    clocks = Clocks(0)
+    torch.cuda.synchronize()
+    clocks.start()
+    for k in range(args.steps):
+        with torch.cuda.stream(st):
+            flush.fill_(k & 255)
+        ev[k][0].record(st)
+        b.run_lloyd()
+        ev[k][1].record(st)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = [x.elapsed_time(y) for x, y in ev]
+    value = vox_it * args.steps / (sum(ms) / 1e3) / 1e6
+    batch_labels = [b.clip_labels(i) for i in range(len(dims))]
+
+    # plain per-clip form: each clip its own context and graph, run one after another
+    imgs = []
+    for (W, H, D, K), c in zip(dims, clips):
+        im = asv.Image(lloyd_iters=I)
+        im.init_gpu(c[0], K)
+        im.upload_flow(c[1], c[2])
+        im.initialization()
+        im.seed_matrix()
+        im.RGB2LAB()
+        im.run_lloyd()
+        imgs.append(im)
+    torch.cuda.synchronize()
+    same = all(np.array_equal(im.labels(), bl) for im, bl in zip(imgs, batch_labels))
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for im in imgs:            # one clip at a time, as the per-clip form runs
+            im.run_lloyd()
+            im.synchronize()
+    plain_s = time.perf_counter() - t0
+    plain = vox_it * args.steps / plain_s / 1e6
+    for im in imgs:
+        im.close()
+
+    # e2e: pinned host clips in, labels out, through the batch API
+    pin = [tuple(_pinned(a) for a in c) for c in clips]
+    outs = [_pinned(np.empty((D, H, W), np.int32)) for W, H, D, _ in dims]
+    lib = b.lib
+    for _ in range(2):
+        for i, c in enumerate(pin):
+            b.upload(i, *c)
+        b.prepare()
+        b.run_lloyd()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for i, c in enumerate(pin):
+            b.upload(i, *c)
+        b.prepare()
+        b.run_lloyd()
+        for i, o in enumerate(outs):
+            lib.asv_batch_get_labels(b.h, i, o.ctypes.data)
+    e2e_s = time.perf_counter() - t0
+    h2d = sum(a.nbytes for c in clips for a in c)
+    d2h = sum(o.nbytes for o in outs)
+    b.close()
+    _line(args, value, sum(ms) / len(ms),
+          {"workload": "batch16_uneven", "clips": len(dims),
+           "voxels": sum(W * H * D for W, H, D, _ in dims), "K_total": sum(d[3] for d in dims),
+           "lloyd_iters": I, "variant": "plain", "parallelism": "replicas1",
+           "l2": "flushed before every step (512 MiB write)"},
+          {"e2e": {"value": vox_it * args.steps / e2e_s / 1e6, "unit": UNIT,
+                   "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+           "plain_per_clip": {"value": plain, "unit": UNIT,
+                              "note": "same clips, one context and graph per clip, sequential"},
+           "batch_over_plain": value / plain, "labels_equal_plain": same,
+           "clocks": clk, "gpu_launches": int(launches * args.steps)})
+
+
+def run_stream_720p(args):
+    """1280x720 video, 900 frames, 30-frame windows with 10-frame overlap, on
+    one resident streaming context; per-window latency = asv_stream_push wall
+    time (new frames up from pinned memory, the window's Lloyd loop, finished
+    labels back)."""
+    import numpy as np
+    import torch
+
+    import anisotropic_supervoxel_gb300 as asv
+    from anisotropic_supervoxel_gb300 import workloads
+    torch.cuda.set_device(0)
+    w = workloads.STREAM_720P
+    W, H, D_all, bs = w["W"], w["H"], w["D_all"], w["block_size"]
+    s100 = w["seeds_num_100"]
+    st = asv.Stream(W, H, D_all, seeds_num_100=s100, block_size=bs, lloyd_iters=w["iters"])
+    nb = st.info().blocks
+    lat, vox_it, kps = [], 0, []
+    clocks = Clocks(0)
+    clocks.start()
+    t_all = 0.0
+    for b in range(nb):
+        inf = st.info()
+        a = inf.block_end - inf.frames_needed
+        rgb, fwd, bwd = asv.synth_clip(W, H, inf.frames_needed, n_ellipses=w["n_ellipses"],
+                                       noise_sigma=w["noise_sigma"], vmax=w["vmax"],
+                                       drift_amp=w["drift_amp"], drift_period=w["drift_period"],
+                                       seed=w["seed"], frame0=a)
+        rgb, fwd, bwd = _pinned(rgb), _pinned(fwd), _pinned(bwd)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st.push(rgb, fwd, bwd)
+        dt = time.perf_counter() - t0
+        if b >= args.warmup:
+            lat.append(dt * 1e3)
+            vox_it += W * H * (inf.block_end - inf.block_start) * w["iters"]
+            t_all += dt
+            kps.append(st.info().block_Kp)
+    clk = clocks.stop()
+    st.close()
+    value = vox_it / t_all / 1e6
+    _line(args, value, statistics.mean(lat),
+          {"workload": "stream_1280x720x900_w30o10", "K_window": w["K_window"],
+           "seeds_num_100": s100, "lloyd_iters": w["iters"], "variant": "stream",
+           "parallelism": "replicas1", "l2": "inputs larger than L2 (each window 27.6 M voxels)"},
+          {"latency_ms": {"p50": _pct(lat, 50), "p99": _pct(lat, 99), "max": max(lat),
+                          "windows": len(lat), "target_p99": 33.0},
+           "block_Kp_mean": statistics.mean(kps),
+           "e2e": {"value": value, "unit": UNIT,
+                   "h2d_bytes_per_step": int(W * H * 20 * 19), "d2h_bytes_per_step": int(W * H * 20 * 4)},
+           "clocks": clk})
+
+
+def run_serve_mix(args):
+    """Poisson arrivals of mixed requests through the request pool
+    (asv_server_*): 50% 240x160x30 K=200 clips, 35% 640x480x60 K=1000 clips,
+    15% 720p 30-frame streaming windows K=2000 (two sessions), 120 GB HBM
+    budget.  Latency = submit -> labels on the host."""
+    import numpy as np
+    import torch
+
+    import anisotropic_supervoxel_gb300 as asv
+    from anisotropic_supervoxel_gb300 import workloads
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(20240605)
+    mix = workloads.serving_mix()
+    n = args.requests
+    kinds = rng.choice(len(mix), size=n, p=[m[0] for m in mix])
+    gaps = rng.exponential(1.0 / args.rate, size=n)
+    # input pools (two clips per clip class, reused; one 30- and one 20-frame window)
+    pools = {}
+    for c in (0, 1):
+        w = dict(mix[c][1])
+        pools[c] = []
+        for j in range(2):
+            w["seed"] = 777 + 10 * c + j
+            pools[c].append(tuple(_pinned(a) for a in workloads.make_clip(w)))
+    ww = mix[2][1]
+    win = {}
+    for nf, f0 in ((30, 0), (20, 30)):
+        win[nf] = tuple(_pinned(a) for a in asv.synth_clip(
+            ww["W"], ww["H"], nf, n_ellipses=ww["n_ellipses"], noise_sigma=ww["noise_sigma"],
+            vmax=ww["vmax"], seed=4242, frame0=f0))
+    n_sess = 2
+    per_sess = [0] * n_sess
+    plan = []
+    for i, k in enumerate(kinds):
+        if k == 2:
+            s = sum(per_sess) % n_sess
+            plan.append((2, s, per_sess[s]))
+            per_sess[s] += 1
+        else:
+            plan.append((int(k), i % 2, 0))
+    budget = 120 << 30
+    srv = asv.Server(max_slots=6, hbm_budget=budget, lloyd_iters=10)
+    sids = []
+    for s in range(n_sess):
+        nw = max(per_sess[s], 1)
+        sids.append(srv.open_session(ww["W"], ww["H"], 30 + 20 * (nw - 1),
+                                     seeds_num_100=ww["K"] * 100 // 20))
+    # warm-up: one request of each clip class
+    for c in (0, 1):
+        srv.wait(srv.submit_clip(*pools[c][0], mix[c][1]["K"]))
+    clocks = Clocks(0)
+    clocks.start()
+    ids, vox = [], 0
+    t0 = time.perf_counter()
+    t_next = t0
+    for (k, j, b), g in zip(plan, gaps):
+        t_next += g
+        now = time.perf_counter()
+        if t_next > now:
+            time.sleep(t_next - now)
+        if k == 2:
+            nf = 30 if b == 0 else 20
+            ids.append((k, srv.submit_window(sids[j], *win[nf])))
+            vox += ww["W"] * ww["H"] * 30 * 10
+        else:
+            w = mix[k][1]
+            ids.append((k, srv.submit_clip(*pools[k][j], w["K"])))
+            vox += w["W"] * w["H"] * w["D"] * 10
+    lat = {0: [], 1: [], 2: []}
+    for k, rid in ids:
+        _, ms, _ = srv.wait(rid)
+        lat[k].append(ms)
+    t_end = time.perf_counter()
+    clk = clocks.stop()
+    st = srv.stats()
+    srv.close()
+    allv = lat[0] + lat[1] + lat[2]
+    span = t_end - t0
+    value = vox / span / 1e6
+    names = ["clip_240x160x30", "clip_640x480x60", "window_1280x720x30"]
+    _line(args, value, span * 1e3 / n,
+          {"workload": "serve_poisson_mix", "requests": n, "rate_per_s": args.rate,
+           "mix": "50% 240x160x30 K200, 35% 640x480x60 K1000, 15% 720p 30-frame windows K2000",
+           "hbm_budget_gb": 120, "slots": 6, "sessions": n_sess, "lloyd_iters": 10,
+           "parallelism": "replicas1", "l2": "inputs larger than L2"},
+          {"latency_ms": {"p50": _pct(allv, 50), "p99": _pct(allv, 99),
+                          **{nm: {"p50": _pct(lat[i], 50), "p99": _pct(lat[i], 99), "n": len(lat[i])}
+                             for i, nm in enumerate(names)}},
+           "requests_per_s": n / span, "failed": st.failed,
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": None,
+                   "d2h_bytes_per_step": None},
+           "clocks": clk})
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch16":
+        run_batch16(args)
+    elif args.workload == "stream_720p":
+        run_stream_720p(args)
+    elif args.workload == "serve_mix":
+        run_serve_mix(args)
     else:
         run_ours(args)
 

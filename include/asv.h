@@ -59,6 +59,9 @@ typedef struct asv_config {
     size_t hbm_budget;  /* bytes the context may allocate; 0 = unlimited */
     int use_graph;      /* 1: asv_run_lloyd replays a captured CUDA graph */
     int instrument;     /* 1: record per-stage CUDA-event times (asv_get_stats) */
+    int jfa_zrun;       /* JFA tile depth (voxels of a column per tile, walked along the
+                           step's chains); 0: chosen from the clip sizes; asv_autotune
+                           measures it */
 } asv_config;
 
 typedef struct asv_info {
@@ -144,6 +147,15 @@ asv_status asv_check_dead_seeds(asv_ctx *ctx, int32_t *labels_out);
  * final labels stay on the device (read them with asv_get_labels). */
 asv_status asv_run_lloyd(asv_ctx *ctx);
 
+/* No counterpart in the reference.  Times the whole Lloyd loop at JFA tile
+ * depths 4, 8, 16 and 32 (the voxels of a column one block walks along a
+ * step's chains: deeper shares more slice work, shallower fills the GPU
+ * better), keeps the fastest for this context (also for its later layouts)
+ * and returns it in *zrun (may be NULL).  Needs a context ready for
+ * asv_run_lloyd (clip or batch, not streaming); leaves the labels of a
+ * complete run, which do not depend on the depth. */
+asv_status asv_autotune(asv_ctx *ctx, int *zrun);
+
 /* Convenience: init_gpu + upload_flow + initialization + seed_matrix +
  * RGB2LAB + run_lloyd + labels, the plain per-clip form of Render::run. */
 asv_status asv_segment_clip(asv_ctx *ctx, const uint8_t *rgb, const float *fwd,
@@ -172,6 +184,24 @@ asv_status asv_get_stream(asv_ctx *ctx, void **stream);
 asv_status asv_synchronize(asv_ctx *ctx);
 /* bytes of device memory a clip of this size needs (admission control) */
 size_t asv_clip_bytes(int W, int H, int D, int K);
+
+/* ---- batched form -------------------------------------------------------- */
+
+/* No single counterpart in the reference, which runs clips one after the
+ * other (GPU-AS/main.cpp:74-83, one Render::run each).  Many clips of uneven
+ * size share one context: every stage is one launch over all of them (each
+ * JFA pass one persistent launch over the tiles of all clips; a clip with a
+ * shorter ladder sits out the extra passes), and asv_run_lloyd replays the
+ * whole loop as one CUDA graph.  Each clip's results equal its single-clip
+ * run.  After asv_batch_init and one asv_batch_upload per clip, call
+ * asv_initialization, asv_seed_matrix, asv_rgb2lab and asv_run_lloyd as for
+ * one clip. */
+asv_status asv_batch_init(asv_ctx *ctx, int n, const int *W, const int *H, const int *D, const int *K);
+asv_status asv_batch_upload(asv_ctx *ctx, int clip, const uint8_t *rgb, const float *fwd, const float *bwd);
+asv_status asv_batch_get_labels(asv_ctx *ctx, int clip, int32_t *out);
+asv_status asv_batch_get_info(asv_ctx *ctx, int clip, asv_info *info);
+/* bytes of device memory a batch needs (admission control) */
+size_t asv_batch_bytes(int n, const int *W, const int *H, const int *D, const int *K);
 
 /* ---- streaming form ---------------------------------------------------- */
 
@@ -210,6 +240,60 @@ asv_status asv_stream_info_get(asv_ctx *ctx, asv_stream_info *info);
  * [block_start, block_start + *done_frames), W*H*done_frames int32. */
 asv_status asv_stream_push(asv_ctx *ctx, const uint8_t *rgb, const float *fwd, const float *bwd,
                            int32_t *labels_out, int *done_frames);
+
+/* ---- serving ------------------------------------------------------------- */
+
+/* No counterpart in the reference (a desktop program that segments one clip
+ * at a time).  A request pool on one GPU: clip requests of any size are
+ * admitted as soon as a slot and enough of the HBM budget are free (first
+ * fit, so a small request can pass a large one that does not fit yet), each
+ * admitted request runs on its slot's own CUDA stream so that the work of
+ * several requests overlaps on the device, and a slot keeps its device layout
+ * and captured graph for the next request of the same shape.  Streaming
+ * sessions hold a resident streaming context (asv_stream_*) whose windows
+ * are processed in order.  Results are those of the single-clip / streaming
+ * calls, whatever else is running. */
+typedef struct asv_server asv_server;
+
+enum { ASV_REQ_CLIP = 0, ASV_REQ_WINDOW = 1 };
+
+typedef struct asv_request {
+    int kind;             /* ASV_REQ_CLIP or ASV_REQ_WINDOW */
+    int session;          /* window requests: the session id */
+    int W, H, D, K;       /* clip requests: sizes and requested seeds */
+    const uint8_t *rgb;   /* host inputs, valid until the request completes; for a window,
+                             the block's new frames (asv_stream_push) */
+    const float *fwd, *bwd;
+    int32_t *labels_out;  /* host output: clip labels (D*H*W) or the window's finished frames
+                             (room for W*H*(block_size + block_size/3) int32: the last
+                             block of a video can be that long) */
+} asv_request;
+
+typedef struct asv_server_stats {
+    long long submitted, completed, failed, queued, running;
+    size_t bytes_in_use, budget;
+    int slots, sessions;
+} asv_server_stats;
+
+/* max_slots: concurrent clip requests; hbm_budget: bytes all slots and
+ * sessions together may hold (0 = no limit).  cfg applies to every slot. */
+asv_status asv_server_create(const asv_config *cfg, int max_slots, size_t hbm_budget, asv_server **out);
+/* runs what is queued, then frees everything; no asv_server_wait may be in
+ * progress on another thread.  A clip request that cannot fit beside the
+ * open sessions even with every idle slot emptied fails with
+ * ASV_ERR_OVER_BUDGET. */
+asv_status asv_server_destroy(asv_server *srv);
+/* a streaming session (asv_stream_begin semantics); fails with
+ * ASV_ERR_OVER_BUDGET when its memory does not fit the budget */
+asv_status asv_server_open_session(asv_server *srv, int W, int H, int D_all, int K_video,
+                                   int seeds_num_100, int block_size, int *session);
+asv_status asv_server_submit(asv_server *srv, const asv_request *req, long long *id);
+/* blocks until request `id` completes; latency = submit -> completion (ms),
+ * queue_ms = submit -> start; done_frames for windows */
+asv_status asv_server_wait(asv_server *srv, long long id, double *latency_ms, double *queue_ms,
+                           int *done_frames);
+asv_status asv_server_poll(asv_server *srv, long long id, int *done);
+asv_status asv_server_get_stats(asv_server *srv, asv_server_stats *st);
 
 /* ---- post-processing without device allocation ------------------------- */
 

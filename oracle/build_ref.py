@@ -1,6 +1,7 @@
-"""Compiles the reference's own GLSL shaders as C++ (with the glm copy the
-reference vendors) into oracle/_ref/libref_shaders.so, the checker of the
-CPU restatement's shader maths.
+"""Compiles the reference's own GLSL shaders as C++ into
+oracle/_ref/libref_shaders.so, the checker of the CPU restatement's shader
+maths.  GLSL's vector types and swizzles come from a small header this
+project writes (not from a third-party math library).
 
 TEST INFRASTRUCTURE ONLY.  The shader files are read where they lie under
 the reference tree; the transformed C++ and the library go to oracle/_ref/
@@ -22,7 +23,6 @@ OUT = os.path.join(HERE, "_ref")
 LIB = os.path.join(OUT, "libref_shaders.so")
 REF = os.environ.get("ASV_REFERENCE_ROOT", "/root/reference")
 SHADERS = os.path.join(REF, "GPU-AS", "shaders")
-GLM = os.path.join(REF, "includes")
 
 PROGRAMS = {
     "rgb2lab": ["RGB2LAB.vs", "RGB2LAB.gs", "RGB2LAB.fs"],

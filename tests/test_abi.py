@@ -54,6 +54,22 @@ def test_create_reports_missing_device(asv):
     with pytest.raises(asv.AsvError) as e:
         asv.Image()
     assert e.value.status == 7
+    with pytest.raises(asv.AsvError) as e:
+        asv.Server(max_slots=2)
+    assert e.value.status == 7
+
+
+def test_batch_bytes_is_sum_of_clips(asv):
+    import ctypes
+    import numpy as np
+    lib = asv.load()
+    dims = [(64, 48, 12, 120), (40, 32, 9, 60), (96, 64, 16, 300)]
+    arr = [np.ascontiguousarray([d[i] for d in dims], np.int32) for i in range(4)]
+    ptr = [a.ctypes.data_as(ctypes.c_void_p) for a in arr]
+    total = lib.asv_batch_bytes(len(dims), *ptr)
+    parts = [lib.asv_clip_bytes(*d) for d in dims]
+    assert 0 < total <= sum(parts)
+    assert total >= sum(parts) - 2 * 32 * 256 * len(dims)
 
 
 def test_synth_deterministic_and_windowed(asv):
