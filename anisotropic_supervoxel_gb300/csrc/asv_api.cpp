@@ -370,6 +370,7 @@ asv_status asv_build_layout(asv_ctx *ctx)
     CK(cudaMemsetAsync(d.M, 0, sizeof(float) * 8 * seeds, ctx->st));
     asv_launch_srgb_table(d, ctx->st);
     CK(cudaGetLastError());
+    d.lablut = asv_lab_table(ctx->cfg.device);
     ctx->jfa_blocks = asv_jfa_grid_blocks(std::max(tiles, 1));
     return ASV_OK;
 }

@@ -94,11 +94,13 @@ struct AsvDev {
     int *rank;                   // per seed: relabel LUT / alive rank
     int *scan;                   // per chunk
     float *srgb;                 // 256-entry sRGB linearisation
+    const uchar4 *lablut;        // LAB of every RGB value (per device, shared), or null
     int *err;                    // device error word
 };
 
 void asv_launch_srgb_table(const AsvDev &d, cudaStream_t st);
 void asv_launch_rgb2lab(const AsvDev &d, cudaStream_t st);
+const uchar4 *asv_lab_table(int device);
 void asv_launch_density(const AsvDev &d, cudaStream_t st);
 void asv_launch_density_adjust(const AsvDev &d, cudaStream_t st);
 void asv_launch_first_init(const AsvDev &d, cudaStream_t st);

@@ -8,6 +8,8 @@
 
 #include <cuda_fp16.h>
 
+#include <mutex>
+
 #define FULL 0xffffffffu
 
 // ---------------------------------------------------------------------------
@@ -93,6 +95,35 @@ __global__ void __launch_bounds__(256) k_rgb2lab(AsvDev d)
         if (v >= n) break;
         const uint8_t *p = d.rgb + 3 * (S.vox_off + v);
         d.lab[S.vox_off + v] = asv_lab_of(tab, p[0], p[1], p[2]);
+    }
+}
+
+// The LAB bytes of all 2^24 RGB values, indexed r << 16 | g << 8 | b: built
+// once per device by asv_lab_of itself, so a lookup returns exactly what the
+// computation would (the exhaustive RGB2LAB test covers every entry).
+__global__ void __launch_bounds__(256) k_lab_table(const float *__restrict__ srgb, uchar4 *__restrict__ lut)
+{
+    __shared__ float tab[256];
+    tab[threadIdx.x] = srgb[threadIdx.x];
+    __syncthreads();
+    const unsigned c = blockIdx.x * 256u + threadIdx.x;              // 65536 blocks x 256
+    lut[c] = asv_lab_of(tab, c >> 16, (c >> 8) & 255u, c & 255u);
+}
+
+// RGB -> LAB through the table: one 4-byte gather per voxel
+__global__ void __launch_bounds__(256) k_rgb2lab_lut(AsvDev d)
+{
+    int si = asv_find_seg(d.chunk_prefix, d.nseg, blockIdx.x);
+    const SegDesc &S = d.segs[si];
+    long long base = (long long)(blockIdx.x - d.chunk_prefix[si]) * ASV_CHUNK;
+    long long n = S.nvox;
+    if (base + ASV_CHUNK <= S.lab_from) return;
+    const uchar4 *__restrict__ lut = d.lablut;
+    for (int i = 0; i < ASV_CHUNK / 256; i++) {
+        long long v = base + i * 256 + threadIdx.x;
+        if (v >= n) break;
+        const uint8_t *p = d.rgb + 3 * (S.vox_off + v);
+        d.lab[S.vox_off + v] = __ldg(lut + (((unsigned)p[0] << 16) | ((unsigned)p[1] << 8) | p[2]));
     }
 }
 
@@ -853,7 +884,43 @@ __global__ void __launch_bounds__(256) k_post_apply(AsvDev d)
 static inline int seed_blocks(const AsvDev &d) { return (d.total_seeds + 127) / 128; }
 
 void asv_launch_srgb_table(const AsvDev &d, cudaStream_t st) { k_srgb_table<<<1, 256, 0, st>>>(d.srgb); }
-void asv_launch_rgb2lab(const AsvDev &d, cudaStream_t st) { k_rgb2lab<<<d.total_chunks, 256, 0, st>>>(d); }
+void asv_launch_rgb2lab(const AsvDev &d, cudaStream_t st)
+{
+    if (d.lablut) k_rgb2lab_lut<<<d.total_chunks, 256, 0, st>>>(d);
+    else k_rgb2lab<<<d.total_chunks, 256, 0, st>>>(d);
+}
+
+// per-device LAB table (64 MiB), built on first use; nullptr when it cannot
+// be allocated (k_rgb2lab then computes every voxel)
+const uchar4 *asv_lab_table(int device)
+{
+    static std::mutex mu;
+    static uchar4 *tabs[64] = {};
+    static bool tried[64] = {};
+    if (device < 0 || device >= 64) return nullptr;
+    std::lock_guard<std::mutex> lk(mu);
+    if (tried[device]) return tabs[device];
+    tried[device] = true;
+    float *srgb = nullptr;
+    uchar4 *lut = nullptr;
+    cudaStream_t st = nullptr;
+    if (cudaMalloc(&srgb, 256 * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&lut, sizeof(uchar4) << 24) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        if (srgb) cudaFree(srgb);
+        if (lut) cudaFree(lut);
+        return nullptr;
+    }
+    k_srgb_table<<<1, 256, 0, st>>>(srgb);
+    k_lab_table<<<65536, 256, 0, st>>>(srgb, lut);
+    const bool ok = cudaStreamSynchronize(st) == cudaSuccess && cudaGetLastError() == cudaSuccess;
+    cudaStreamDestroy(st);
+    cudaFree(srgb);
+    if (!ok) { cudaFree(lut); return nullptr; }
+    tabs[device] = lut;
+    return lut;
+}
 void asv_launch_density(const AsvDev &d, cudaStream_t st) { k_density<<<d.total_chunks, 256, 0, st>>>(d); }
 void asv_launch_density_adjust(const AsvDev &d, cudaStream_t st)
 {

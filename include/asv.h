@@ -12,7 +12,10 @@
  *    message of the last failing call on a context.  No exception crosses
  *    the ABI.
  *  - The context owns all device memory.  Host buffers passed in or out stay
- *    owned by the caller and are not retained after the call returns.
+ *    owned by the caller and are not retained after the call returns.  The
+ *    one exception is a 64 MiB RGB->LAB table per device, built by the first
+ *    context that lays out a clip on that device, shared by all contexts,
+ *    kept until the process exits and not counted against hbm_budget.
  *  - A context runs on one CUDA stream (its own, or the one in the config)
  *    and is not thread-safe; distinct contexts are independent.
  *  - Volumes are x-fastest [D][H][W] in texture orientation (row y = 0 is
