@@ -432,7 +432,7 @@ static void do_next_seeds(asv_ctx *ctx)
     asv_launch_metric(ctx->d, 1, ctx->st);
     cudaMemsetAsync(ctx->d.labA, 0xff, sizeof(int32_t) * (size_t)ctx->d.total_chunks * ASV_CHUNK, ctx->st);
     asv_launch_draw(ctx->d, ctx->st);
-    ctx->launches += 4;
+    ctx->launches += 6;       // five metric kernels + the seed draw
 }
 
 static void do_post(asv_ctx *ctx)

@@ -8,14 +8,17 @@
 // least-squares solution in FP32 like the reference's Eigen float solve
 // (one-sided Jacobi SVD, rank rule of Eigen's SVD solve: keep
 // sigma >= max(sigma_max * min(rows,6) * FLT_EPSILON, FLT_MIN)); the 3x3
-// PSD test and the nearest-PSD projection run in FP64.  A non-PSD M falls back to the mean of the PSD metrics of the
-// 1-ring, then 2-ring neighbours, then to the nearest PSD matrix.
+// PSD test is exact (principal minors, error-free FP64 expansion) and the
+// nearest-PSD projection runs in FP64.  A non-PSD M falls back to the mean of
+// the PSD metrics of the 1-ring, then 2-ring neighbours, then to the nearest
+// PSD matrix.
 //
 // One warp per solve: lane i holds row i of the system; column dot products
 // are accumulated row by row in order (shuffles), so every lane computes the
 // same scalars with the same operation sequence as a sequential solver.
-// Launches: k_metric_self (a warp per seed), k_metric_ring (a warp per seed
-// and neighbour, only for non-PSD seeds), k_metric_combine (a thread per
+// Launches: k_metric_self (a warp per seed), k_metric_psd (a thread per
+// solve: the FP64 PSD tests), k_metric_ring (a warp per seed and neighbour,
+// only for non-PSD seeds), k_metric_psd again, k_metric_combine (a thread per
 // seed).  A reseed solve is skipped when the seed's voxel is the one of its
 // previous reseed solve in this Lloyd run: the metric is a function of that
 // voxel and the flow only, so the stored result is the solve's result.
@@ -27,11 +30,18 @@
 #define SVD_SWEEPS 30
 #define FULL 0xffffffffu
 
-// sequential sum over rows 0..m-1 of a per-lane value
-__device__ __forceinline__ float asv_row_sum(float v, int m)
+#define ASV_MAX_ROWS 18      // 9 neighbours x (forward, backward)
+
+// Sequential sum over rows 0..m-1 of a per-lane value.  Lanes at or beyond
+// m hold +0 (their rows are zero), and adding +0 leaves any sum that is not
+// -0 unchanged; these sums start at +0 and, in round-to-nearest, never reach
+// -0.  So the loop always runs ASV_MAX_ROWS rows, fully unrolled: every
+// shuffle is issued up front and only the additions form a chain.
+__device__ __forceinline__ float asv_row_sum(float v)
 {
     float a = 0.0f;
-    for (int i = 0; i < m; i++) a = a + __shfl_sync(FULL, v, i);
+#pragma unroll
+    for (int i = 0; i < ASV_MAX_ROWS; i++) a = a + __shfl_sync(FULL, v, i);
     return a;
 }
 
@@ -51,7 +61,8 @@ __device__ void asv_lsq_minnorm_warp(int m, float u[6], float bl, float x[6])
             for (int q = p + 1; q < 6; q++) {
                 const float pa = u[p] * u[p], pb = u[q] * u[q], pg = u[p] * u[q];
                 float al = 0.0f, be = 0.0f, ga = 0.0f;
-                for (int i = 0; i < m; i++) {
+#pragma unroll
+                for (int i = 0; i < ASV_MAX_ROWS; i++) {      // rows >= m add +0 (asv_row_sum)
                     al = al + __shfl_sync(FULL, pa, i);
                     be = be + __shfl_sync(FULL, pb, i);
                     ga = ga + __shfl_sync(FULL, pg, i);
@@ -76,7 +87,7 @@ __device__ void asv_lsq_minnorm_warp(int m, float u[6], float bl, float x[6])
     float sig[6], smax = 0.0f;
 #pragma unroll
     for (int j = 0; j < 6; j++) {
-        sig[j] = sqrtf(asv_row_sum(u[j] * u[j], m));
+        sig[j] = sqrtf(asv_row_sum(u[j] * u[j]));
         if (sig[j] > smax) smax = sig[j];
     }
     float thr = smax * ((float)(m < 6 ? m : 6) * FLT_EPSILON);
@@ -85,7 +96,7 @@ __device__ void asv_lsq_minnorm_warp(int m, float u[6], float bl, float x[6])
 #pragma unroll
     for (int j = 0; j < 6; j++) {
         if (!(sig[j] >= thr)) continue;
-        float ub = asv_row_sum(u[j] * bl, m);
+        float ub = asv_row_sum(u[j] * bl);
         float coef = (ub / sig[j]) / sig[j];
         xr = xr + v[j] * coef;
     }
@@ -133,11 +144,55 @@ __device__ void asv_sym3_eig(const float M[6], double w[3], double V[3][3])
     for (int k = 0; k < 3; k++) w[k] = a[k][k];
 }
 
+// error-free transformations (Knuth's TwoSum, the FMA TwoProduct)
+__device__ __forceinline__ void asv_two_sum(double a, double b, double &s, double &e)
+{
+    s = a + b;
+    const double bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+__device__ __forceinline__ void asv_two_prod(double a, double b, double &p, double &e)
+{
+    p = a * b;
+    e = fma(a, b, -p);
+}
+
+// Exact "some eigenvalue is negative" test of the symmetric 3x3 matrix M
+// (GPU-AS/Image.cpp:997-1006 asks eigenvalues() for a real part < 0): a
+// symmetric matrix has no negative eigenvalue iff all its principal minors
+// are >= 0.  Products of two floats are exact in double; the determinant's
+// five triple products are split into exact (hi, lo) pairs and summed as a
+// nonoverlapping expansion (Shewchuk's Grow-Expansion), whose last non-zero
+// component carries the exact sign.  Entries that are not finite count as
+// no negative eigenvalue.
 __device__ int asv_m6_negative(const float M[6])
 {
-    double w[3], V[3][3];
-    asv_sym3_eig(M, w, V);
-    return (w[0] < 0.0 || w[1] < 0.0 || w[2] < 0.0) ? 1 : 0;
+    const double a = M[0], b = M[1], c = M[2], d = M[3], e = M[4], f = M[5];
+    if (!(isfinite(a) && isfinite(b) && isfinite(c) && isfinite(d) && isfinite(e) && isfinite(f)))
+        return 0;
+    if (a < 0.0 || d < 0.0 || f < 0.0) return 1;
+    if (a * d < b * b || a * f < c * c || d * f < e * e) return 1;
+    double t[10];
+    asv_two_prod(a * d, f, t[0], t[1]);                 // a d f
+    asv_two_prod(2.0 * (b * c), e, t[2], t[3]);         // 2 b c e
+    asv_two_prod(-(a * e), e, t[4], t[5]);              // - a e e
+    asv_two_prod(-(d * c), c, t[6], t[7]);              // - d c c
+    asv_two_prod(-(f * b), b, t[8], t[9]);              // - f b b
+    double x[10];
+    int n = 0;
+    for (int k = 0; k < 10; k++) {                      // Grow-Expansion
+        double q = t[k];
+        for (int i = 0; i < n; i++) {
+            double h;
+            asv_two_sum(q, x[i], q, h);
+            x[i] = h;
+        }
+        x[n++] = q;
+    }
+    for (int i = n - 1; i >= 0; i--)
+        if (x[i] != 0.0) return x[i] < 0.0 ? 1 : 0;
+    return 0;
 }
 
 __device__ void asv_m6_nearest_psd(const float M[6], float out[6])
@@ -157,11 +212,11 @@ __device__ void asv_m6_nearest_psd(const float M[6], float out[6])
 
 __device__ __forceinline__ float asv_round_half_up(float f) { return (float)floor((double)f + 0.5); }
 
-// matrix_slover (GPU-AS/Image.cpp:874-1009) for one warp; returns the
-// non-PSD flag; M valid on every lane.  Rows are numbered in the
+// matrix_slover (GPU-AS/Image.cpp:874-1009) for one warp; M valid on every
+// lane (its PSD test, :997-1006, is k_metric_psd).  Rows are numbered in the
 // reference's order (neighbour y outer, x inner; forward row, then backward).
-__device__ int asv_metric_solve_warp(const float2 *__restrict__ fwd, const float2 *__restrict__ bwd,
-                                     int W, int H, int D, float sx, float sy, int frame, float M[6])
+__device__ void asv_metric_solve_warp(const float2 *__restrict__ fwd, const float2 *__restrict__ bwd,
+                                      int W, int H, int D, float sx, float sy, int frame, float M[6])
 {
     const int lane = threadIdx.x & 31;
     const float expected_b[9] = { 3, 2, 3, 2, 1, 2, 3, 2, 3 };
@@ -204,7 +259,6 @@ __device__ int asv_metric_solve_warp(const float2 *__restrict__ fwd, const float
         asv_lsq_minnorm_warp(m, u, bl, x);
     }
     for (int k = 0; k < 6; k++) M[k] = x[k];
-    return asv_m6_negative(M);
 }
 
 // plain reseed flow-angle filter (GPU-AS/Image.cpp:1406-1409): accept iff
@@ -253,8 +307,9 @@ __device__ __forceinline__ int asv_seed_key(const SegDesc &S, float4 p)
     return (frame * S.H + y) * S.W + x;
 }
 
-// neg[g]: 0 = PSD, 1 = non-PSD (fallbacks run), 2 = memo hit (reseed only)
-// which seed positions: reseed 0 -> pos0 (seed_matrix), 1 -> pos (reseed)
+// neg[g]: 0 = PSD, 1 = non-PSD (fallbacks run), 2 = memo hit (reseed only),
+// 3 = solved, PSD test pending (k_metric_psd).  Which seed positions:
+// reseed 0 -> pos0 (seed_matrix), 1 -> pos (reseed).
 __global__ void __launch_bounds__(128) k_metric_self(AsvDev d, int reseed)
 {
     const int lane = threadIdx.x & 31;
@@ -269,10 +324,27 @@ __global__ void __launch_bounds__(128) k_metric_self(AsvDev d, int reseed)
     float fx = floorf(p.x), fy = floorf(p.y);
     int frame = min(max((int)p.z, 0), S.D - 1);   // positions are inside; keep reads in bounds
     float M[6];
-    int neg = asv_metric_solve_warp(d.fwd + S.vox_off, d.bwd + S.vox_off, S.W, S.H, S.D, fx, fy,
-                                    frame, M);
+    asv_metric_solve_warp(d.fwd + S.vox_off, d.bwd + S.vox_off, S.W, S.H, S.D, fx, fy, frame, M);
     if (lane < 6) d.Mself[8 * r.g + lane] = M[lane];
-    if (lane == 0) d.neg[r.g] = neg;
+    if (lane == 0) d.neg[r.g] = 3;
+}
+
+// The FP64 PSD tests of the solves, one thread per solve: the warp solves
+// leave them pending so that each 3x3 eigen-decomposition runs on one lane
+// of a full warp instead of on all 32 lanes of the solving warp (GB300's FP64
+// pipe is narrow).  flag 3 (self) / 2 (ring) marks a pending test.
+__global__ void k_metric_psd(AsvDev d)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long nself = d.total_seeds;
+    SeedRef r;
+    if (t < nself) {
+        if (asv_seed_ref(d, (int)t, r) && d.neg[t] == 3) d.neg[t] = asv_m6_negative(d.Mself + 8 * t);
+        return;
+    }
+    const long long k = t - nself;                       // ring task: seed * ASV_RING + neighbour
+    if (k >= nself * ASV_RING || !asv_seed_ref(d, (int)(k / ASV_RING), r)) return;
+    if (d.ringok[k] == 2) d.ringok[k] = asv_m6_negative(d.Mring + 8 * k) ? 0 : 1;
 }
 
 __global__ void __launch_bounds__(128) k_metric_ring(AsvDev d, int reseed)
@@ -297,10 +369,10 @@ __global__ void __launch_bounds__(128) k_metric_ring(AsvDev d, int reseed)
         return;
     }
     float M[6];
-    int neg = asv_metric_solve_warp(fwd, bwd, S.W, S.H, S.D, nx, ny, frame, M);
+    asv_metric_solve_warp(fwd, bwd, S.W, S.H, S.D, nx, ny, frame, M);
     float *dst = d.Mring + 8 * (ASV_RING * g + t);
     if (lane < 6) dst[lane] = M[lane];
-    if (lane == 0) *ok = neg ? 0 : 1;
+    if (lane == 0) *ok = 2;                              // PSD test pending (k_metric_psd)
 }
 
 // writes M0 (reseed 0) or M (reseed 1, and the memo)
@@ -351,6 +423,8 @@ void asv_launch_metric(const AsvDev &d, int reseed, cudaStream_t st)
     long long warps = d.total_seeds;
     k_metric_self<<<(int)((warps * 32 + 127) / 128), 128, 0, st>>>(d, reseed);
     long long rw = (long long)d.total_seeds * ASV_RING;
+    k_metric_psd<<<(int)((warps + 127) / 128), 128, 0, st>>>(d);     // self tests
     k_metric_ring<<<(int)((rw * 32 + 127) / 128), 128, 0, st>>>(d, reseed);
+    k_metric_psd<<<(int)((warps + rw + 127) / 128), 128, 0, st>>>(d); // ring tests
     k_metric_combine<<<(d.total_seeds + 63) / 64, 64, 0, st>>>(d, reseed);
 }

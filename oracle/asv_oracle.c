@@ -401,14 +401,56 @@ static void m6_to_3(const float M[6], double A[3][3])
     A[2][0] = M[2]; A[2][1] = M[4]; A[2][2] = M[5];
 }
 
-/* any eigenvalue < 0: Image.cpp:997-1006 */
+/* Knuth's TwoSum and the FMA TwoProduct: exact error terms */
+static void two_sum(double a, double b, double *s, double *e)
+{
+    *s = a + b;
+    double bb = *s - a;
+    *e = (a - (*s - bb)) + (b - bb);
+}
+
+static void two_prod(double a, double b, double *p, double *e)
+{
+    *p = a * b;
+    *e = fma(a, b, -*p);
+}
+
+/* Any eigenvalue < 0 (Image.cpp:997-1006), decided exactly: a symmetric
+ * matrix is PSD iff every principal minor is >= 0.  Float products of two
+ * are exact in double; the determinant is the exact sum of five triple
+ * products, each split into an exact (hi, lo) pair, accumulated as a
+ * nonoverlapping expansion (Shewchuk, "Adaptive precision floating-point
+ * arithmetic", Grow-Expansion); its most significant non-zero component has
+ * the sign of the sum.  Non-finite entries count as no negative eigenvalue. */
 static int m6_negative(const float M[6])
 {
-    double A[3][3], w[3], V[3][3];
-    m6_to_3(M, A);
-    sym3_eig(A, w, V);
-    return (w[0] < 0.0 || w[1] < 0.0 || w[2] < 0.0) ? 1 : 0;
+    const double a = M[0], b = M[1], c = M[2], d = M[3], e = M[4], f = M[5];
+    if (!(isfinite(a) && isfinite(b) && isfinite(c) && isfinite(d) && isfinite(e) && isfinite(f)))
+        return 0;
+    if (a < 0.0 || d < 0.0 || f < 0.0) return 1;
+    if (a * d < b * b || a * f < c * c || d * f < e * e) return 1;
+    double t[10], x[10];
+    two_prod(a * d, f, &t[0], &t[1]);
+    two_prod(2.0 * (b * c), e, &t[2], &t[3]);
+    two_prod(-(a * e), e, &t[4], &t[5]);
+    two_prod(-(d * c), c, &t[6], &t[7]);
+    two_prod(-(f * b), b, &t[8], &t[9]);
+    int n = 0;
+    for (int k = 0; k < 10; k++) {
+        double q = t[k];
+        for (int i = 0; i < n; i++) {
+            double h;
+            two_sum(q, x[i], &q, &h);
+            x[i] = h;
+        }
+        x[n++] = q;
+    }
+    for (int i = n - 1; i >= 0; i--)
+        if (x[i] != 0.0) return x[i] < 0.0 ? 1 : 0;
+    return 0;
 }
+
+int orc_m6_negative(const float M[6]) { return m6_negative(M); }
 
 /* nearest PSD by clipping negative eigenvalues: Image.cpp:786-835 */
 static void m6_nearest_psd(const float M[6], float out[6])
@@ -765,6 +807,72 @@ int orc_postprocess(int W, int H, int D, int Kp, const int64_t *sums, int32_t *l
     }
     free(dead_ids); free(rank);
     return dead;
+}
+
+/* ====================================================================
+ * 3D connectivity enforcement: Image::EnforceLabelConnectivity3D
+ * (GPU-AS/Image.cpp:1938-2063; the same loop is streamGPU-AS/Render.cpp:
+ * 572-695 label_connected3D over a whole video).  Voxels are visited in
+ * raster order; an unvisited voxel starts a new segment: first the label
+ * `adj` is taken from the last already-labelled voxel among its 24
+ * neighbours (slices z-1, z, z+1 x the 8 in-plane offsets; the voxel
+ * straight above or below is not a neighbour), in the loop order dz
+ * -1, 0, 1 and offsets (-1,0) (-1,-1) (0,-1) (1,-1) (1,0) (1,1) (0,1)
+ * (-1,1); `adj` keeps its previous value when none is labelled (0 at the
+ * start).  The segment grows over unvisited neighbours with the seed's input
+ * label; a segment of fewer than supsz / 4 voxels takes `adj` and does not
+ * consume a new label.  Returns the number of labels.
+ * ==================================================================== */
+int orc_enforce_connectivity(const int32_t *labels, int W, int H, int D, int supsz, int32_t *out)
+{
+    static const int dx8[8] = { -1, -1, 0, 1, 1, 1, 0, -1 };
+    static const int dy8[8] = { 0, -1, -1, -1, 0, 1, 1, 1 };
+    const long n = (long)W * H * D, sl = (long)W * H;
+    long *q = (long *)malloc(sizeof(long) * (size_t)(n > 0 ? n : 1));
+    if (!q) return -1;
+    for (long i = 0; i < n; i++) out[i] = -1;
+    int label = 0, adj = 0;
+    for (long s = 0; s < n; s++) {
+        if (out[s] >= 0) continue;
+        const int sx = (int)(s % W), sy = (int)((s / W) % H), sz = (int)(s / sl);
+        out[s] = label;
+        for (int dz = -1; dz <= 1; dz++) {                           /* :1980-1999 */
+            int z = sz + dz;
+            if (z < 0 || z >= D) continue;
+            for (int k = 0; k < 8; k++) {
+                int x = sx + dx8[k], y = sy + dy8[k];
+                if (x < 0 || x >= W || y < 0 || y >= H) continue;
+                long v = z * sl + (long)y * W + x;
+                if (out[v] >= 0) adj = out[v];
+            }
+        }
+        long head = 0, tail = 0;                                      /* :2001-2037 */
+        q[tail++] = s;
+        while (head < tail) {
+            long c = q[head++];
+            const int cx = (int)(c % W), cy = (int)((c / W) % H), cz = (int)(c / sl);
+            for (int dz = -1; dz <= 1; dz++) {
+                int z = cz + dz;
+                if (z < 0 || z >= D) continue;
+                for (int k = 0; k < 8; k++) {
+                    int x = cx + dx8[k], y = cy + dy8[k];
+                    if (x < 0 || x >= W || y < 0 || y >= H) continue;
+                    long v = z * sl + (long)y * W + x;
+                    if (out[v] < 0 && labels[v] == labels[s]) {
+                        out[v] = label;
+                        q[tail++] = v;
+                    }
+                }
+            }
+        }
+        if (tail < supsz / 4) {                                       /* :2042-2050 */
+            for (long i = 0; i < tail; i++) out[q[i]] = adj;
+            label--;
+        }
+        label++;
+    }
+    free(q);
+    return label;
 }
 
 /* final centroids of alive seeds (streamGPU-AS/Image.cpp:1563-1582) */

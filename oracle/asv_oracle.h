@@ -60,6 +60,7 @@ void orc_grid_cell_tables(int W, int H, int D, const float *grid4, const orc_gri
                           int *xcell, int *ycell, int *zcell);
 int  orc_density_adjust(const uint8_t *rgb, int W, int H, int D, const float *grid4,
                         const orc_grid_info *g, float *seeds4_out, float *density_out);
+int  orc_m6_negative(const float M[6]);   /* exact "an eigenvalue < 0" of (M00,M01,M02,M11,M12,M22) */
 int  orc_metric_solve(const float *fwd, const float *bwd, int W, int H, int D,
                       float sx, float sy, int frame, float M[6]);
 void orc_seed_metrics(const float *fwd, const float *bwd, int W, int H, int D, int Kp,
@@ -75,6 +76,7 @@ void orc_centroid_sums(int W, int H, int D, int Kp, const int32_t *labels, const
 void orc_finalize(int W, int H, int D, int Kp, const int64_t *sums, const uint8_t *lab4,
                   float *pos3, float *slab3);
 int  orc_postprocess(int W, int H, int D, int Kp, const int64_t *sums, int32_t *labels, int *stats);
+int  orc_enforce_connectivity(const int32_t *labels, int W, int H, int D, int supsz, int32_t *out);
 void orc_final_centroids(int Kp, const int64_t *sums, float *seeds4_out, int *nalive);
 
 /* ---- whole plain per-clip run (GPU-AS/Render.cpp:254-303) ----------- */

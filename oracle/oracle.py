@@ -106,6 +106,23 @@ def gradient_half(rgb):
     return out
 
 
+def m6_negative(M):
+    """exact test: the symmetric matrix (M00,M01,M02,M11,M12,M22) has an eigenvalue < 0"""
+    M = np.ascontiguousarray(M, np.float32)
+    return int(load().orc_m6_negative(_p(M)))
+
+
+def enforce_connectivity(labels, supsz):
+    """Image::EnforceLabelConnectivity3D restated; returns (labels, number of labels)."""
+    labels = np.ascontiguousarray(labels, np.int32)
+    D, H, W = labels.shape
+    out = np.empty_like(labels)
+    n = load().orc_enforce_connectivity(_p(labels), W, H, D, int(supsz), _p(out))
+    if n < 0:
+        raise MemoryError("oracle connectivity: allocation failed")
+    return out, int(n)
+
+
 def metric_solve(fwd, bwd, sx, sy, frame):
     D, H, W, _ = fwd.shape
     M = np.zeros(6, np.float32)

@@ -304,3 +304,36 @@ def test_lloyd_uniform_colour_fixed_point(orc, asv):
     sums = orc.centroid_sums(raw, lab4, info["Kp"])
     cen = np.floor((sums[:-1, :3] / 2.0) / sums[:-1, 3:4]) + 0.5
     assert np.abs(cen - seeds[:, :3]).max() <= 1.0
+
+
+def _negative_exact(M):
+    """some eigenvalue < 0, in exact rational arithmetic (principal minors)"""
+    from fractions import Fraction as F
+    a, b, c, d, e, f = (F(float(v)) for v in M)
+    minors = [a, d, f, a * d - b * b, a * f - c * c, d * f - e * e,
+              a * (d * f - e * e) - b * (b * f - c * e) + c * (b * e - d * c)]
+    return int(any(m < 0 for m in minors))
+
+
+def test_psd_test_is_exact(orc):
+    """The metric's PSD test (Image.cpp:997-1006, decided exactly) against
+    rational arithmetic: random, rank-deficient, exactly singular and
+    near-singular symmetric matrices."""
+    rng = np.random.default_rng(17)
+    cases = []
+    for _ in range(3000):
+        cases.append(rng.normal(size=6).astype(np.float32))
+    for _ in range(1500):                      # S^T S of 1 or 2 rows: PSD, rank 1/2
+        S = rng.normal(size=(int(rng.integers(1, 3)), 3)).astype(np.float32)
+        A = (S.T.astype(np.float64) @ S.astype(np.float64)).astype(np.float32)
+        cases.append(np.array([A[0, 0], A[0, 1], A[0, 2], A[1, 1], A[1, 2], A[2, 2]], np.float32))
+    for _ in range(1500):                      # integer matrices: many exactly singular
+        v = rng.integers(-3, 4, size=3).astype(np.float32)
+        w = rng.integers(-3, 4, size=3).astype(np.float32)
+        A = np.outer(v, v) + (rng.integers(0, 2) * np.outer(w, w))
+        cases.append(np.array([A[0, 0], A[0, 1], A[0, 2], A[1, 1], A[1, 2], A[2, 2]], np.float32))
+    cases += [np.zeros(6, np.float32), np.array([1, 1, 0, 1, 0, 0], np.float32),
+              np.array([1, 0, 0, 1, 0, -1e-30], np.float32), np.array([1e-20, 1e-10, 0, 1, 0, 1], np.float32),
+              np.array([3e38, 1e38, 0, 3e38, 0, 1e-38], np.float32)]
+    for M in cases:
+        assert orc.m6_negative(M) == _negative_exact(M), M.tolist()
