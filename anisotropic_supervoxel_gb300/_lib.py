@@ -89,6 +89,9 @@ SIGNATURES = {
     "asv_ld_next_seeds_matrix": (c_int, [c_void_p, c_int]),
     "asv_check_dead_seeds": (c_int, [c_void_p, c_void_p]),
     "asv_run_lloyd": (c_int, [c_void_p]),
+    "asv_enforce_connectivity": (c_int, [c_void_p, c_int, c_void_p, P(c_int)]),
+    "asv_enforce_connectivity_labels": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p,
+                                                P(c_int)]),
     "asv_autotune": (c_int, [c_void_p, P(c_int)]),
     "asv_segment_clip": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_int,
                                  c_int, c_void_p]),

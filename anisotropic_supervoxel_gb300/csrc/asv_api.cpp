@@ -6,6 +6,7 @@
 #include "asv.h"
 #include "asv_common.cuh"
 #include "asv_internal.h"
+#include "asv_connect.cuh"
 #include "asv_stream.cuh"
 
 #include <cuda_runtime.h>
@@ -167,9 +168,12 @@ struct asv_ctx {
         StreamDev s{};
         int placed = 0, kept = 0, last_Kp = 0;
     } sm;
+    // connectivity enforcement scratch (asv_enforce_connectivity*), grown on demand
+    void *cc = nullptr;
+    size_t cc_bytes = 0;
 };
 
-size_t asv::ctx_bytes(const asv_ctx *c) { return c ? c->bytes : 0; }
+size_t asv::ctx_bytes(const asv_ctx *c) { return c ? c->bytes + c->cc_bytes : 0; }
 
 static asv_status fail(asv_ctx *c, asv_status s, const std::string &m)
 {
@@ -539,6 +543,7 @@ asv_status asv_destroy(asv_ctx *ctx)
     cudaSetDevice(ctx->cfg.device);
     cudaStreamSynchronize(ctx->st);
     free_layout(ctx);
+    if (ctx->cc) cudaFree(ctx->cc);
     for (auto e : ctx->ev) cudaEventDestroy(e);
     if (ctx->own_st) cudaStreamDestroy(ctx->st);
     delete ctx;
@@ -804,6 +809,81 @@ asv_status asv_autotune(asv_ctx *ctx, int *zrun_out)
     ctx->seeded = ctx->ran = true;
     if (zrun_out) *zrun_out = best;
     return ASV_OK;
+}
+
+// Connectivity enforcement: the context's scratch holds the output volume,
+// an input volume (caller labels) and the union-find arrays; it is grown on
+// demand and kept until the context is destroyed.
+static asv_status connect_scratch(asv_ctx *ctx, long long n, int32_t **out, int32_t **in, void **cc)
+{
+    const size_t vol = ((size_t)n * 4 + 255) & ~(size_t)255;
+    const size_t need = 2 * vol + asv_connect_scratch_bytes(n);
+    if (ctx->cc_bytes < need) {
+        if (ctx->cfg.hbm_budget && ctx->bytes + need > ctx->cfg.hbm_budget)
+            return fail(ctx, ASV_ERR_OVER_BUDGET, "connectivity scratch exceeds the configured HBM budget");
+        if (ctx->cc) { cudaFree(ctx->cc); ctx->cc = nullptr; ctx->cc_bytes = 0; }
+        cudaError_t e = cudaMalloc(&ctx->cc, need);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            ctx->cc = nullptr;
+            return fail(ctx, ASV_ERR_OOM, "cudaMalloc: connectivity scratch");
+        }
+        ctx->cc_bytes = need;
+    }
+    *out = (int32_t *)ctx->cc;
+    *in = (int32_t *)((unsigned char *)ctx->cc + vol);
+    *cc = (unsigned char *)ctx->cc + 2 * vol;
+    return ASV_OK;
+}
+
+static asv_status run_connect(asv_ctx *ctx, const int32_t *lab, int32_t *out, void *cc, int W, int H, int D,
+                              int supsz, int32_t *labels_out, int *label_num)
+{
+    const long long n = (long long)W * H * D;
+    int R = 0, num = 0;
+    const int rc = asv_launch_connect(lab, W, H, D, supsz, out, cc, ctx->st, &R, &num);
+    if (rc == -2) return fail(ctx, ASV_ERR_TIMEOUT, "connectivity: union-find retry bound exceeded");
+    if (rc == -3) return fail(ctx, ASV_ERR_BAD_ARG, "connectivity: more than 2^30 segments");
+    if (rc != 0) return cuda_fail(ctx, cudaGetLastError(), "connectivity kernels");
+    if (labels_out) {
+        CK(cudaMemcpyAsync(labels_out, out, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+    }
+    if (label_num) *label_num = num;
+    return ASV_OK;
+}
+
+asv_status asv_enforce_connectivity(asv_ctx *ctx, int supsz, int32_t *labels_out, int *label_num)
+{
+    if (!ctx) return ASV_ERR_BAD_ARG;
+    if (ctx->sm.on || ctx->seg.size() != 1) return fail(ctx, ASV_ERR_STATE, "connectivity needs a context holding one clip");
+    if (!ctx->ran) return fail(ctx, ASV_ERR_STATE, "no labels: run the Lloyd loop first");
+    cudaSetDevice(ctx->cfg.device);
+    const SegDesc &s = ctx->sd[0];
+    const SegHost &h = ctx->seg[0];
+    if (supsz <= 0) supsz = (int)(s.nvox / std::max(h.K, 1));          // texel_num / seeds_num
+    int32_t *out, *in;
+    void *cc;
+    asv_status st = connect_scratch(ctx, s.nvox, &out, &in, &cc);
+    if (st != ASV_OK) return st;
+    const int32_t *raw = (s.final_buf == 1 ? ctx->d.labB : ctx->d.labA) + s.vox_off;
+    return run_connect(ctx, raw, out, cc, s.W, s.H, s.D, supsz, labels_out, label_num);
+}
+
+asv_status asv_enforce_connectivity_labels(asv_ctx *ctx, const int32_t *labels, int W, int H, int D,
+                                           int supsz, int32_t *labels_out, int *label_num)
+{
+    if (!ctx) return ASV_ERR_BAD_ARG;
+    if (!labels || W < 1 || H < 1 || D < 1 || supsz < 1 || (long long)W * H * D >= (1LL << 31))
+        return fail(ctx, ASV_ERR_BAD_ARG, "need labels, W,H,D >= 1 with W*H*D < 2^31 and supsz >= 1");
+    cudaSetDevice(ctx->cfg.device);
+    const long long n = (long long)W * H * D;
+    int32_t *out, *in;
+    void *cc;
+    asv_status st = connect_scratch(ctx, n, &out, &in, &cc);
+    if (st != ASV_OK) return st;
+    CK(cudaMemcpyAsync(in, labels, sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice, ctx->st));
+    return run_connect(ctx, in, out, cc, W, H, D, supsz, labels_out, label_num);
 }
 
 asv_status asv_segment_clip(asv_ctx *ctx, const uint8_t *rgb, const float *fwd, const float *bwd,

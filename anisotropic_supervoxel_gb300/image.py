@@ -118,6 +118,25 @@ class Image:
     def run_lloyd(self):
         self._ck(self.lib.asv_run_lloyd(self.h))
 
+    def enforce_connectivity(self, supsz=0):
+        """Image::enforce_connectivity_3d on the last JFA labels; returns
+        (labels, number of labels).  supsz 0: W*H*D / K."""
+        out = np.empty(self.shape, np.int32)
+        n = ctypes.c_int()
+        self._ck(self.lib.asv_enforce_connectivity(self.h, supsz, _ptr(out), ctypes.byref(n)))
+        return out, n.value
+
+    def enforce_connectivity_labels(self, labels, supsz):
+        """Render::label_connected3D / EnforceLabelConnectivity3D on a label
+        volume [D,H,W]; returns (labels, number of labels)."""
+        labels = np.ascontiguousarray(labels, np.int32)
+        D, H, W = labels.shape
+        out = np.empty_like(labels)
+        n = ctypes.c_int()
+        self._ck(self.lib.asv_enforce_connectivity_labels(self.h, _ptr(labels), W, H, D, int(supsz), _ptr(out),
+                                                          ctypes.byref(n)))
+        return out, n.value
+
     def autotune(self):
         """asv_autotune: times the Lloyd loop at JFA tile depths 4..32, keeps the
         fastest; returns it."""

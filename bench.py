@@ -45,7 +45,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="clip_320x240x85",
                     choices=["clip_320x240x85", "clip_240x160x30", "batch16", "stream_720p",
-                             "serve_mix"])
+                             "serve_mix", "connect_320x240x85"])
     ap.add_argument("--requests", type=int, default=160, help="serve_mix: requests in the run")
     ap.add_argument("--rate", type=float, default=40.0, help="serve_mix: mean arrivals per second")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -609,6 +609,50 @@ def run_serve_mix(args):
            "clocks": clk})
 
 
+def run_connect(args):
+    """3D connectivity enforcement (Image::enforce_connectivity_3d) on the raw
+    labels of the 320x240x85 clip after its Lloyd loop; step = one
+    asv_enforce_connectivity on the device labels (labels back to the host
+    included).  CPU baseline: the oracle's restatement of the reference's
+    sequential scan (pinned to the reference's C++) on the same labels."""
+    import numpy as np
+    import torch
+
+    import anisotropic_supervoxel_gb300 as asv
+    from anisotropic_supervoxel_gb300 import workloads
+    torch.cuda.set_device(0)
+    w = workloads.CLIP_320x240x85
+    rgb, fwd, bwd = workloads.make_clip(w)
+    D, H, W, _ = rgb.shape
+    n = W * H * D
+    img = asv.Image(lloyd_iters=w["iters"])
+    img.segment(rgb, fwd, bwd, w["K"])
+    raw = img.raw_labels()
+    supsz = n // w["K"]
+    for _ in range(args.warmup):
+        got, num = img.enforce_connectivity()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        got, num = img.enforce_connectivity()
+    dt = (time.perf_counter() - t0) / args.steps
+    from oracle import oracle
+    t1 = time.perf_counter()
+    want, m = oracle.enforce_connectivity(raw, supsz)
+    cpu_dt = time.perf_counter() - t1
+    img.close()
+    _line(args, n / dt / 1e6, dt * 1e3,
+          {"workload": "connect_320x240x85", "supsz": supsz, "parallelism": "replicas1",
+           "l2": "labels (26 MB) and scratch (200 MB) exceed the working set of one pass"},
+          {"metric": "Mvoxel/s of 3D connectivity enforcement", "unit": "Mvoxel/s", "dtype": "int32",
+           "labels_equal_oracle": bool(np.array_equal(got, want)) and num == m, "label_num": num,
+           "cpu_baseline": {"value": n / cpu_dt / 1e6, "unit": "Mvoxel/s", "cores": 1, "kind": "port",
+                            "sample": f"the same {W}x{H}x{D} labels, the oracle's sequential scan, "
+                                      f"{cpu_dt:.2f} s"},
+           "e2e": {"value": n / dt / 1e6, "unit": "Mvoxel/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": int(4 * n)}})
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -619,6 +663,8 @@ def main():
         run_stream_720p(args)
     elif args.workload == "serve_mix":
         run_serve_mix(args)
+    elif args.workload == "connect_320x240x85":
+        run_connect(args)
     else:
         run_ours(args)
 

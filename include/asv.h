@@ -165,6 +165,24 @@ asv_status asv_segment_clip(asv_ctx *ctx, const uint8_t *rgb, const float *fwd,
                             const float *bwd, int W, int H, int D, int K,
                             int32_t *labels_out);
 
+/* Image::enforce_connectivity_3d (GPU-AS/Image.cpp:1808-1837) with
+ * EnforceLabelConnectivity3D (:1938-2063), the reference's alternative to
+ * check_dead_seeds (Render.cpp "6.2"): the raw labels of the last JFA pass
+ * are split into connected segments (24-neighbourhood: the 8 in-plane
+ * offsets in slices z-1, z, z+1) numbered in raster order, and segments of
+ * fewer than supsz/4 voxels take the label of a neighbouring earlier
+ * segment.  supsz <= 0 means W*H*D / K (texel_num / seeds_num, :1833).
+ * Writes labels_out (D*H*W int32, may be NULL) and *label_num (may be NULL).
+ * One clip per context (not a batch or a stream).  Device scratch of about
+ * 32 bytes per voxel is held by the context after the first call. */
+asv_status asv_enforce_connectivity(asv_ctx *ctx, int supsz, int32_t *labels_out, int *label_num);
+
+/* The same on caller-provided labels: Render::label_connected3D of the
+ * streaming form over a whole video (streamGPU-AS/Render.cpp:572-695), or any
+ * label volume.  labels: D*H*W int32 host array; supsz > 0. */
+asv_status asv_enforce_connectivity_labels(asv_ctx *ctx, const int32_t *labels, int W, int H, int D,
+                                           int supsz, int32_t *labels_out, int *label_num);
+
 /* ---- state access ------------------------------------------------------ */
 asv_status asv_get_info(asv_ctx *ctx, asv_info *info);
 asv_status asv_get_labels(asv_ctx *ctx, int32_t *out);     /* post-processed */

@@ -280,5 +280,90 @@ def build(force=False):
     return LIB
 
 
+# ---------------------------------------------------------------------------
+# Host functions of the reference compiled from its C++ files: the function
+# text is cut out where it lies (comments dropped, `Class::` removed) and
+# placed in a struct that supplies the class members it reads.
+# ---------------------------------------------------------------------------
+HOST_LIB = os.path.join(OUT, "libref_host.so")
+HOST_FUNCS = [
+    # (file, signature start, shim struct, members)
+    ("GPU-AS/Image.cpp", "void Image::EnforceLabelConnectivity3D(", "ImageShim",
+     "int texel_num, depth, height, width, slice_num;"),
+    ("streamGPU-AS/Render.cpp", "void Render::label_connected3D(", "RenderShim",
+     "int width, height, depth_all;"),
+]
+
+HOST_WRAPPERS = r"""
+extern "C" int ref_enforce_connectivity(const int *labels, int W, int H, int D, int supsz, int *out)
+{
+    ImageShim s;
+    s.width = W; s.height = H; s.depth = D; s.slice_num = W * H; s.texel_num = W * H * D;
+    int *nl = out;
+    int num = 0;
+    s.EnforceLabelConnectivity3D(const_cast<int *>(labels), nl, num, supsz);
+    return num;
+}
+
+extern "C" int ref_label_connected3D(const int *labels, int W, int H, int D, int supsz, int *out)
+{
+    RenderShim s;
+    s.width = W; s.height = H; s.depth_all = D;
+    int num = 0;
+    s.label_connected3D(const_cast<int *>(labels), out, num, supsz);
+    return num;
+}
+"""
+
+
+def _strip_comments(src):
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return re.sub(r"//[^\n]*", "", src)
+
+
+def _cut_function(src, start):
+    i = src.index(start)
+    j = src.index("{", i)
+    depth = 0
+    for k in range(j, len(src)):
+        if src[k] == "{":
+            depth += 1
+        elif src[k] == "}":
+            depth -= 1
+            if depth == 0:
+                return src[i:k + 1]
+    raise ValueError("unbalanced braces after " + start)
+
+
+def build_host(force=False):
+    """Compiles the reference's host functions listed above; returns the
+    library path, or None when the reference tree is not present."""
+    srcs = [os.path.join(REF, f) for f, _, _, _ in HOST_FUNCS]
+    if not all(os.path.exists(f) for f in srcs):
+        return None
+    if not force and os.path.exists(HOST_LIB) and os.path.getmtime(HOST_LIB) >= max(
+            [os.path.getmtime(f) for f in srcs] + [os.path.getmtime(__file__)]):
+        return HOST_LIB
+    os.makedirs(OUT, exist_ok=True)
+    parts = ["#include <cstring>\n"]
+    for path, start, shim, members in HOST_FUNCS:
+        text = _strip_comments(open(os.path.join(REF, path), encoding="latin-1").read())
+        fn = _cut_function(text, start)
+        fn = re.sub(r"\b\w+::(\w+\s*\()", r"\1", fn, count=1)
+        parts.append(f"struct {shim} {{\n    {members}\n{fn}\n}};\n")
+    parts.append(HOST_WRAPPERS)
+    cpp = os.path.join(OUT, "ref_host.cpp")
+    with open(cpp, "w", encoding="latin-1") as fh:
+        fh.write("\n".join(parts))
+    tmp = HOST_LIB + ".tmp"
+    cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-w", "-o", tmp, cpp]
+    p = subprocess.run(cmd, capture_output=True, text=True)
+    if p.returncode != 0:
+        raise RuntimeError("reference host build failed:\n" + p.stderr[-6000:])
+    os.replace(tmp, HOST_LIB)
+    return HOST_LIB
+
+
 if __name__ == "__main__":
     print(build(force=True))
+    print(build_host(force=True))

@@ -5,8 +5,10 @@ shaders compiled as C++ (oracle/build_ref.py; needs the reference tree).
 
 Fixtures (npz): inputs plus the compiled reference shaders' outputs for
 RGB2LAB.fs (a seeded sample of RGB values), derivative_t.gs, flood.gs (one
-pass at several steps) and aver_exception.vs.  tests/test_golden.py checks
-the CPU restatement and the CUDA path against them.
+pass at several steps) and aver_exception.vs, and of the reference's
+Image::EnforceLabelConnectivity3D compiled from its C++ (connectivity.npz).
+tests/test_golden.py checks the CPU restatement and the CUDA path against
+them.
 """
 import ctypes
 import os
@@ -86,6 +88,18 @@ def main():
     for i in range(kp):
         lib.ref_aver_exception(P(sp), P(scol), P(img), W, H, D, i, P(pos[i]), P(col[i]))
     np.savez_compressed(os.path.join(HERE, "aver_exception.npz"), rgb=clip, sums=sums, pos=pos, col=col)
+
+    # Image::EnforceLabelConnectivity3D, compiled from the reference's C++
+    host = ctypes.CDLL(build_ref.build_host())
+    host.ref_enforce_connectivity.argtypes = [V, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, V]
+    host.ref_enforce_connectivity.restype = ctypes.c_int
+    arrays = {}
+    for i, (labels, supsz) in enumerate(pin.connectivity_cases(np.random.default_rng(31))):
+        D, H, W = labels.shape
+        out = np.empty_like(labels)
+        n = host.ref_enforce_connectivity(P(labels), W, H, D, supsz, P(out))
+        arrays.update({f"labels_{i}": labels, f"out_{i}": out, f"supsz_{i}": supsz, f"n_{i}": n})
+    np.savez_compressed(os.path.join(HERE, "connectivity.npz"), **arrays)
     print("fixtures written to", HERE)
 
 

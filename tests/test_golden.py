@@ -64,3 +64,25 @@ def test_cuda_flood(asv, step):
     img.set_seeds(f["seeds"])
     got = img.jfa_pass(f["labels"], int(f["step"]), float(np.float32(f["ratio"])))
     assert np.array_equal(got, f["out"])
+
+
+def _connectivity_cases():
+    f = load("connectivity.npz")
+    i = 0
+    while f"labels_{i}" in f:
+        yield f[f"labels_{i}"], int(f[f"supsz_{i}"]), f[f"out_{i}"], int(f[f"n_{i}"])
+        i += 1
+
+
+def test_oracle_connectivity(orc):
+    for labels, supsz, out, n in _connectivity_cases():
+        got, m = orc.enforce_connectivity(labels, supsz)
+        assert m == n and np.array_equal(got, out)
+
+
+@pytest.mark.gpu
+def test_cuda_connectivity(asv):
+    with asv.Image(lloyd_iters=1) as img:
+        for labels, supsz, out, n in _connectivity_cases():
+            got, m = img.enforce_connectivity_labels(labels, supsz)
+            assert m == n and np.array_equal(got, out), labels.shape

@@ -158,3 +158,56 @@ def test_aver_exception(ref, orc, asv):
         assert np.array_equal(p4[:3], got_pos[i]), i
         assert np.array_equal(c3, got_col[i]), i
         assert p4[3] == i
+
+
+@pytest.fixture(scope="module")
+def ref_host():
+    from oracle import build_ref
+    path = build_ref.build_host()
+    if path is None:
+        pytest.skip("reference tree not present")
+    lib = ctypes.CDLL(path)
+    V = ctypes.c_void_p
+    for f in (lib.ref_enforce_connectivity, lib.ref_label_connected3D):
+        f.argtypes = [V, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, V]
+        f.restype = ctypes.c_int
+    return lib
+
+
+def connectivity_cases(rng):
+    """label volumes: noisy, blocky (nearest of random centres), with -1, degenerate shapes"""
+    out = []
+    for (D, H, W) in ((7, 13, 17), (1, 9, 11), (5, 1, 19), (6, 12, 1), (3, 2, 2), (9, 20, 24)):
+        out.append((rng.integers(-1, 4, (D, H, W)).astype(np.int32), 40))
+        c = rng.integers(0, [W, H, D], (6, 3))
+        zz, yy, xx = np.meshgrid(np.arange(D), np.arange(H), np.arange(W), indexing="ij")
+        dist = [(xx - cx) ** 2 + (yy - cy) ** 2 + 2 * (zz - cz) ** 2 for cx, cy, cz in c]
+        blocky = np.argmin(np.stack(dist), 0).astype(np.int32)
+        noisy = blocky.copy()
+        flip = rng.random(blocky.shape) < 0.05
+        noisy[flip] = rng.integers(-1, 6, int(flip.sum()))
+        out.append((blocky, D * H * W // 6))
+        out.append((noisy, D * H * W // 6))
+    return out
+
+
+def test_connectivity_matches_reference(ref_host, orc):
+    rng = np.random.default_rng(29)
+    for labels, supsz in connectivity_cases(rng):
+        D, H, W = labels.shape
+        for fn in (ref_host.ref_enforce_connectivity, ref_host.ref_label_connected3D):
+            want = np.empty_like(labels)
+            n = fn(P(labels), W, H, D, supsz, P(want))
+            got, m = orc.enforce_connectivity(labels, supsz)
+            assert m == n
+            assert np.array_equal(got, want), (labels.shape, supsz)
+
+
+def test_connectivity_on_jfa_labels(ref_host, orc, asv):
+    rgb, fwd, bwd = small_clip(asv, W=48, H=36, D=10, seed=4, jitter=0.3, drift=1.0)
+    _, raw, _, info = orc.run_clip(rgb, fwd, bwd, 60, iters=3, nthreads=4)
+    supsz = raw.size // 60
+    want = np.empty_like(raw)
+    n = ref_host.ref_enforce_connectivity(P(raw), 48, 36, 10, supsz, P(want))
+    got, m = orc.enforce_connectivity(raw, supsz)
+    assert m == n and np.array_equal(got, want)
