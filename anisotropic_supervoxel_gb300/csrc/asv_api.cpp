@@ -175,6 +175,15 @@ struct asv_ctx {
 
 size_t asv::ctx_bytes(const asv_ctx *c) { return c ? c->bytes + c->cc_bytes : 0; }
 
+void asv::set_stream(asv_ctx *c, cudaStream_t st)
+{
+    if (!c || c->st == st) return;
+    cudaStreamSynchronize(c->st);
+    if (c->own_st) cudaStreamDestroy(c->st);
+    c->st = st;
+    c->own_st = false;
+}
+
 static asv_status fail(asv_ctx *c, asv_status s, const std::string &m)
 {
     if (c) c->err = m;

@@ -29,6 +29,7 @@ struct SegHost {
 
 int grid_seeds(int W, int H, int D, int K, int middlebury, GridInfo *g, std::vector<float> *seeds4);
 size_t ctx_bytes(const asv_ctx *ctx);   // device bytes a context holds
+void set_stream(asv_ctx *ctx, cudaStream_t st);   // later work of ctx runs on st (caller-owned)
 void cell_tables(int W, int H, int D, const GridInfo &g, const std::vector<float> &grid,
                  std::vector<int> *cells);
 float ratio_of(int s, float compactness);

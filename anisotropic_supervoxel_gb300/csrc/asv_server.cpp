@@ -4,9 +4,12 @@
 // request it can admit: one of its own shape (its context keeps the device
 // layout and the captured graph, no new memory), or one whose memory fits
 // the free part of the HBM budget after the worker drops its current layout.
-// Each slot's context runs on its own CUDA stream, so admitted requests
-// overlap on the device.  A streaming session owns a resident streaming
-// context and a worker that runs its windows in submission order.
+// Each slot's context runs on its own CUDA streams, so admitted requests
+// overlap on the device; small clips run on a higher-priority stream than
+// large ones, and streaming windows on the device's highest priority, so the
+// block scheduler serves them first when the GPU is shared.  A streaming
+// session owns a resident streaming context and a worker that runs its
+// windows in submission order.
 #include "asv.h"
 #include "asv_internal.h"
 
@@ -36,6 +39,7 @@ struct Slot {
     asv_ctx *ctx = nullptr;
     int W = 0, H = 0, D = 0, K = 0;
     size_t bytes = 0;
+    cudaStream_t small = nullptr, large = nullptr;   // priority streams for the two request classes
 };
 
 struct Session {
@@ -43,7 +47,12 @@ struct Session {
     size_t bytes = 0;
     std::deque<long long> q;
     std::thread th;
+    cudaStream_t st = nullptr;                       // highest priority: windows are real-time
 };
+
+// clips up to this many voxels run on the slot's higher-priority stream, so
+// their blocks are scheduled ahead of those of large clips sharing the GPU
+const long long kSmallClipVoxels = 4LL << 20;
 
 } // namespace
 
@@ -59,6 +68,7 @@ struct asv_server {
     std::vector<std::unique_ptr<Session>> sessions;
     long long next_id = 1, submitted = 0, completed = 0, failed = 0;
     int running = 0;
+    int prio_hi = 0;                  // greatest stream priority of the device
     bool stop = false;
 };
 
@@ -145,9 +155,14 @@ static void worker(asv_server *s, int w)
         q.t_start = Clock::now();
         lk.unlock();
         asv_status st = ASV_OK;
-        if (!sl.ctx) st = asv_create(&s->cfg, &sl.ctx);
+        if (!sl.ctx) {
+            asv_config c = s->cfg;
+            c.stream = sl.large;
+            st = asv_create(&c, &sl.ctx);
+        }
         if (st == ASV_OK) {
             const asv_request &r = q.r;
+            asv::set_stream(sl.ctx, (long long)r.W * r.H * r.D <= kSmallClipVoxels ? sl.small : sl.large);
             st = asv_segment_clip(sl.ctx, r.rgb, r.fwd, r.bwd, r.W, r.H, r.D, r.K, r.labels_out);
             if (st == ASV_OK) { sl.W = r.W; sl.H = r.H; sl.D = r.D; sl.K = r.K; }
             else { sl.W = sl.H = sl.D = sl.K = 0; }
@@ -203,9 +218,26 @@ asv_status asv_server_create(const asv_config *cfg, int max_slots, size_t hbm_bu
     if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) { cudaGetLastError(); return ASV_ERR_NO_DEVICE; }
     asv_server *s = new asv_server();
     if (cfg) s->cfg = *cfg; else asv_config_default(&s->cfg);
-    s->cfg.stream = nullptr;          // every slot gets its own stream
+    s->cfg.stream = nullptr;          // every slot gets its own streams
     s->budget = hbm_budget;
     s->slots.resize(max_slots);
+    cudaSetDevice(s->cfg.device);
+    int least = 0, greatest = 0;
+    cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    s->prio_hi = greatest;
+    const int mid = (least + greatest) / 2;
+    for (auto &sl : s->slots) {
+        if (cudaStreamCreateWithPriority(&sl.small, cudaStreamNonBlocking, mid) != cudaSuccess ||
+            cudaStreamCreateWithPriority(&sl.large, cudaStreamNonBlocking, least) != cudaSuccess) {
+            cudaGetLastError();
+            for (auto &t : s->slots) {
+                if (t.small) cudaStreamDestroy(t.small);
+                if (t.large) cudaStreamDestroy(t.large);
+            }
+            delete s;
+            return ASV_ERR_CUDA;
+        }
+    }
     for (int w = 0; w < max_slots; w++) s->workers.emplace_back(worker, s, w);
     *out = s;
     return ASV_OK;
@@ -230,6 +262,11 @@ asv_status asv_server_destroy(asv_server *s)
     }
     for (auto &sl : s->slots) if (sl.ctx) asv_destroy(sl.ctx);
     for (auto &ss : s->sessions) if (ss->ctx) asv_destroy(ss->ctx);
+    for (auto &sl : s->slots) {
+        cudaStreamDestroy(sl.small);
+        cudaStreamDestroy(sl.large);
+    }
+    for (auto &ss : s->sessions) if (ss->st) cudaStreamDestroy(ss->st);
     delete s;
     return ASV_OK;
 }
@@ -239,15 +276,25 @@ asv_status asv_server_open_session(asv_server *s, int W, int H, int D_all, int K
 {
     if (!s || !session) return ASV_ERR_BAD_ARG;
     auto ss = std::make_unique<Session>();
+    cudaSetDevice(s->cfg.device);
+    if (cudaStreamCreateWithPriority(&ss->st, cudaStreamNonBlocking, s->prio_hi) != cudaSuccess) {
+        cudaGetLastError();
+        return ASV_ERR_CUDA;
+    }
     asv_config c = s->cfg;
     c.use_graph = 0;
+    c.stream = ss->st;
     asv_status st = asv_create(&c, &ss->ctx);
-    if (st != ASV_OK) return st;
+    if (st != ASV_OK) { cudaStreamDestroy(ss->st); return st; }
     st = asv_stream_begin(ss->ctx, W, H, D_all, K_video, seeds_num_100, block_size);
-    if (st != ASV_OK) { asv_destroy(ss->ctx); return st; }
+    if (st != ASV_OK) { asv_destroy(ss->ctx); cudaStreamDestroy(ss->st); return st; }
     ss->bytes = asv::ctx_bytes(ss->ctx);
     std::lock_guard<std::mutex> lk(s->mu);
-    if (s->budget && s->used + ss->bytes > s->budget) { asv_destroy(ss->ctx); return ASV_ERR_OVER_BUDGET; }
+    if (s->budget && s->used + ss->bytes > s->budget) {
+        asv_destroy(ss->ctx);
+        cudaStreamDestroy(ss->st);
+        return ASV_ERR_OVER_BUDGET;
+    }
     s->used += ss->bytes;
     Session *raw = ss.get();
     s->sessions.push_back(std::move(ss));

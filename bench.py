@@ -58,6 +58,19 @@ def workload(name):
             "clip_240x160x30": workloads.CLIP_240x160x30}[name]
 
 
+def replicas_value(units_per_rank, seconds, device=None):
+    """Whole-job throughput of independent replicas: every rank processed
+    `units_per_rank`; the job took the slowest rank's time (max over ranks).
+    Returns (units of all ranks / max seconds, max seconds)."""
+    import torch
+    ws = torch.distributed.get_world_size() if torch.distributed.is_initialized() else 1
+    if ws > 1:
+        t = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        seconds = float(t.item())
+    return units_per_rank * ws / seconds, seconds
+
+
 def dist():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -238,12 +251,8 @@ def run_ours(args):
     barrier()
     clk = clocks.stop()
     step_ms = [a.elapsed_time(b) for a, b in ev]
-    tot_ms = sum(step_ms)
-    if ws > 1:
-        t = torch.tensor([tot_ms], device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        tot_ms = float(t.item())
-    value = nvox * I * args.steps * ws / (tot_ms / 1e3) / 1e6
+    value, tot_s = replicas_value(nvox * I * args.steps / 1e6, sum(step_ms) / 1e3, f"cuda:{local}")
+    tot_ms = tot_s * 1e3
     info = img.info()
 
     # --- JFA kernel: per-launch device time (CUDA events around each pass) ----
@@ -295,12 +304,7 @@ def run_ours(args):
         e2e_step()
     torch.cuda.synchronize()
     barrier()
-    e2e_s = time.perf_counter() - t0
-    if ws > 1:
-        t = torch.tensor([e2e_s], device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_val = nvox * I * args.steps * ws / e2e_s / 1e6
+    e2e_val, e2e_s = replicas_value(nvox * I * args.steps / 1e6, time.perf_counter() - t0, f"cuda:{local}")
     ok_labels = bool((plab == img.labels()).all())
     e2e.close()
 

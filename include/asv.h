@@ -269,8 +269,10 @@ asv_status asv_stream_push(asv_ctx *ctx, const uint8_t *rgb, const float *fwd, c
  * admitted as soon as a slot and enough of the HBM budget are free (first
  * fit, so a small request can pass a large one that does not fit yet), each
  * admitted request runs on its slot's own CUDA stream so that the work of
- * several requests overlaps on the device, and a slot keeps its device layout
- * and captured graph for the next request of the same shape.  Streaming
+ * several requests overlaps on the device (clips of up to 4 Mi voxels on a
+ * higher-priority stream than larger ones, streaming windows on the highest
+ * priority), and a slot keeps its device layout and captured graph for the
+ * next request of the same shape.  Streaming
  * sessions hold a resident streaming context (asv_stream_*) whose windows
  * are processed in order.  Results are those of the single-clip / streaming
  * calls, whatever else is running. */
