@@ -79,6 +79,7 @@ SIGNATURES = {
     "asv_status_string": (c_char_p, [c_int]),
     "asv_version": (c_int, []),
     "asv_init_gpu": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int]),
+    "asv_init_gpu_bgr": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int]),
     "asv_upload_flow": (c_int, [c_void_p, c_void_p, c_void_p]),
     "asv_initialization": (c_int, [c_void_p]),
     "asv_seed_matrix": (c_int, [c_void_p]),

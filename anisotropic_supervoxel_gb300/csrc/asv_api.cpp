@@ -573,20 +573,37 @@ size_t asv_clip_bytes(int W, int H, int D, int K)
     return asv_layout_bytes(v);
 }
 
-asv_status asv_init_gpu(asv_ctx *ctx, const uint8_t *rgb, int W, int H, int D, int K)
+// the clip's RGB volume: copied as is, or (bgr) raw frames copied into the
+// second label buffer (unused until the Lloyd loop) and preprocessed into
+// the RGB volume on the device
+static asv_status upload_clip(asv_ctx *ctx, const uint8_t *px, bool bgr)
+{
+    const SegDesc &s = ctx->sd[0];
+    const size_t n3 = (size_t)s.nvox * 3;
+    if (!bgr) {
+        CK(cudaMemcpyAsync(ctx->d.rgb, px, n3, cudaMemcpyHostToDevice, ctx->st));
+    } else {
+        uint8_t *stage = (uint8_t *)ctx->d.labB;                       // 4 bytes / voxel >= 3
+        CK(cudaMemcpyAsync(stage, px, n3, cudaMemcpyHostToDevice, ctx->st));
+        asv_launch_preprocess(stage, ctx->d.rgb, s.W, s.H, s.D, ctx->st);
+        CK(cudaGetLastError());
+    }
+    ctx->have_rgb = true;
+    return ASV_OK;
+}
+
+static asv_status init_clip(asv_ctx *ctx, const uint8_t *px, int W, int H, int D, int K, bool bgr)
 {
     if (!ctx) return ASV_ERR_BAD_ARG;
-    if (!rgb) return fail(ctx, ASV_ERR_BAD_ARG, "rgb is NULL");
+    if (!px) return fail(ctx, ASV_ERR_BAD_ARG, "frames pointer is NULL");
     cudaSetDevice(ctx->cfg.device);
-    if (ctx->seg.size() == 1 && !ctx->allocs.empty()) {
+    if (ctx->seg.size() == 1 && !ctx->allocs.empty() && !ctx->sm.on) {
         const SegHost &o = ctx->seg[0];
         if (o.W == W && o.H == H && o.D == D && o.K == K) {
             // same clip shape: keep the device layout and the captured graph
-            CK(cudaMemcpyAsync(ctx->d.rgb, rgb, (size_t)W * H * D * 3, cudaMemcpyHostToDevice, ctx->st));
-            ctx->have_rgb = true;
             ctx->have_flow = ctx->have_pos0 = ctx->have_M0 = ctx->have_lab = false;
             ctx->seeded = ctx->ran = false;
-            return ASV_OK;
+            return upload_clip(ctx, px, bgr);
         }
     }
     SegHost h;
@@ -598,9 +615,17 @@ asv_status asv_init_gpu(asv_ctx *ctx, const uint8_t *rgb, int W, int H, int D, i
     ctx->seg = v;
     s = asv_build_layout(ctx);
     if (s != ASV_OK) return s;
-    CK(cudaMemcpyAsync(ctx->d.rgb, rgb, (size_t)W * H * D * 3, cudaMemcpyHostToDevice, ctx->st));
-    ctx->have_rgb = true;
-    return ASV_OK;
+    return upload_clip(ctx, px, bgr);
+}
+
+asv_status asv_init_gpu(asv_ctx *ctx, const uint8_t *rgb, int W, int H, int D, int K)
+{
+    return init_clip(ctx, rgb, W, H, D, K, false);
+}
+
+asv_status asv_init_gpu_bgr(asv_ctx *ctx, const uint8_t *bgr, int W, int H, int D, int K)
+{
+    return init_clip(ctx, bgr, W, H, D, K, true);
 }
 
 asv_status asv_upload_flow(asv_ctx *ctx, const float *fwd, const float *bwd)

@@ -100,6 +100,7 @@ struct AsvDev {
 
 void asv_launch_srgb_table(const AsvDev &d, cudaStream_t st);
 void asv_launch_rgb2lab(const AsvDev &d, cudaStream_t st);
+void asv_launch_preprocess(const uint8_t *bgr, uint8_t *rgb, int W, int H, int D, cudaStream_t st);
 const uchar4 *asv_lab_table(int device);
 void asv_launch_density(const AsvDev &d, cudaStream_t st);
 void asv_launch_density_adjust(const AsvDev &d, cudaStream_t st);

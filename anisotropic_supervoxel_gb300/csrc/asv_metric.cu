@@ -210,7 +210,15 @@ __device__ void asv_m6_nearest_psd(const float M[6], float out[6])
     }
 }
 
-__device__ __forceinline__ float asv_round_half_up(float f) { return (float)floor((double)f + 0.5); }
+// floor(f + 0.5) of the reference's round (GPU-AS/Image.cpp:901), exactly:
+// f + 0.5 can round in FP32, but f - floorf(f) cannot change which side of
+// 0.5 the fraction lies on, and the result is the reference's value for every
+// float (the +0.0f turns the -0 of f = -0 into +0, as floor(-0 + 0.5) is +0).
+__device__ __forceinline__ float asv_round_half_up(float f)
+{
+    const float r = floorf(f);
+    return (f - r >= 0.5f ? r + 1.0f : r) + 0.0f;
+}
 
 // matrix_slover (GPU-AS/Image.cpp:874-1009) for one warp; M valid on every
 // lane (its PSD test, :997-1006, is k_metric_psd).  Rows are numbered in the

@@ -128,6 +128,53 @@ __global__ void __launch_bounds__(256) k_rgb2lab_lut(AsvDev d)
 }
 
 // ---------------------------------------------------------------------------
+// Render::cvMat2TexureInput (GPU-AS/Render.cpp:354-359) for raw frames (BGR8,
+// top row first): 3x3 Gaussian blur with sigma 0 (the [1,2,1] x [1,2,1] / 16
+// kernel, border reflect-101, rounded half up), BGR -> RGB and the vertical
+// flip into texture orientation.  One thread per output pixel and frame;
+// the same integer arithmetic as the host asv_preprocess_frame.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int asv_reflect101(int i, int n)
+{
+    if (n == 1) return 0;
+    while (i < 0 || i >= n) i = i < 0 ? -i : 2 * n - 2 - i;
+    return i;
+}
+
+__global__ void k_preprocess(const uint8_t *__restrict__ bgr, uint8_t *__restrict__ rgb, int W, int H, int D)
+{
+    const long long fr = (long long)W * H;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= fr * D) return;
+    const int z = (int)(t / fr), p = (int)(t - (long long)z * fr);
+    const int yo = p / W, x = p - yo * W, y = H - 1 - yo;          // output row yo <- source row y
+    const uint8_t *src = bgr + 3 * fr * z;
+    int acc[3] = { 0, 0, 0 };
+    for (int j = -1; j <= 1; j++) {
+        const int yy = asv_reflect101(y + j, H);
+        const int wy = j == 0 ? 2 : 1;
+        for (int i = -1; i <= 1; i++) {
+            const int xx = asv_reflect101(x + i, W);
+            const int wgt = wy * (i == 0 ? 2 : 1);
+            const uint8_t *q = src + 3 * ((long long)yy * W + xx);
+            acc[0] += wgt * q[0];
+            acc[1] += wgt * q[1];
+            acc[2] += wgt * q[2];
+        }
+    }
+    uint8_t *o = rgb + 3 * t;
+    o[0] = (uint8_t)((acc[2] + 8) >> 4);                             // R <- channel 2 of BGR
+    o[1] = (uint8_t)((acc[1] + 8) >> 4);
+    o[2] = (uint8_t)((acc[0] + 8) >> 4);
+}
+
+void asv_launch_preprocess(const uint8_t *bgr, uint8_t *rgb, int W, int H, int D, cudaStream_t st)
+{
+    const long long n = (long long)W * H * D;
+    k_preprocess<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(bgr, rgb, W, H, D);
+}
+
+// ---------------------------------------------------------------------------
 // Gradient density per grid cell (GPU-AS/Image.cpp:350-620,
 // derivative_t.gs:24-49, density_grid.vs:17-43).  Each voxel's gradient is
 // rounded to half (RGB16F target) and summed exactly, in units of 2^-24.

@@ -84,6 +84,14 @@ class Image:
         self._ck(self.lib.asv_init_gpu(self.h, _ptr(rgb), W, H, D, K))
         self.shape = (D, H, W)
 
+    def init_gpu_bgr(self, bgr, K):
+        """init_gpu for raw BGR frames [D,H,W,3] (top row first): blur, BGR->RGB
+        and flip on the device (Render::cvMat2TexureInput)."""
+        bgr = np.ascontiguousarray(bgr, np.uint8)
+        D, H, W, _ = bgr.shape
+        self._ck(self.lib.asv_init_gpu_bgr(self.h, _ptr(bgr), W, H, D, K))
+        self.shape = (D, H, W)
+
     def upload_flow(self, fwd, bwd):
         fwd = np.ascontiguousarray(fwd, np.float32)
         bwd = np.ascontiguousarray(bwd, np.float32)

@@ -106,6 +106,13 @@ int asv_version(void);
  * RGB8 clip (D*H*W*3 bytes) and places the regular grid of seeds for K. */
 asv_status asv_init_gpu(asv_ctx *ctx, const uint8_t *rgb, int W, int H, int D, int K);
 
+/* asv_init_gpu for raw frames: D frames of BGR8, each top row first (as
+ * read from a video), preprocessed on the device as Render::cvMat2TexureInput
+ * does (GPU-AS/Render.cpp:354-359: 3x3 Gaussian blur, BGR -> RGB, vertical
+ * flip) before they become the clip's RGB volume.  Same bytes as running
+ * asv_preprocess_frame (asv_host.h) on each frame and calling asv_init_gpu. */
+asv_status asv_init_gpu_bgr(asv_ctx *ctx, const uint8_t *bgr, int W, int H, int D, int K);
+
 /* Output of Image::forward_backward_flow (GPU-AS/Image.cpp:643-686), which
  * the reference computes with OpenCV; here it is an input: fwd[z] is the
  * flow z -> z+1, bwd[z] the flow z -> z-1, each D*H*W*2 floats.  fwd[D-1]

@@ -337,3 +337,20 @@ def test_psd_test_is_exact(orc):
               np.array([3e38, 1e38, 0, 3e38, 0, 1e-38], np.float32)]
     for M in cases:
         assert orc.m6_negative(M) == _negative_exact(M), M.tolist()
+
+
+def test_round_half_up_fp32_form():
+    """The GPU's FP32 form of floor(f + 0.5) (no FP64) equals the FP64 form on
+    random bit patterns, values next to every k + 0.5 and small values."""
+    rng = np.random.default_rng(0)
+    f = rng.integers(0, 2 ** 32, 4_000_000, dtype=np.uint64).astype(np.uint32).view(np.float32)
+    near = (rng.integers(-2 ** 24, 2 ** 24, 1_000_000).astype(np.float64) + 0.5).astype(np.float32)
+    near = np.concatenate([near, np.nextafter(near, np.float32(np.inf)), np.nextafter(near, np.float32(-np.inf))])
+    f = np.concatenate([f, near, rng.uniform(-3, 3, 1_000_000).astype(np.float32),
+                        np.array([0.0, -0.0, 0.5, -0.5, 0.49999997, -0.49999997, np.inf, -np.inf], np.float32)])
+    with np.errstate(all="ignore"):
+        want = np.floor(f.astype(np.float64) + 0.5).astype(np.float32)
+        r = np.floor(f)
+        got = (np.where(f - r >= np.float32(0.5), r + np.float32(1), r) + np.float32(0)).astype(np.float32)
+    same = (want.view(np.uint32) == got.view(np.uint32)) | (np.isnan(want) & np.isnan(got))
+    assert same.all()
