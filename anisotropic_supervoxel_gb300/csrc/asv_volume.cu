@@ -386,23 +386,29 @@ __device__ __forceinline__ void asv_chain_pos(int p, int D, int step, int &r, in
 }
 
 // valid ids among the 9 labels of one slice (offset zoff) around the
-// column, first-occurrence order; an id equal to one of the last four listed
-// is dropped.  Writes the list (stride ASV_JFA_THREADS), returns its length.
+// column, each once, in first-occurrence order: a label is listed unless it
+// equals one of the labels before it (compares against the loaded labels,
+// all in registers, so nothing is shifted or stored to dedup).  Writes the
+// list (stride ASV_JFA_THREADS), returns its length.
 __device__ __forceinline__ int asv_slice_list(const int32_t *__restrict__ in, int zoff, const int xs[3],
                                               const int ys[3], int Kp, asv_list_t *__restrict__ lst)
 {
-    int n = 0, r1 = -1, r2 = -1, r3 = -1, r4 = -1;
+    int32_t c[9];
 #pragma unroll
     for (int oy = 0; oy < 3; oy++)
 #pragma unroll
-        for (int ox = 0; ox < 3; ox++) {
-            const int32_t l = __ldg(in + zoff + ys[oy] + xs[ox]);
-            if ((unsigned)l < (unsigned)Kp && l != r1 && l != r2 && l != r3 && l != r4) {
-                lst[n * ASV_JFA_THREADS] = l;
-                n++;
-                r4 = r3; r3 = r2; r2 = r1; r1 = l;
-            }
+        for (int ox = 0; ox < 3; ox++) c[oy * 3 + ox] = __ldg(in + zoff + ys[oy] + xs[ox]);
+    int n = 0;
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+        bool fresh = (unsigned)c[k] < (unsigned)Kp;
+#pragma unroll
+        for (int e = 0; e < k; e++) fresh = fresh && c[k] != c[e];
+        if (fresh) {
+            lst[n * ASV_JFA_THREADS] = c[k];
+            n++;
         }
+    }
     return n;
 }
 
