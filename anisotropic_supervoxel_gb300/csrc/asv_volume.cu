@@ -254,9 +254,10 @@ __global__ void __launch_bounds__(256) k_density(AsvDev d)
 
 // 1-D redistribution of the seeds along the cells (Image.cpp:549-616).  One
 // block per segment: the densities are formed in parallel, the prefix sums
-// (sequential float sums in the reference) and the walk by one thread, on
-// shared memory when Kp <= ASV_ADJ_SMEM, else on `scratch` (Kp floats).
-#define ASV_ADJ_SMEM 12288
+// (sequential float sums in the reference) by one thread, the placement in
+// parallel; on shared memory when Kp <= ASV_ADJ_SMEM, else on `scratch`
+// (Kp floats).
+#define ASV_ADJ_SMEM 12256     // floats: with the kernel's static counter the block stays within 48 KB
 
 __global__ void __launch_bounds__(256) k_density_adjust(AsvDev d, float *scratch)
 {
@@ -274,27 +275,41 @@ __global__ void __launch_bounds__(256) k_density_adjust(AsvDev d, float *scratch
         float res = __ull2float_rn(tot) * 0x1p-24f;
         len[i] = (float)(0.001 * (double)res);                        // :554
     }
+    __shared__ int placed;
     __syncthreads();
-    if (threadIdx.x != 0) return;
-    for (int i = 1; i < Kp; i++) len[i] = len[i] + len[i - 1];        // :558-569
-    float interval = len[Kp - 1] / (float)(Kp + 1);                   // :570
-    int i = 0, j1 = 0, n = 0;
-    while (i < Kp) {                                                  // :586-616
-        float seed_in = (float)(i + 1) * interval;
-        if (seed_in < len[j1]) {
-            int c = j1 % S.wNum;
-            int x1 = xl[c], x2 = xr[c];
-            float frac = j1 == 0 ? seed_in / len[j1] : (seed_in - len[j1 - 1]) / (len[j1] - len[j1 - 1]);
-            float ax = floorf((float)x1 + (float)(x2 - x1) * frac);
-            float4 g = grid[j1];
-            d.pos0[S.seed_off + n] = make_float4((float)((double)ax + 0.5), g.y, g.z, (float)i);
-            n++; i++;
-        } else {
-            j1++;
-            if (j1 == Kp) break;
-        }
+    if (threadIdx.x == 0) {
+        for (int i = 1; i < Kp; i++) len[i] = len[i] + len[i - 1];    // :558-569 (float order kept)
+        placed = 0;
     }
-    d.post[si * ASV_POST_WORDS + POST_VALID] = n;   // seeds placed (checked by the host)
+    __syncthreads();
+    const float interval = len[Kp - 1] / (float)(Kp + 1);             // :570
+    // The reference walks seeds and cells together (:586-616): seed i lands
+    // in the first cell j1 with seed_in < len[j1], searching on from the
+    // previous seed's cell.  seed_in grows with i and len never decreases,
+    // so that cell is the first such cell of the whole array: found here by
+    // a binary search per seed.  Once no cell qualifies the walk stops, so
+    // the placed seeds are a prefix 0..n-1 of the ids.
+    int mine = 0;
+    for (int i = threadIdx.x; i < Kp; i += blockDim.x) {
+        const float seed_in = (float)(i + 1) * interval;
+        int lo = 0, hi = Kp;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (seed_in < len[mid]) hi = mid; else lo = mid + 1;
+        }
+        const int j1 = lo;
+        if (j1 == Kp) continue;
+        const int c = j1 % S.wNum;
+        const int x1 = xl[c], x2 = xr[c];
+        const float frac = j1 == 0 ? seed_in / len[j1] : (seed_in - len[j1 - 1]) / (len[j1] - len[j1 - 1]);
+        const float ax = floorf((float)x1 + (float)(x2 - x1) * frac);
+        const float4 g = grid[j1];
+        d.pos0[S.seed_off + i] = make_float4((float)((double)ax + 0.5), g.y, g.z, (float)i);
+        mine++;
+    }
+    atomicAdd(&placed, mine);
+    __syncthreads();
+    if (threadIdx.x == 0) d.post[si * ASV_POST_WORDS + POST_VALID] = placed;   // checked by the host
 }
 
 // ---------------------------------------------------------------------------
