@@ -20,9 +20,10 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["asv_volume.cu", "asv_metric.cu", "asv_noalloc.cu", "asv_stream.cu", "asv_connect.cu"]
+CU_SOURCES = ["asv_volume.cu", "asv_metric.cu", "asv_noalloc.cu", "asv_stream.cu", "asv_connect.cu",
+              "asv_flow.cu"]
 CPP_SOURCES = ["asv_api.cpp", "asv_synth.cpp", "asv_server.cpp"]
-HEADERS = ["asv_common.cuh", "asv_internal.h", "asv_stream.cuh", "asv_connect.cuh"]
+HEADERS = ["asv_common.cuh", "asv_internal.h", "asv_stream.cuh", "asv_connect.cuh", "asv_flow.cuh"]
 PUBLIC_HEADERS = ["asv.h", "asv_host.h"]
 
 

@@ -82,6 +82,7 @@ SIGNATURES = {
     "asv_init_gpu_bgr": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int]),
     "asv_upload_flow": (c_int, [c_void_p, c_void_p, c_void_p]),
     "asv_initialization": (c_int, [c_void_p]),
+    "asv_compute_flow": (c_int, [c_void_p]),
     "asv_seed_matrix": (c_int, [c_void_p]),
     "asv_rgb2lab": (c_int, [c_void_p]),
     "asv_ld_first_init": (c_int, [c_void_p]),
@@ -99,6 +100,7 @@ SIGNATURES = {
     "asv_get_info": (c_int, [c_void_p, P(Info)]),
     "asv_get_labels": (c_int, [c_void_p, c_void_p]),
     "asv_get_raw_labels": (c_int, [c_void_p, c_void_p]),
+    "asv_get_flow": (c_int, [c_void_p, c_void_p, c_void_p]),
     "asv_get_seeds": (c_int, [c_void_p, c_void_p]),
     "asv_set_seeds": (c_int, [c_void_p, c_void_p, c_int]),
     "asv_get_lab": (c_int, [c_void_p, c_void_p]),

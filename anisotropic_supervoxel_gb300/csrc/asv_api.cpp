@@ -7,6 +7,7 @@
 #include "asv_common.cuh"
 #include "asv_internal.h"
 #include "asv_connect.cuh"
+#include "asv_flow.cuh"
 #include "asv_stream.cuh"
 
 #include <cuda_runtime.h>
@@ -171,9 +172,12 @@ struct asv_ctx {
     // connectivity enforcement scratch (asv_enforce_connectivity*), grown on demand
     void *cc = nullptr;
     size_t cc_bytes = 0;
+    // optical-flow scratch (asv_compute_flow), grown on demand
+    void *fl = nullptr;
+    size_t fl_bytes = 0;
 };
 
-size_t asv::ctx_bytes(const asv_ctx *c) { return c ? c->bytes + c->cc_bytes : 0; }
+size_t asv::ctx_bytes(const asv_ctx *c) { return c ? c->bytes + c->cc_bytes + c->fl_bytes : 0; }
 
 void asv::set_stream(asv_ctx *c, cudaStream_t st)
 {
@@ -553,6 +557,7 @@ asv_status asv_destroy(asv_ctx *ctx)
     cudaStreamSynchronize(ctx->st);
     free_layout(ctx);
     if (ctx->cc) cudaFree(ctx->cc);
+    if (ctx->fl) cudaFree(ctx->fl);
     for (auto e : ctx->ev) cudaEventDestroy(e);
     if (ctx->own_st) cudaStreamDestroy(ctx->st);
     delete ctx;
@@ -636,6 +641,34 @@ asv_status asv_upload_flow(asv_ctx *ctx, const float *fwd, const float *bwd)
     size_t n = (size_t)ctx->seg[0].W * ctx->seg[0].H * ctx->seg[0].D;
     CK(cudaMemcpyAsync(ctx->d.fwd, fwd, n * 8, cudaMemcpyHostToDevice, ctx->st));
     CK(cudaMemcpyAsync(ctx->d.bwd, bwd, n * 8, cudaMemcpyHostToDevice, ctx->st));
+    ctx->have_flow = true;
+    return ASV_OK;
+}
+
+asv_status asv_compute_flow(asv_ctx *ctx)
+{
+    if (!ctx) return ASV_ERR_BAD_ARG;
+    if (!ctx->have_rgb || ctx->sm.on) return fail(ctx, ASV_ERR_STATE, "no clip: call asv_init_gpu first");
+    cudaSetDevice(ctx->cfg.device);
+    size_t need = 0;
+    for (const SegDesc &s : ctx->sd) need = std::max(need, asv_flow_scratch_bytes(s.W, s.H, s.D));
+    if (ctx->fl_bytes < need) {
+        if (ctx->cfg.hbm_budget && ctx->bytes + ctx->cc_bytes + need > ctx->cfg.hbm_budget)
+            return fail(ctx, ASV_ERR_OVER_BUDGET, "optical-flow scratch exceeds the configured HBM budget");
+        if (ctx->fl) { cudaFree(ctx->fl); ctx->fl = nullptr; ctx->fl_bytes = 0; }
+        cudaError_t e = cudaMalloc(&ctx->fl, need);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            ctx->fl = nullptr;
+            return fail(ctx, ASV_ERR_OOM, "cudaMalloc: optical-flow scratch");
+        }
+        ctx->fl_bytes = need;
+    }
+    for (const SegDesc &s : ctx->sd)                    // segments share the scratch, one after another
+        if (asv_launch_flow(ctx->d.rgb + 3 * s.vox_off, s.W, s.H, s.D, ctx->d.fwd + s.vox_off,
+                            ctx->d.bwd + s.vox_off, ctx->fl, ctx->st) != 0)
+            return cuda_fail(ctx, cudaGetLastError(), "optical-flow kernels");
+    CK(cudaStreamSynchronize(ctx->st));
     ctx->have_flow = true;
     return ASV_OK;
 }
@@ -1018,6 +1051,17 @@ asv_status asv_get_lab(asv_ctx *ctx, uint8_t *out)
     if (!ctx->have_lab) return fail(ctx, ASV_ERR_STATE, "no LAB volume: call asv_rgb2lab first");
     const SegDesc &s = ctx->sd[0];
     CK(cudaMemcpyAsync(out, ctx->d.lab + s.vox_off, 4 * (size_t)s.nvox, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return ASV_OK;
+}
+
+asv_status asv_get_flow(asv_ctx *ctx, float *fwd, float *bwd)
+{
+    if (!ctx || !fwd || !bwd) return ASV_ERR_BAD_ARG;
+    if (!ctx->have_flow || ctx->sd.empty()) return fail(ctx, ASV_ERR_STATE, "no flow on the device");
+    const SegDesc &s = ctx->sd[0];
+    CK(cudaMemcpyAsync(fwd, ctx->d.fwd + s.vox_off, 8 * (size_t)s.nvox, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(bwd, ctx->d.bwd + s.vox_off, 8 * (size_t)s.nvox, cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
     return ASV_OK;
 }

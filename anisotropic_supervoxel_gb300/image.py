@@ -97,6 +97,18 @@ class Image:
         bwd = np.ascontiguousarray(bwd, np.float32)
         self._ck(self.lib.asv_upload_flow(self.h, _ptr(fwd), _ptr(bwd)))
 
+    def compute_flow(self):
+        """forward_backward_flow on the device (asv_compute_flow), instead of upload_flow"""
+        self._ck(self.lib.asv_compute_flow(self.h))
+
+    def flow(self):
+        """(fwd, bwd) flow volumes [D,H,W,2] of a one-clip context"""
+        D, H, W = self.shape
+        fwd = np.empty((D, H, W, 2), np.float32)
+        bwd = np.empty((D, H, W, 2), np.float32)
+        self._ck(self.lib.asv_get_flow(self.h, _ptr(fwd), _ptr(bwd)))
+        return fwd, bwd
+
     def initialization(self):
         self._ck(self.lib.asv_initialization(self.h))
 

@@ -45,7 +45,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="clip_320x240x85",
                     choices=["clip_320x240x85", "clip_240x160x30", "batch16", "stream_720p",
-                             "serve_mix", "connect_320x240x85"])
+                             "serve_mix", "connect_320x240x85", "pipeline_320x240x85"])
     ap.add_argument("--requests", type=int, default=160, help="serve_mix: requests in the run")
     ap.add_argument("--rate", type=float, default=40.0, help="serve_mix: mean arrivals per second")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -657,6 +657,65 @@ def run_connect(args):
                    "d2h_bytes_per_step": int(4 * n)}})
 
 
+def run_pipeline(args):
+    """The whole Render::run on the device for the 320x240x85 clip: raw BGR
+    frames (top row first) up from pinned memory, preprocessing
+    (asv_init_gpu_bgr), the forward/backward optical flow (asv_compute_flow,
+    in place of OpenCV's Farneback), seed placement, metric, LAB, the Lloyd
+    loop, labels back.  value = voxel-iterations / wall time of that step."""
+    import numpy as np
+    import torch
+
+    import anisotropic_supervoxel_gb300 as asv
+    from anisotropic_supervoxel_gb300 import workloads
+    torch.cuda.set_device(0)
+    w = workloads.CLIP_320x240x85
+    rgb, _, _ = workloads.make_clip(w)
+    bgr = _pinned(np.ascontiguousarray(rgb[:, ::-1, :, ::-1]))      # as read from a video
+    D, H, W, _ = rgb.shape
+    n, I, K = W * H * D, w["iters"], w["K"]
+    out = _pinned(np.empty((D, H, W), np.int32))
+    img = asv.Image(lloyd_iters=I)
+    lib = img.lib
+
+    def step(timed):
+        ev = None
+        if timed:
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        img.init_gpu_bgr(bgr, K)
+        st = torch.cuda.ExternalStream(img.stream(), device=torch.device("cuda", 0))
+        if ev:
+            ev[0].record(st)
+        img.compute_flow()
+        if ev:
+            ev[1].record(st)
+        img.initialization()
+        img.seed_matrix()
+        img.RGB2LAB()
+        img.run_lloyd()
+        lib.asv_get_labels(img.h, out.ctypes.data)
+        if ev:
+            ev[2].record(st)
+        return ev
+
+    for _ in range(args.warmup):
+        step(False)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    evs = [step(True) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / args.steps
+    flow_ms = statistics.mean(e[0].elapsed_time(e[1]) for e in evs)
+    img.close()
+    _line(args, n * I / dt / 1e6, dt * 1e3,
+          {"workload": "pipeline_320x240x85_K1000_I15", "parallelism": "replicas1",
+           "l2": "inputs larger than L2 (19.6 MB frames, 80 MB working set, flow scratch 1.1 GB)"},
+          {"flow_ms": flow_ms, "flow_pairs": 2 * (D - 1),
+           "e2e": {"value": n * I / dt / 1e6, "unit": UNIT, "h2d_bytes_per_step": int(bgr.nbytes),
+                   "d2h_bytes_per_step": int(out.nbytes)},
+           "note": "flow by this library's Farneback implementation (OpenCV's is not available)"})
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -669,6 +728,8 @@ def main():
         run_serve_mix(args)
     elif args.workload == "connect_320x240x85":
         run_connect(args)
+    elif args.workload == "pipeline_320x240x85":
+        run_pipeline(args)
     else:
         run_ours(args)
 

@@ -119,6 +119,17 @@ asv_status asv_init_gpu_bgr(asv_ctx *ctx, const uint8_t *bgr, int W, int H, int 
  * and bwd[0] are not read by the metric solve. */
 asv_status asv_upload_flow(asv_ctx *ctx, const float *fwd, const float *bwd);
 
+/* Image::forward_backward_flow (GPU-AS/Image.cpp:643-686) on the device:
+ * the forward (z -> z+1) and backward (z -> z-1) dense flow of every frame
+ * of the clip(s) already uploaded, from their grey frames, in place of
+ * asv_upload_flow.  The reference calls OpenCV's CUDA Farneback with its
+ * default configuration; OpenCV is not available to this library, so this is
+ * its own implementation of Farneback's polynomial-expansion method with that
+ * configuration (5 levels, scale 0.5, neighbourhood 5, sigma 1.1, 13x13
+ * window, 10 iterations): not bit-identical to OpenCV's.  Device scratch of
+ * about 50 bytes per voxel and frame pair is held by the context. */
+asv_status asv_compute_flow(asv_ctx *ctx);
+
 /* Image::initialization (GPU-AS/Image.cpp:350-620): gradient-density seed
  * placement (derivative_t.gs, density_grid.vs, 1-D redistribution). */
 asv_status asv_initialization(asv_ctx *ctx);
@@ -194,6 +205,8 @@ asv_status asv_enforce_connectivity_labels(asv_ctx *ctx, const int32_t *labels, 
 asv_status asv_get_info(asv_ctx *ctx, asv_info *info);
 asv_status asv_get_labels(asv_ctx *ctx, int32_t *out);     /* post-processed */
 asv_status asv_get_raw_labels(asv_ctx *ctx, int32_t *out); /* last JFA pass */
+/* the flow volumes on the device (uploaded or computed), D*H*W*2 floats each */
+asv_status asv_get_flow(asv_ctx *ctx, float *fwd, float *bwd);
 /* seed table, Kp x 12 floats: x, y, z, L, a, b, M00, M01, M02, M11, M12, M22 */
 asv_status asv_get_seeds(asv_ctx *ctx, float *out);
 asv_status asv_set_seeds(asv_ctx *ctx, const float *in, int Kp);
