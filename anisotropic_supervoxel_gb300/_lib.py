@@ -63,6 +63,13 @@ class ServerStats(ctypes.Structure):
                 ("slots", c_int), ("sessions", c_int)]
 
 
+class Eval(ctypes.Structure):
+    _fields_ = [("undersegmentation", ctypes.c_double), ("segmentation_accuracy", ctypes.c_double),
+                ("boundary_recall", ctypes.c_double), ("mean_duration", ctypes.c_double),
+                ("supervoxels", c_int), ("truth_segments", c_int), ("truth_boundary", ctypes.c_longlong),
+                ("recalled", ctypes.c_longlong)]
+
+
 class SynthParams(ctypes.Structure):
     _fields_ = [("W", c_int), ("H", c_int), ("frame0", c_int), ("nframes", c_int),
                 ("n_ellipses", c_int), ("noise_sigma", c_float), ("vmax", c_float),
@@ -101,6 +108,7 @@ SIGNATURES = {
     "asv_get_labels": (c_int, [c_void_p, c_void_p]),
     "asv_get_raw_labels": (c_int, [c_void_p, c_void_p]),
     "asv_get_flow": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "asv_evaluate": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_void_p]),
     "asv_get_seeds": (c_int, [c_void_p, c_void_p]),
     "asv_set_seeds": (c_int, [c_void_p, c_void_p, c_int]),
     "asv_get_lab": (c_int, [c_void_p, c_void_p]),
@@ -131,6 +139,7 @@ SIGNATURES = {
     "asv_stream_push": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, P(c_int)]),
     # include/asv_host.h
     "asv_synth_clip": (c_int, [P(SynthParams), c_void_p, c_void_p, c_void_p]),
+    "asv_synth_truth": (c_int, [P(SynthParams), c_void_p]),
     "asv_preprocess_frame": (c_int, [c_void_p, c_int, c_int, c_void_p]),
     "asv_write_labels_txt": (c_int, [c_char_p, c_void_p, c_int, c_int, c_int]),
     "asv_write_render_ppm": (c_int, [c_char_p, c_void_p, c_int, c_int, c_int, c_int]),

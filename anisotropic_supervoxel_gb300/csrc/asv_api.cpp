@@ -8,6 +8,7 @@
 #include "asv_internal.h"
 #include "asv_connect.cuh"
 #include "asv_flow.cuh"
+#include "asv_eval.cuh"
 #include "asv_stream.cuh"
 
 #include <cuda_runtime.h>
@@ -498,6 +499,19 @@ static asv_status read_post(asv_ctx *ctx)
 // ---------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------
+// device buffers of one evaluation, freed on return
+struct EvalBuffers {
+    std::vector<void *> p;
+    ~EvalBuffers() { for (void *q : p) cudaFree(q); }
+    template <typename T> cudaError_t get(T **out, size_t n)
+    {
+        void *q = nullptr;
+        cudaError_t e = cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T));
+        if (e == cudaSuccess) { p.push_back(q); *out = (T *)q; }
+        return e;
+    }
+};
+
 extern "C" {
 
 void asv_config_default(asv_config *cfg)
@@ -951,6 +965,91 @@ asv_status asv_enforce_connectivity_labels(asv_ctx *ctx, const int32_t *labels, 
     if (st != ASV_OK) return st;
     CK(cudaMemcpyAsync(in, labels, sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice, ctx->st));
     return run_connect(ctx, in, out, cc, W, H, D, supsz, labels_out, label_num);
+}
+
+asv_status asv_evaluate(asv_ctx *ctx, const int32_t *labels, const int32_t *truth, int W, int H, int D,
+                        asv_eval *out)
+{
+    if (!ctx) return ASV_ERR_BAD_ARG;
+    if (!labels || !truth || !out || W < 1 || H < 1 || D < 1 || (long long)W * H * D >= (1LL << 31))
+        return fail(ctx, ASV_ERR_BAD_ARG, "need labels, truth, out and W,H,D >= 1 with W*H*D < 2^31");
+    cudaSetDevice(ctx->cfg.device);
+    const long long n = (long long)W * H * D;
+    cudaStream_t st = ctx->st;
+    EvalBuffers b;
+    int32_t *lab, *gt;
+    int *meta;
+    if (b.get(&lab, n) != cudaSuccess || b.get(&gt, n) != cudaSuccess || b.get(&meta, 4) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ctx, ASV_ERR_OOM, "cudaMalloc: evaluation buffers");
+    }
+    CK(cudaMemcpyAsync(lab, labels, sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(gt, truth, sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
+    int hm[3];
+    if (asv_launch_eval_range(lab, gt, n, meta, st) != 0) return cuda_fail(ctx, cudaGetLastError(), "eval range");
+    CK(cudaMemcpyAsync(hm, meta, sizeof(hm), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (hm[2]) return fail(ctx, ASV_ERR_BAD_ARG, "labels must lie in [-1, 32767) and truth ids in [0, 4096)");
+    const int rows = hm[0] + 2, NG = hm[1] + 1;
+    unsigned *cnt;
+    int *zmin, *zmax;
+    uint8_t *sb;
+    unsigned long long *tot;
+    if (b.get(&cnt, (size_t)rows * NG) != cudaSuccess || b.get(&zmin, rows) != cudaSuccess ||
+        b.get(&zmax, rows) != cudaSuccess || b.get(&sb, n) != cudaSuccess || b.get(&tot, 2) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ctx, ASV_ERR_OOM, "cudaMalloc: evaluation counts");
+    }
+    if (asv_launch_eval(lab, gt, W, H, D, rows, NG, cnt, zmin, zmax, sb, tot, st) != 0)
+        return cuda_fail(ctx, cudaGetLastError(), "evaluation kernels");
+    std::vector<unsigned> c((size_t)rows * NG);
+    std::vector<int> z0(rows), z1(rows);
+    unsigned long long t[2];
+    CK(cudaMemcpyAsync(c.data(), cnt, sizeof(unsigned) * c.size(), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(z0.data(), zmin, sizeof(int) * rows, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(z1.data(), zmax, sizeof(int) * rows, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(t, tot, sizeof(t), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    // sizes, argmax assignment, then the measures (sums in truth-id order)
+    std::vector<long long> ssz(rows, 0), gsz(NG, 0), cover(NG, 0), under(NG, 0);
+    std::vector<int> arg(rows, -1);
+    for (int s = 0; s < rows; s++)
+        for (int g = 0; g < NG; g++) {
+            const unsigned v = c[(size_t)s * NG + g];
+            ssz[s] += v;
+            gsz[g] += v;
+            if (v && (arg[s] < 0 || v > c[(size_t)s * NG + arg[s]])) arg[s] = g;
+        }
+    for (int s = 0; s < rows; s++)
+        for (int g = 0; g < NG; g++)
+            if (c[(size_t)s * NG + g]) under[g] += ssz[s];
+    for (int s = 0; s < rows; s++)
+        if (arg[s] >= 0) cover[arg[s]] += c[(size_t)s * NG + arg[s]];
+    double ue = 0.0, sa = 0.0;
+    int ng = 0;
+    for (int g = 0; g < NG; g++)
+        if (gsz[g]) {
+            ue += (double)(under[g] - gsz[g]) / (double)gsz[g];
+            sa += (double)cover[g] / (double)gsz[g];
+            ng++;
+        }
+    int nsv = 0;
+    double dur = 0.0;
+    for (int s = 0; s < rows; s++)
+        if (ssz[s]) {
+            nsv++;
+            if (s > 0) dur += (double)(z1[s] - z0[s] + 1);   // durations of labels >= 0 only
+        }
+    out->undersegmentation = ng ? ue / ng : 0.0;
+    out->segmentation_accuracy = ng ? sa / ng : 0.0;
+    out->boundary_recall = t[0] ? (double)t[1] / (double)t[0] : 1.0;
+    const int nlab = nsv - (ssz[0] ? 1 : 0);
+    out->mean_duration = nlab ? dur / nlab : 0.0;
+    out->supervoxels = nsv;
+    out->truth_segments = ng;
+    out->truth_boundary = (long long)t[0];
+    out->recalled = (long long)t[1];
+    return ASV_OK;
 }
 
 asv_status asv_segment_clip(asv_ctx *ctx, const uint8_t *rgb, const float *fwd, const float *bwd,

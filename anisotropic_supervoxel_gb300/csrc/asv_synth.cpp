@@ -102,7 +102,7 @@ inline void drift(const Scene &s, long f, double *ox, double *oy)
     *oy = 0.5 * s.p->drift_amp * std::sin(0.5 * w);
 }
 
-void render_frame(const Scene &s, long f, uint8_t *rgb, float *fwd, float *bwd)
+void render_frame(const Scene &s, long f, uint8_t *rgb, float *fwd, float *bwd, int32_t *ids = nullptr)
 {
     const asv_synth_params *p = s.p;
     const int W = p->W, H = p->H, n = (int)s.e.size();
@@ -138,6 +138,7 @@ void render_frame(const Scene &s, long f, uint8_t *rgb, float *fwd, float *bwd)
         for (int x = 0; x < W; x++) {
             size_t q = (size_t)y * W + x;
             int t = top[q];
+            if (ids) ids[q] = t >= 0 ? t : n;   // ground truth: the ellipse on top, n = background
             double col[3];
             if (t >= 0) {
                 for (int k = 0; k < 3; k++) col[k] = s.e[t].rgb[k];
@@ -180,6 +181,21 @@ extern "C" int asv_synth_clip(const asv_synth_params *p, uint8_t *rgb, float *fw
     for (int i = 0; i < p->nframes; i++)
         render_frame(s, (long)p->frame0 + i, rgb + 3 * fr * i, fwd ? fwd + 2 * fr * i : nullptr,
                      bwd ? bwd + 2 * fr * i : nullptr);
+    return 0;
+}
+
+extern "C" int asv_synth_truth(const asv_synth_params *p, int32_t *ids)
+{
+    if (!p || !ids || p->W < 1 || p->H < 1 || p->nframes < 1 || p->n_ellipses < 0 || p->frame0 < 0)
+        return -1;
+    Scene s;
+    build_scene(p, &s);
+    const size_t fr = (size_t)p->W * p->H;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int i = 0; i < p->nframes; i++) {
+        std::vector<uint8_t> rgb(3 * fr);
+        render_frame(s, (long)p->frame0 + i, rgb.data(), nullptr, nullptr, ids + fr * i);
+    }
     return 0;
 }
 

@@ -32,6 +32,19 @@ def synth_clip(W, H, D, n_ellipses=12, noise_sigma=5.0, vmax=3.0, jitter=0.0, dr
     return rgb, fwd, bwd
 
 
+def synth_truth(W, H, D, n_ellipses=12, noise_sigma=5.0, vmax=3.0, jitter=0.0, drift_amp=0.0,
+                drift_period=60.0, seed=1, frame0=0):
+    """Ground-truth ids [D,H,W] int32 of synth_clip with the same arguments:
+    the ellipse on top of each pixel, n_ellipses for the background."""
+    lib = _lib.load()
+    ids = np.empty((D, H, W), np.int32)
+    p = SynthParams(W, H, frame0, D, n_ellipses, noise_sigma, vmax, jitter, drift_amp,
+                    drift_period, seed)
+    if lib.asv_synth_truth(ctypes.byref(p), _ptr(ids)) != 0:
+        raise ValueError("bad synthetic clip parameters")
+    return ids
+
+
 def config(variant=_lib.VARIANT_PLAIN, lloyd_iters=20, full_ladder=0, middlebury=0,
            density_adjust=1, device=0, stream=None, hbm_budget=0, use_graph=1, instrument=0,
            jfa_zrun=0):
@@ -156,6 +169,16 @@ class Image:
         self._ck(self.lib.asv_enforce_connectivity_labels(self.h, _ptr(labels), W, H, D, int(supsz), _ptr(out),
                                                           ctypes.byref(n)))
         return out, n.value
+
+    def evaluate(self, labels, truth):
+        """asv_evaluate: LIBSVX-style measures of labels [D,H,W] against truth ids;
+        returns a dict."""
+        labels = np.ascontiguousarray(labels, np.int32)
+        truth = np.ascontiguousarray(truth, np.int32)
+        D, H, W = labels.shape
+        e = _lib.Eval()
+        self._ck(self.lib.asv_evaluate(self.h, _ptr(labels), _ptr(truth), W, H, D, ctypes.byref(e)))
+        return {k: getattr(e, k) for k, _ in _lib.Eval._fields_}
 
     def autotune(self):
         """asv_autotune: times the Lloyd loop at JFA tile depths 4..32, keeps the

@@ -45,7 +45,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="clip_320x240x85",
                     choices=["clip_320x240x85", "clip_240x160x30", "batch16", "stream_720p",
-                             "serve_mix", "connect_320x240x85", "pipeline_320x240x85"])
+                             "serve_mix", "connect_320x240x85", "pipeline_320x240x85",
+                             "quality_320x240x85"])
     ap.add_argument("--requests", type=int, default=160, help="serve_mix: requests in the run")
     ap.add_argument("--rate", type=float, default=40.0, help="serve_mix: mean arrivals per second")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -716,6 +717,50 @@ def run_pipeline(args):
            "note": "flow by this library's Farneback implementation (OpenCV's is not available)"})
 
 
+def run_quality(args):
+    """LIBSVX-style quality of the 320x240x85 clip's supervoxels against the
+    generator's ground truth (asv_evaluate), with the exact generating flow
+    and with the device optical flow; value = evaluation throughput."""
+    import torch
+
+    import anisotropic_supervoxel_gb300 as asv
+    from anisotropic_supervoxel_gb300 import workloads
+    torch.cuda.set_device(0)
+    w = workloads.CLIP_320x240x85
+    rgb, fwd, bwd = workloads.make_clip(w)
+    truth = asv.synth_truth(w["W"], w["H"], w["D"], n_ellipses=w["n_ellipses"], noise_sigma=w["noise_sigma"],
+                            vmax=w["vmax"], jitter=w["jitter"], seed=w["seed"])
+    n = rgb.shape[0] * rgb.shape[1] * rgb.shape[2]
+    img = asv.Image(lloyd_iters=w["iters"])
+    given = img.segment(rgb, fwd, bwd, w["K"])
+    img.init_gpu(rgb, w["K"])
+    img.compute_flow()
+    img.initialization()
+    img.seed_matrix()
+    img.RGB2LAB()
+    img.run_lloyd()
+    computed = img.labels()
+    conn, _ = img.enforce_connectivity()
+    for _ in range(args.warmup):
+        img.evaluate(given, truth)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        q_given = img.evaluate(given, truth)
+    dt = (time.perf_counter() - t0) / args.steps
+    q_flow = img.evaluate(computed, truth)
+    q_conn = img.evaluate(conn, truth)
+    img.close()
+    _line(args, n / dt / 1e6, dt * 1e3,
+          {"workload": "quality_320x240x85_K1000_I15", "parallelism": "replicas1",
+           "l2": "labels and truth (52 MB) uploaded every step"},
+          {"metric": "Mvoxel/s of supervoxel evaluation (LIBSVX-style measures)", "unit": "Mvoxel/s",
+           "dtype": "int32",
+           "quality": {"generating_flow": q_given, "device_flow": q_flow,
+                       "generating_flow_connectivity_enforced": q_conn},
+           "e2e": {"value": n / dt / 1e6, "unit": "Mvoxel/s", "h2d_bytes_per_step": int(8 * n),
+                   "d2h_bytes_per_step": 0}})
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -730,6 +775,8 @@ def main():
         run_connect(args)
     elif args.workload == "pipeline_320x240x85":
         run_pipeline(args)
+    elif args.workload == "quality_320x240x85":
+        run_quality(args)
     else:
         run_ours(args)
 

@@ -201,6 +201,36 @@ asv_status asv_enforce_connectivity(asv_ctx *ctx, int supsz, int32_t *labels_out
 asv_status asv_enforce_connectivity_labels(asv_ctx *ctx, const int32_t *labels, int W, int H, int D,
                                            int supsz, int32_t *labels_out, int *label_num);
 
+/* ---- evaluation --------------------------------------------------------- */
+
+/* Supervoxel quality against a ground-truth segmentation, as the LIBSVX
+ * benchmark the reference is evaluated with (README.md:26-28; Xu & Corso,
+ * CVPR 2012).  LIBSVX's code is not available to this library; these are
+ * the definitions computed (n_sg = voxels of supervoxel s in truth segment
+ * g, |s| and |g| the sizes, means over the truth segments present):
+ *   undersegmentation    mean_g (sum_{s: n_sg > 0} |s| - |g|) / |g|
+ *   segmentation_accuracy mean_g sum_{s: argmax_g' n_sg' = g} n_sg / |g|
+ *                        (ties to the smaller truth id)
+ *   boundary_recall      truth boundary voxels (a 6-neighbour in another
+ *                        truth segment) with a supervoxel boundary voxel in
+ *                        their 3x3x3 neighbourhood, over all of them
+ *   mean_duration        mean over labels >= 0 of last - first frame + 1
+ * Label -1 counts as one more supervoxel in the other measures.  labels: D*H*W int32 in
+ * [-1, 32767); truth: D*H*W int32 in [0, 4096); both host arrays. */
+typedef struct asv_eval {
+    double undersegmentation;
+    double segmentation_accuracy;
+    double boundary_recall;
+    double mean_duration;
+    int supervoxels;            /* distinct labels present (with -1 if present) */
+    int truth_segments;         /* distinct truth ids present */
+    long long truth_boundary;   /* truth boundary voxels */
+    long long recalled;         /* ... with a supervoxel boundary within one voxel */
+} asv_eval;
+
+asv_status asv_evaluate(asv_ctx *ctx, const int32_t *labels, const int32_t *truth, int W, int H, int D,
+                        asv_eval *out);
+
 /* ---- state access ------------------------------------------------------ */
 asv_status asv_get_info(asv_ctx *ctx, asv_info *info);
 asv_status asv_get_labels(asv_ctx *ctx, int32_t *out);     /* post-processed */

@@ -38,6 +38,10 @@ typedef struct asv_synth_params {
 /* rgb: nframes*H*W*3; fwd, bwd: nframes*H*W*2 (either may be NULL). */
 int asv_synth_clip(const asv_synth_params *p, uint8_t *rgb, float *fwd, float *bwd);
 
+/* Ground truth of the same frames: per pixel the index of the ellipse on
+ * top, n_ellipses for the background (nframes*H*W int32). */
+int asv_synth_truth(const asv_synth_params *p, int32_t *ids);
+
 /* Render::cvMat2TexureInput (GPU-AS/Render.cpp:354-359): 3x3 Gaussian blur
  * (sigma 0 -> [1,2,1]/4 separable, border reflect-101, rounded half up),
  * BGR -> RGB and vertical flip, for one frame stored top row first. */

@@ -354,3 +354,24 @@ def test_round_half_up_fp32_form():
         got = (np.where(f - r >= np.float32(0.5), r + np.float32(1), r) + np.float32(0)).astype(np.float32)
     same = (want.view(np.uint32) == got.view(np.uint32)) | (np.isnan(want) & np.isnan(got))
     assert same.all()
+
+
+def test_evaluate_known_answers():
+    """The quality measures on a hand-checked case: truth = left/right halves
+    of a 4x4x2 volume, supervoxels = top/bottom halves."""
+    from oracle import evaluate as ev
+    truth = np.zeros((2, 4, 4), np.int32)
+    truth[:, :, 2:] = 1
+    labels = np.zeros((2, 4, 4), np.int32)
+    labels[:, 2:, :] = 1
+    r = ev.evaluate(labels, truth)
+    # each truth half (16 voxels) meets both supervoxels (16 each): (32 - 16) / 16 = 1
+    assert r["undersegmentation"] == 1.0
+    # each supervoxel is split 8/8: argmax ties go to truth 0, which gets 16 of 16
+    assert r["segmentation_accuracy"] == (16 / 16 + 0 / 16) / 2
+    assert r["mean_duration"] == 2.0 and r["supervoxels"] == 2 and r["truth_segments"] == 2
+    # truth boundary: columns 1 and 2 (16 voxels); supervoxel boundary rows 1 and 2 cross them
+    assert r["truth_boundary"] == 16 and r["recalled"] == 16
+    same = ev.evaluate(truth, truth)
+    assert same["undersegmentation"] == 0.0 and same["segmentation_accuracy"] == 1.0
+    assert same["boundary_recall"] == 1.0
