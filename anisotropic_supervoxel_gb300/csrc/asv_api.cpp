@@ -1057,7 +1057,9 @@ asv_status asv_segment_clip(asv_ctx *ctx, const uint8_t *rgb, const float *fwd, 
 {
     asv_status s;
     if ((s = asv_init_gpu(ctx, rgb, W, H, D, K)) != ASV_OK) return s;
-    if ((s = asv_upload_flow(ctx, fwd, bwd)) != ASV_OK) return s;
+    if (!fwd && !bwd) s = asv_compute_flow(ctx);             // no flow given: compute it here
+    else s = asv_upload_flow(ctx, fwd, bwd);
+    if (s != ASV_OK) return s;
     if ((s = asv_initialization(ctx)) != ASV_OK) return s;
     if ((s = asv_seed_matrix(ctx)) != ASV_OK) return s;
     if ((s = asv_rgb2lab(ctx)) != ASV_OK) return s;
@@ -1430,7 +1432,8 @@ asv_status asv_stream_push(asv_ctx *ctx, const uint8_t *rgb, const float *fwd, c
     auto &m = ctx->sm;
     if (!m.on) return fail(ctx, ASV_ERR_STATE, "no stream: call asv_stream_begin first");
     if (m.next >= m.nb) return fail(ctx, ASV_ERR_STATE, "the stream is finished");
-    if (!rgb || !fwd || !bwd || !labels_out) return fail(ctx, ASV_ERR_BAD_ARG, "NULL buffer");
+    if (!rgb || !labels_out || (!fwd) != (!bwd)) return fail(ctx, ASV_ERR_BAD_ARG, "NULL buffer");
+    const bool device_flow = !fwd;                                  // both NULL: flow computed here
     cudaSetDevice(ctx->cfg.device);
     const int b = m.next;
     const int Db = m.iv[2 * b + 1] - m.iv[2 * b];
@@ -1448,8 +1451,32 @@ asv_status asv_stream_push(asv_ctx *ctx, const uint8_t *rgb, const float *fwd, c
     }
     const size_t nnew = (size_t)(Db - z0) * WH;
     CK(cudaMemcpyAsync(d.rgb + 3 * z0 * WH, rgb, 3 * nnew, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(d.fwd + z0 * WH, fwd, 8 * nnew, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(d.bwd + z0 * WH, bwd, 8 * nnew, cudaMemcpyHostToDevice, st));
+    if (!device_flow) {
+        CK(cudaMemcpyAsync(d.fwd + z0 * WH, fwd, 8 * nnew, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(d.bwd + z0 * WH, bwd, 8 * nnew, cudaMemcpyHostToDevice, st));
+    } else {
+        // the block's flow from its own frames, as the streaming program does
+        // per block.  Pairs within the overlap frames were computed by the
+        // previous block (same two frames, same flow) and came along with the
+        // shift; the pairs touching a new frame are computed here: frames
+        // z0-1 .. Db-1, keeping the backward flow of frame z0-1.  The last
+        // frame's forward flow is not read by the metric.
+        const int zf = z0 > 0 ? z0 - 1 : 0;
+        const size_t need = asv_flow_scratch_bytes(m.W, m.H, Db - zf);
+        if (ctx->fl_bytes < need) {
+            if (ctx->fl) { cudaFree(ctx->fl); ctx->fl = nullptr; ctx->fl_bytes = 0; }
+            cudaError_t e = cudaMalloc(&ctx->fl, need);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                ctx->fl = nullptr;
+                return fail(ctx, ASV_ERR_OOM, "cudaMalloc: optical-flow scratch");
+            }
+            ctx->fl_bytes = need;
+        }
+        if (asv_launch_flow(d.rgb + 3 * zf * WH, m.W, m.H, Db - zf, d.fwd + zf * WH, d.bwd + zf * WH, ctx->fl,
+                            st, zf > 0) != 0)
+            return cuda_fail(ctx, cudaGetLastError(), "optical-flow kernels");
+    }
 
     // new seeds of the block: grid + density placement (Render.cpp:376-379, :429-432)
     SegHost h;

@@ -101,12 +101,27 @@ __global__ void k_cc_union(const int32_t *__restrict__ lab, int *par, int W, int
     }
 }
 
-// par[v] = root; component sizes at the roots
+// root of x by reading only: after the union kernel no links change, so the
+// walk ends at the true root
+__device__ __forceinline__ int cc_root(const int *par, int x, int *err)
+{
+    for (int it = 0; it < CC_SPIN_LIMIT; it++) {
+        const int p = __ldcg(par + x);
+        if (p == x) return x;
+        x = p;
+    }
+    atomicOr(err, 1);
+    return x;
+}
+
+// par[v] = root; component sizes at the roots.  Only thread v writes par[v]:
+// a path-halving write by another thread could land after it and leave an
+// ancestor that is not the root.
 __global__ void k_cc_flatten(int *par, int *cnt, long long n, int *err)
 {
     const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= n) return;
-    const int r = cc_find(par, (int)v, err);
+    const int r = cc_root(par, (int)v, err);
     par[v] = r;
     atomicAdd(cnt + r, 1);
 }

@@ -249,7 +249,7 @@ __global__ void k_fl_up(const float *__restrict__ coarse, int Wc, int Hc, float 
 
 // level-0 flow of the pairs into the clip's interleaved fwd / bwd volumes
 __global__ void k_fl_store(const float *__restrict__ flow, int W, int H, int D, float2 *__restrict__ fwd,
-                           float2 *__restrict__ bwd)
+                           float2 *__restrict__ bwd, int keep_first_bwd)
 {
     const long long fr = (long long)W * H, vox = fr * D, mplane = fr * 2 * (D - 1);
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -266,7 +266,7 @@ __global__ void k_fl_store(const float *__restrict__ flow, int W, int H, int D, 
         b = make_float2(flow[e], flow[mplane + e]);
     }
     fwd[t] = f;
-    bwd[t] = b;
+    if (z > 0 || !keep_first_bwd) bwd[t] = b;
 }
 
 // ---------------------------------------------------------------------------
@@ -354,7 +354,7 @@ static float *fl_carve(unsigned char *&p, size_t floats)
 static unsigned fl_blocks(long long n) { return (unsigned)((n + FL_T - 1) / FL_T); }
 
 int asv_launch_flow(const uint8_t *rgb, int W, int H, int D, float2 *fwd, float2 *bwd, void *scratch,
-                    cudaStream_t st)
+                    cudaStream_t st, int keep_first_bwd)
 {
     if (D < 2) return -1;
     // filter constants: computed once (thread-safe static), copied to this
@@ -398,6 +398,6 @@ int asv_launch_flow(const uint8_t *rgb, int W, int H, int D, float2 *fwd, float2
             k_fl_box_solve<<<tiles, 256, 0, st>>>(M, flow[k], w, h, P);
         }
     }
-    k_fl_store<<<fl_blocks((long long)fr0 * D), FL_T, 0, st>>>(flow[0], W, H, D, fwd, bwd);
+    k_fl_store<<<fl_blocks((long long)fr0 * D), FL_T, 0, st>>>(flow[0], W, H, D, fwd, bwd, keep_first_bwd);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

@@ -306,7 +306,7 @@ asv_status asv_server_open_session(asv_server *s, int W, int H, int D_all, int K
 asv_status asv_server_submit(asv_server *s, const asv_request *req, long long *id)
 {
     if (!s || !req || !id) return ASV_ERR_BAD_ARG;
-    if (!req->rgb || !req->fwd || !req->bwd || !req->labels_out) return ASV_ERR_BAD_ARG;
+    if (!req->rgb || !req->labels_out || (!req->fwd) != (!req->bwd)) return ASV_ERR_BAD_ARG;
     auto q = std::make_unique<Req>();
     q->r = *req;
     q->t_submit = Clock::now();

@@ -310,13 +310,15 @@ class Stream(Image):
         self._ck(self.lib.asv_stream_info_get(self.h, ctypes.byref(i)))
         return i
 
-    def push(self, rgb, fwd, bwd):
-        """rgb [n,H,W,3] uint8, fwd/bwd [n,H,W,2] float32: the next block's new frames.
+    def push(self, rgb, fwd=None, bwd=None):
+        """rgb [n,H,W,3] uint8, fwd/bwd [n,H,W,2] float32: the next block's new frames
+        (fwd and bwd None: the block's flow is computed on the device).
         Returns (first frame index, labels [done,H,W] int32)."""
         inf = self.info()
         rgb = np.ascontiguousarray(rgb, np.uint8)
-        fwd = np.ascontiguousarray(fwd, np.float32)
-        bwd = np.ascontiguousarray(bwd, np.float32)
+        if fwd is not None:
+            fwd = np.ascontiguousarray(fwd, np.float32)
+            bwd = np.ascontiguousarray(bwd, np.float32)
         if rgb.shape[0] != inf.frames_needed:
             raise ValueError(f"block {inf.next_block} needs {inf.frames_needed} new frames")
         D = inf.block_end - inf.block_start
@@ -379,25 +381,31 @@ class Server:
         return rid.value
 
     def submit_clip(self, rgb, fwd, bwd, K):
+        """fwd and bwd None: the clip's flow is computed on the device"""
         rgb = np.ascontiguousarray(rgb, np.uint8)
-        fwd = np.ascontiguousarray(fwd, np.float32)
-        bwd = np.ascontiguousarray(bwd, np.float32)
+        if fwd is not None:
+            fwd = np.ascontiguousarray(fwd, np.float32)
+            bwd = np.ascontiguousarray(bwd, np.float32)
         D, H, W = rgb.shape[:3]
         out = np.empty((D, H, W), np.int32)
-        req = _lib.Request(_lib.REQ_CLIP, 0, W, H, D, K, _ptr(rgb).value, _ptr(fwd).value,
-                           _ptr(bwd).value, _ptr(out).value)
+        req = _lib.Request(_lib.REQ_CLIP, 0, W, H, D, K, _ptr(rgb).value,
+                           _ptr(fwd).value if fwd is not None else None,
+                           _ptr(bwd).value if bwd is not None else None, _ptr(out).value)
         return self._submit(req, (rgb, fwd, bwd), out)
 
-    def submit_window(self, session, rgb, fwd, bwd):
-        """the next block's new frames of a session (asv_stream_push semantics)"""
+    def submit_window(self, session, rgb, fwd=None, bwd=None):
+        """the next block's new frames of a session (asv_stream_push semantics;
+        fwd and bwd None: the block's flow is computed on the device)"""
         W, H, block = self._sessions[session]
         rgb = np.ascontiguousarray(rgb, np.uint8)
-        fwd = np.ascontiguousarray(fwd, np.float32)
-        bwd = np.ascontiguousarray(bwd, np.float32)
+        if fwd is not None:
+            fwd = np.ascontiguousarray(fwd, np.float32)
+            bwd = np.ascontiguousarray(bwd, np.float32)
         # the last block of a video can reach block_size + block_size/3 - 1 frames
         out = np.empty((block + block // 3, H, W), np.int32)
         req = _lib.Request(_lib.REQ_WINDOW, session, W, H, rgb.shape[0], 0, _ptr(rgb).value,
-                           _ptr(fwd).value, _ptr(bwd).value, _ptr(out).value)
+                           _ptr(fwd).value if fwd is not None else None,
+                           _ptr(bwd).value if bwd is not None else None, _ptr(out).value)
         return self._submit(req, (rgb, fwd, bwd), out)
 
     def wait(self, rid):

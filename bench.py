@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--workload", default="clip_320x240x85",
                     choices=["clip_320x240x85", "clip_240x160x30", "batch16", "stream_720p",
                              "serve_mix", "connect_320x240x85", "pipeline_320x240x85",
-                             "quality_320x240x85"])
+                             "quality_320x240x85", "stream_720p_flow"])
     ap.add_argument("--requests", type=int, default=160, help="serve_mix: requests in the run")
     ap.add_argument("--rate", type=float, default=40.0, help="serve_mix: mean arrivals per second")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -468,7 +468,7 @@ def run_batch16(args):
            "clocks": clk, "gpu_launches": int(launches * args.steps)})
 
 
-def run_stream_720p(args):
+def run_stream_720p(args, device_flow=False):
     """1280x720 video, 900 frames, 30-frame windows with 10-frame overlap, on
     one resident streaming context; per-window latency = asv_stream_push wall
     time (new frames up from pinned memory, the window's Lloyd loop, finished
@@ -498,7 +498,10 @@ def run_stream_720p(args):
         rgb, fwd, bwd = _pinned(rgb), _pinned(fwd), _pinned(bwd)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        st.push(rgb, fwd, bwd)
+        if device_flow:
+            st.push(rgb)                       # the block's flow computed on the device
+        else:
+            st.push(rgb, fwd, bwd)
         dt = time.perf_counter() - t0
         if b >= args.warmup:
             lat.append(dt * 1e3)
@@ -509,14 +512,16 @@ def run_stream_720p(args):
     st.close()
     value = vox_it / t_all / 1e6
     _line(args, value, statistics.mean(lat),
-          {"workload": "stream_1280x720x900_w30o10", "K_window": w["K_window"],
+          {"workload": "stream_1280x720x900_w30o10" + ("_device_flow" if device_flow else ""),
+           "K_window": w["K_window"],
            "seeds_num_100": s100, "lloyd_iters": w["iters"], "variant": "stream",
            "parallelism": "replicas1", "l2": "inputs larger than L2 (each window 27.6 M voxels)"},
           {"latency_ms": {"p50": _pct(lat, 50), "p99": _pct(lat, 99), "max": max(lat),
                           "windows": len(lat), "target_p99": 33.0},
            "block_Kp_mean": statistics.mean(kps),
            "e2e": {"value": value, "unit": UNIT,
-                   "h2d_bytes_per_step": int(W * H * 20 * 19), "d2h_bytes_per_step": int(W * H * 20 * 4)},
+                   "h2d_bytes_per_step": int(W * H * 20 * (3 if device_flow else 19)),
+                   "d2h_bytes_per_step": int(W * H * 20 * 4)},
            "clocks": clk})
 
 
@@ -769,6 +774,8 @@ def main():
         run_batch16(args)
     elif args.workload == "stream_720p":
         run_stream_720p(args)
+    elif args.workload == "stream_720p_flow":
+        run_stream_720p(args, device_flow=True)
     elif args.workload == "serve_mix":
         run_serve_mix(args)
     elif args.workload == "connect_320x240x85":

@@ -178,7 +178,8 @@ asv_status asv_run_lloyd(asv_ctx *ctx);
 asv_status asv_autotune(asv_ctx *ctx, int *zrun);
 
 /* Convenience: init_gpu + upload_flow + initialization + seed_matrix +
- * RGB2LAB + run_lloyd + labels, the plain per-clip form of Render::run. */
+ * RGB2LAB + run_lloyd + labels, the plain per-clip form of Render::run.
+ * fwd and bwd both NULL: asv_compute_flow instead of upload_flow. */
 asv_status asv_segment_clip(asv_ctx *ctx, const uint8_t *rgb, const float *fwd,
                             const float *bwd, int W, int H, int D, int K,
                             int32_t *labels_out);
@@ -307,8 +308,11 @@ asv_status asv_stream_info_get(asv_ctx *ctx, asv_stream_info *info);
  * (streamGPU-AS/Render.cpp:348-569).  rgb / fwd / bwd: the block's new
  * frames (frames_needed of them, same layouts as asv_init_gpu and
  * asv_upload_flow; fwd of a frame is its flow to the next frame of the
- * video).  labels_out: the video-wide labels of the block's finished frames
- * [block_start, block_start + *done_frames), W*H*done_frames int32. */
+ * video).  fwd and bwd both NULL: the block's flow is computed on the
+ * device from its frames (asv_compute_flow's method), as the streaming
+ * program computes it per block.  labels_out: the video-wide labels of the
+ * block's finished frames [block_start, block_start + *done_frames),
+ * W*H*done_frames int32. */
 asv_status asv_stream_push(asv_ctx *ctx, const uint8_t *rgb, const float *fwd, const float *bwd,
                            int32_t *labels_out, int *done_frames);
 
@@ -336,7 +340,7 @@ typedef struct asv_request {
     int W, H, D, K;       /* clip requests: sizes and requested seeds */
     const uint8_t *rgb;   /* host inputs, valid until the request completes; for a window,
                              the block's new frames (asv_stream_push) */
-    const float *fwd, *bwd;
+    const float *fwd, *bwd;  /* both NULL: flow computed on the device */
     int32_t *labels_out;  /* host output: clip labels (D*H*W) or the window's finished frames
                              (room for W*H*(block_size + block_size/3) int32: the last
                              block of a video can be that long) */

@@ -49,3 +49,17 @@ def test_volumes_match_oracle(asv, orc, shape, kind):
     want, m = orc.enforce_connectivity(labels, supsz)
     assert n == m
     assert np.array_equal(got, want)
+
+
+def test_repeated_runs_are_identical(asv, orc):
+    """Many tiny segments, 40 runs: the union-find flattening must leave every
+    voxel at its root in every run (a path-halving write landing after a
+    voxel's own flatten once left an ancestor in about 1 run in 14)."""
+    rng = np.random.default_rng(73)
+    labels = rng.integers(-1, 12, (12, 50, 70)).astype(np.int32)
+    supsz = labels.size // 200
+    want, m = orc.enforce_connectivity(labels, supsz)
+    with asv.Image(lloyd_iters=1) as img:
+        for _ in range(40):
+            got, n = img.enforce_connectivity_labels(labels, supsz)
+            assert n == m and np.array_equal(got, want)

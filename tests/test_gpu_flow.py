@@ -58,3 +58,39 @@ def test_segmentation_with_device_flow_is_deterministic(asv):
             out.append(img.labels())
     assert np.array_equal(out[0], out[1])
     assert (out[0] >= 0).all()
+
+
+def test_stream_with_device_flow_matches_oracle(asv, orc):
+    """Streaming with the block's flow computed on the device equals the
+    CPU restatement of the streaming form fed with the restated flow (each
+    frame pair's flow depends only on its two frames)."""
+    from oracle import flow as ofl
+    W, H, D, s100, iters = 48, 40, 75, 200, 4
+    rgb, _, _ = asv.synth_clip(W, H, D, n_ellipses=6, noise_sigma=3.0, vmax=2.0, jitter=0.3, drift_amp=2.0,
+                               drift_period=40.0, seed=7)
+    fwd, bwd = ofl.compute_flow(rgb)
+    st = asv.Stream(W, H, D, seeds_num_100=s100, lloyd_iters=iters)
+    got = np.full((D, H, W), -7, np.int32)
+    for _ in range(st.info().blocks):
+        inf = st.info()
+        a = inf.block_end - inf.frames_needed
+        f0, lab = st.push(rgb[a:inf.block_end])
+        got[f0:f0 + lab.shape[0]] = lab
+    st.close()
+    want, _ = orc.run_stream(rgb, fwd, bwd, seeds_num_100=s100, iters=iters, nthreads=8)
+    assert np.array_equal(got, want)
+
+
+def test_clip_without_flow_uses_device_flow(asv):
+    rgb, _, _ = asv.synth_clip(64, 48, 6, n_ellipses=5, noise_sigma=3.0, seed=4)
+    with asv.Image(lloyd_iters=3) as a:
+        a.init_gpu(rgb, 100)
+        a.compute_flow()
+        a.initialization()
+        a.seed_matrix()
+        a.RGB2LAB()
+        a.run_lloyd()
+        want = a.labels()
+    with asv.Server(max_slots=1, lloyd_iters=3) as srv:
+        got, _, _ = srv.wait(srv.submit_clip(rgb, None, None, 100))
+    assert np.array_equal(got, want)
