@@ -143,6 +143,12 @@ SIGNATURES = {
     "asv_preprocess_frame": (c_int, [c_void_p, c_int, c_int, c_void_p]),
     "asv_write_labels_txt": (c_int, [c_char_p, c_void_p, c_int, c_int, c_int]),
     "asv_write_render_ppm": (c_int, [c_char_p, c_void_p, c_int, c_int, c_int, c_int]),
+    "asv_png_info": (c_int, [c_char_p, P(c_int), P(c_int)]),
+    "asv_png_read_bgr": (c_int, [c_char_p, c_void_p, c_int, c_int]),
+    "asv_png_read_frames_bgr": (c_int, [P(c_char_p), c_int, c_int, c_int, c_void_p]),
+    "asv_png_write_rgb": (c_int, [c_char_p, c_void_p, c_int, c_int]),
+    "asv_render_rgb": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_void_p]),
+    "asv_write_render_png": (c_int, [c_char_p, c_void_p, c_int, c_int, c_int, c_int, c_int]),
 }
 
 _LIB = None

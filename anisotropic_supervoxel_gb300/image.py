@@ -7,6 +7,7 @@ host buffers in and labels out.  Everything runs on the CUDA path of
 libasv.so; there is no CPU fallback.
 """
 import ctypes
+import os
 
 import numpy as np
 
@@ -257,6 +258,18 @@ class Image:
         self.run_lloyd()
         return self.labels()
 
+    def segment_folder(self, folder, K):
+        """Render::run from a folder of PNG frames (GPU-AS/Render.cpp:151-243):
+        the sorted frames decoded on the host, preprocessing and optical flow
+        on the device, then the plain sequence.  Returns post-processed labels."""
+        self.init_gpu_bgr(read_frames(list_frames(folder)), K)
+        self.compute_flow()
+        self.initialization()
+        self.seed_matrix()
+        self.RGB2LAB()
+        self.run_lloyd()
+        return self.labels()
+
 
 class Batch(Image):
     """Many clips of uneven size in one context: every stage one launch over all
@@ -441,6 +454,78 @@ def write_render_ppm(prefix, labels, n_labels):
     lab = np.ascontiguousarray(labels, np.int32)
     if _lib.load().asv_write_render_ppm(prefix.encode(), _ptr(lab), W, H, D, n_labels) != 0:
         raise OSError(f"cannot write {prefix}*.ppm")
+
+
+_PNG_ERRORS = {-1: "bad argument", -2: "file I/O error", -3: "malformed PNG", -4: "unsupported PNG",
+               -5: "frame size differs"}
+
+
+def _png_ck(st, what):
+    if st != 0:
+        raise (OSError if st == -2 else ValueError)(f"{what}: {_PNG_ERRORS.get(st, st)}")
+
+
+def png_info(path):
+    """(W, H) from a PNG file's header"""
+    W, H = ctypes.c_int(), ctypes.c_int()
+    _png_ck(_lib.load().asv_png_info(os.fsencode(path), ctypes.byref(W), ctypes.byref(H)), path)
+    return W.value, H.value
+
+
+def read_png(path):
+    """cv::imread(path, 1) of a PNG frame: [H, W, 3] uint8 BGR, top row first."""
+    W, H = png_info(path)
+    out = np.empty((H, W, 3), np.uint8)
+    _png_ck(_lib.load().asv_png_read_bgr(os.fsencode(path), _ptr(out), W, H), path)
+    return out
+
+
+def list_frames(folder):
+    """The PNG frames of a folder in sorted order (Render::run sorts the file
+    list, GPU-AS/Render.cpp:151-153)."""
+    names = sorted(f for f in os.listdir(folder) if f.lower().endswith(".png"))
+    if not names:
+        raise ValueError(f"no PNG frames in {folder}")
+    return [os.path.join(folder, f) for f in names]
+
+
+def read_frames(paths, out=None):
+    """Frames of one size decoded on all host threads: [D, H, W, 3] uint8 BGR
+    (into `out`, e.g. a pinned buffer, when given)."""
+    paths = list(paths)
+    W, H = png_info(paths[0])
+    if out is None:
+        out = np.empty((len(paths), H, W, 3), np.uint8)
+    elif out.shape != (len(paths), H, W, 3) or out.dtype != np.uint8 or not out.flags.c_contiguous:
+        raise ValueError(f"out must be a contiguous uint8 array of shape {(len(paths), H, W, 3)}")
+    arr = (ctypes.c_char_p * len(paths))(*[os.fsencode(p) for p in paths])
+    _png_ck(_lib.load().asv_png_read_frames_bgr(arr, len(paths), W, H, _ptr(out)), "frames")
+    return out
+
+
+def write_png(path, rgb):
+    """8-bit RGB image [H, W, 3], top row first."""
+    rgb = np.ascontiguousarray(rgb, np.uint8)
+    H, W, _ = rgb.shape
+    _png_ck(_lib.load().asv_png_write_rgb(os.fsencode(path), _ptr(rgb), W, H), path)
+
+
+def render_rgb(labels, n_labels):
+    """Pseudo-colour frames of print_render: [D, H, W, 3] RGB, top row first."""
+    D, H, W = labels.shape
+    lab = np.ascontiguousarray(labels, np.int32)
+    out = np.empty((D, H, W, 3), np.uint8)
+    _png_ck(_lib.load().asv_render_rgb(_ptr(lab), W, H, D, n_labels, _ptr(out)), "render")
+    return out
+
+
+def write_render_png(prefix, labels, n_labels, start_index=-1):
+    """The pseudo-colour frames as PNG files: <prefix>NNNNN.png (from 1), or
+    <prefix>SSSSS_NNNNN.png for a streaming window starting at start_index."""
+    D, H, W = labels.shape
+    lab = np.ascontiguousarray(labels, np.int32)
+    _png_ck(_lib.load().asv_write_render_png(os.fsencode(prefix), _ptr(lab), W, H, D, n_labels, start_index),
+            prefix)
 
 
 def preprocess_frame(bgr):

@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--workload", default="clip_320x240x85",
                     choices=["clip_320x240x85", "clip_240x160x30", "batch16", "stream_720p",
                              "serve_mix", "connect_320x240x85", "pipeline_320x240x85",
-                             "quality_320x240x85", "stream_720p_flow"])
+                             "pipeline_png_320x240x85", "quality_320x240x85", "stream_720p_flow"])
     ap.add_argument("--requests", type=int, default=160, help="serve_mix: requests in the run")
     ap.add_argument("--rate", type=float, default=40.0, help="serve_mix: mean arrivals per second")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -663,12 +663,15 @@ def run_connect(args):
                    "d2h_bytes_per_step": int(4 * n)}})
 
 
-def run_pipeline(args):
+def run_pipeline(args, from_png=False):
     """The whole Render::run on the device for the 320x240x85 clip: raw BGR
     frames (top row first) up from pinned memory, preprocessing
     (asv_init_gpu_bgr), the forward/backward optical flow (asv_compute_flow,
     in place of OpenCV's Farneback), seed placement, metric, LAB, the Lloyd
-    loop, labels back.  value = voxel-iterations / wall time of that step."""
+    loop, labels back.  from_png: the step starts from the 85 frames as PNG
+    files (written once, untimed) and decodes them on the host threads
+    (asv_png_read_frames_bgr, the imread loop of Render::run).
+    value = voxel-iterations / wall time of that step."""
     import numpy as np
     import torch
 
@@ -683,11 +686,22 @@ def run_pipeline(args):
     out = _pinned(np.empty((D, H, W), np.int32))
     img = asv.Image(lloyd_iters=I)
     lib = img.lib
+    tmp = tempfile.TemporaryDirectory() if from_png else None
+    paths, png_bytes, decode_ms = [], 0, []
+    if from_png:
+        for t in range(D):
+            paths.append(os.path.join(tmp.name, f"{t + 1:05d}.png"))
+            asv.write_png(paths[-1], bgr[t][..., ::-1])
+            png_bytes += os.path.getsize(paths[-1])
 
     def step(timed):
         ev = None
         if timed:
             ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        if from_png:
+            t0 = time.perf_counter()
+            asv.read_frames(paths, out=bgr)
+            decode_ms.append((time.perf_counter() - t0) * 1e3)
         img.init_gpu_bgr(bgr, K)
         st = torch.cuda.ExternalStream(img.stream(), device=torch.device("cuda", 0))
         if ev:
@@ -713,13 +727,19 @@ def run_pipeline(args):
     dt = (time.perf_counter() - t0) / args.steps
     flow_ms = statistics.mean(e[0].elapsed_time(e[1]) for e in evs)
     img.close()
+    extra = {"flow_ms": flow_ms, "flow_pairs": 2 * (D - 1),
+             "e2e": {"value": n * I / dt / 1e6, "unit": UNIT, "h2d_bytes_per_step": int(bgr.nbytes),
+                     "d2h_bytes_per_step": int(out.nbytes)},
+             "note": "flow by this library's Farneback implementation (OpenCV's is not available)"}
+    if from_png:
+        tmp.cleanup()
+        extra.update({"png_decode_ms": statistics.median(decode_ms[-args.steps:]), "png_bytes": png_bytes,
+                      "decode_threads": os.cpu_count()})
     _line(args, n * I / dt / 1e6, dt * 1e3,
-          {"workload": "pipeline_320x240x85_K1000_I15", "parallelism": "replicas1",
+          {"workload": ("pipeline_png" if from_png else "pipeline") + "_320x240x85_K1000_I15",
+           "parallelism": "replicas1",
            "l2": "inputs larger than L2 (19.6 MB frames, 80 MB working set, flow scratch 1.1 GB)"},
-          {"flow_ms": flow_ms, "flow_pairs": 2 * (D - 1),
-           "e2e": {"value": n * I / dt / 1e6, "unit": UNIT, "h2d_bytes_per_step": int(bgr.nbytes),
-                   "d2h_bytes_per_step": int(out.nbytes)},
-           "note": "flow by this library's Farneback implementation (OpenCV's is not available)"})
+          extra)
 
 
 def run_quality(args):
@@ -782,6 +802,8 @@ def main():
         run_connect(args)
     elif args.workload == "pipeline_320x240x85":
         run_pipeline(args)
+    elif args.workload == "pipeline_png_320x240x85":
+        run_pipeline(args, from_png=True)
     elif args.workload == "quality_320x240x85":
         run_quality(args)
     else:

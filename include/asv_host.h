@@ -58,6 +58,40 @@ int asv_write_labels_txt(const char *path, const int32_t *labels, int W, int H, 
 int asv_write_render_ppm(const char *prefix, const int32_t *labels, int W, int H, int D,
                          int n_labels);
 
+/* ---- PNG frames (PNG / zlib RFC 1950 / DEFLATE RFC 1951, no codec library).
+ * Return 0, or -1 bad argument, -2 file I/O, -3 malformed file (signature,
+ * chunk CRC, zlib stream, Adler-32, filter type, palette index), -4
+ * unsupported (unknown critical chunk, more than 2^28 pixels), -5 the image
+ * is not W x H. */
+
+/* Width and height from a PNG file's header. */
+int asv_png_info(const char *path, int *W, int *H);
+
+/* cv::imread(path, 1) of Render::run (GPU-AS/Render.cpp:151-157, 229-238)
+ * for a PNG frame: W*H*3 bytes BGR, top row first.  Every colour type, bit
+ * depth and Adam7 interlacing; grey replicated, alpha dropped, 16-bit
+ * samples reduced to their high byte, 1/2/4-bit grey scaled to 0..255. */
+int asv_png_read_bgr(const char *path, uint8_t *bgr, int W, int H);
+
+/* n frames of one size, decoded on all host threads, into n*W*H*3 bytes
+ * (the clip layout asv_init_gpu_bgr takes).  Returns the error of the
+ * first frame that failed. */
+int asv_png_read_frames_bgr(const char *const *paths, int n, int W, int H, uint8_t *bgr);
+
+/* 8-bit RGB PNG (W*H*3 bytes, top row first). */
+int asv_png_write_rgb(const char *path, const uint8_t *rgb, int W, int H);
+
+/* The pseudo-colour frames of asv_write_render_ppm in memory: D*W*H*3
+ * bytes RGB, top row first. */
+int asv_render_rgb(const int32_t *labels, int W, int H, int D, int n_labels, uint8_t *rgb);
+
+/* The same frames as PNG files: <prefix>NNNNN.png numbered from 1
+ * (print_render, GPU-AS/Image.cpp:1930-1932) when start_index < 0, else
+ * <prefix>SSSSS_NNNNN.png with S = start_index and N = start_index + 1 + t
+ * (output_render_all, streamGPU-AS/Render.cpp:819-821). */
+int asv_write_render_png(const char *prefix, const int32_t *labels, int W, int H, int D,
+                         int n_labels, int start_index);
+
 #ifdef __cplusplus
 }
 #endif
