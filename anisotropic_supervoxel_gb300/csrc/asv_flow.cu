@@ -85,8 +85,10 @@ __global__ void k_fl_poly_h(const float *__restrict__ img, int W, int H, int D, 
     h[2 * plane + t] = s2;
 }
 
-// vertical moments and the fit: poly planes b1, b2, a11, a22, a12
-__global__ void k_fl_poly_v(const float *__restrict__ h, int W, int H, int D, float *__restrict__ poly)
+// vertical moments and the fit: per pixel (b1, b2, a11, a22) in polyA and
+// a12 in polyB, so a bilinear tap of the expansion is two loads
+__global__ void k_fl_poly_v(const float *__restrict__ h, int W, int H, int D, float4 *__restrict__ polyA,
+                            float *__restrict__ polyB)
 {
     const long long plane = (long long)W * H * D;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -107,13 +109,15 @@ __global__ void k_fl_poly_v(const float *__restrict__ h, int W, int H, int D, fl
         m[4] += vvg * h0;
         m[5] += vg * h1;
     }
+    float r[5];
 #pragma unroll
     for (int k = 0; k < 5; k++) {
-        float r = 0.f;
+        r[k] = 0.f;
 #pragma unroll
-        for (int e = 0; e < 6; e++) r += c_fl_ginv[k][e] * m[e];
-        poly[k * plane + t] = k == 4 ? 0.5f * r : r;
+        for (int e = 0; e < 6; e++) r[k] += c_fl_ginv[k][e] * m[e];
     }
+    polyA[t] = make_float4(r[0], r[1], r[2], r[3]);
+    polyB[t] = 0.5f * r[4];
 }
 
 // frame pair p: source and destination frames (forward pairs first)
@@ -123,105 +127,145 @@ __device__ __forceinline__ void fl_pair(int p, int D, int &src, int &dst)
     else { src = p - (D - 1) + 1; dst = src - 1; }
 }
 
-// the per-pixel products A^T A (g11, g12, g22) and A^T db (h1, h2)
-__global__ void k_fl_update(const float *__restrict__ poly, const float *__restrict__ flow, int W, int H, int D,
-                            int P, float *__restrict__ M)
+// the per-pixel products A^T A (g11, g12, g22) and A^T db (h1, h2) at pixel
+// (x, y) with the current flow (dx, dy), from the expansions sA/sB of the
+// source frame and dA/dB of the destination frame; zero when x + d falls
+// outside the frame
+__device__ __forceinline__ void fl_matrix(const float4 *__restrict__ sA, const float *__restrict__ sB,
+                                          const float4 *__restrict__ dA, const float *__restrict__ dB, int W,
+                                          int H, int x, int y, float dx, float dy, float o[5])
 {
-    const long long fr = (long long)W * H, pplane = fr * D, mplane = fr * P;
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= mplane) return;
-    const int pr = (int)(t / fr);
-    const int pix = (int)(t - pr * fr), y = pix / W, x = pix - y * W;
-    int src, dst;
-    fl_pair(pr, D, src, dst);
-    const float dx = flow[t], dy = flow[mplane + t];
+#pragma unroll
+    for (int k = 0; k < 5; k++) o[k] = 0.f;
     const float qx = (float)x + dx, qy = (float)y + dy;
-    float o[5] = { 0.f, 0.f, 0.f, 0.f, 0.f };
-    if (qx >= 0.f && qy >= 0.f && qx <= (float)(W - 1) && qy <= (float)(H - 1)) {
-        const int x0 = min((int)qx, W - 2 < 0 ? 0 : W - 2), y0 = min((int)qy, H - 2 < 0 ? 0 : H - 2);
-        const int x1 = min(x0 + 1, W - 1), y1 = min(y0 + 1, H - 1);
-        const float fx = qx - (float)x0, fy = qy - (float)y0;
-        const float w00 = (1.f - fx) * (1.f - fy), w01 = fx * (1.f - fy), w10 = (1.f - fx) * fy, w11 = fx * fy;
-        const long long s = fr * src + pix, d0 = fr * dst;
-        const long long i00 = d0 + (long long)y0 * W + x0, i01 = d0 + (long long)y0 * W + x1;
-        const long long i10 = d0 + (long long)y1 * W + x0, i11 = d0 + (long long)y1 * W + x1;
-        float q[5];
-#pragma unroll
-        for (int k = 0; k < 5; k++) {
-            const float *P5 = poly + k * pplane;
-            q[k] = w00 * P5[i00] + w01 * P5[i01] + w10 * P5[i10] + w11 * P5[i11];
-        }
-        const float a11 = 0.5f * (poly[2 * pplane + s] + q[2]);
-        const float a22 = 0.5f * (poly[3 * pplane + s] + q[3]);
-        const float a12 = 0.5f * (poly[4 * pplane + s] + q[4]);
-        const float db1 = -0.5f * (q[0] - poly[s]) + a11 * dx + a12 * dy;
-        const float db2 = -0.5f * (q[1] - poly[pplane + s]) + a12 * dx + a22 * dy;
-        o[0] = a11 * a11 + a12 * a12;
-        o[1] = a11 * a12 + a12 * a22;
-        o[2] = a12 * a12 + a22 * a22;
-        o[3] = a11 * db1 + a12 * db2;
-        o[4] = a12 * db1 + a22 * db2;
-    }
-#pragma unroll
-    for (int k = 0; k < 5; k++) M[k * mplane + t] = o[k];
+    if (!(qx >= 0.f && qy >= 0.f && qx <= (float)(W - 1) && qy <= (float)(H - 1))) return;
+    const int x0 = min((int)qx, W - 2 < 0 ? 0 : W - 2), y0 = min((int)qy, H - 2 < 0 ? 0 : H - 2);
+    const int x1 = min(x0 + 1, W - 1), y1 = min(y0 + 1, H - 1);
+    const float fx = qx - (float)x0, fy = qy - (float)y0;
+    const float w00 = (1.f - fx) * (1.f - fy), w01 = fx * (1.f - fy), w10 = (1.f - fx) * fy, w11 = fx * fy;
+    const int s = y * W + x;                                   // frames hold < 2^31 pixels
+    const int i00 = y0 * W + x0, i01 = y0 * W + x1, i10 = y1 * W + x0, i11 = y1 * W + x1;
+    const float4 t00 = __ldg(dA + i00), t01 = __ldg(dA + i01), t10 = __ldg(dA + i10), t11 = __ldg(dA + i11);
+    const float u00 = __ldg(dB + i00), u01 = __ldg(dB + i01), u10 = __ldg(dB + i10), u11 = __ldg(dB + i11);
+    const float4 sa = __ldg(sA + s);
+    const float sb = __ldg(sB + s);
+    float q[5];
+    q[0] = w00 * t00.x + w01 * t01.x + w10 * t10.x + w11 * t11.x;
+    q[1] = w00 * t00.y + w01 * t01.y + w10 * t10.y + w11 * t11.y;
+    q[2] = w00 * t00.z + w01 * t01.z + w10 * t10.z + w11 * t11.z;
+    q[3] = w00 * t00.w + w01 * t01.w + w10 * t10.w + w11 * t11.w;
+    q[4] = w00 * u00 + w01 * u01 + w10 * u10 + w11 * u11;
+    const float a11 = 0.5f * (sa.z + q[2]);
+    const float a22 = 0.5f * (sa.w + q[3]);
+    const float a12 = 0.5f * (sb + q[4]);
+    const float db1 = -0.5f * (q[0] - sa.x) + a11 * dx + a12 * dy;
+    const float db2 = -0.5f * (q[1] - sa.y) + a12 * dx + a22 * dy;
+    o[0] = a11 * a11 + a12 * a12;
+    o[1] = a11 * a12 + a12 * a22;
+    o[2] = a12 * a12 + a22 * a22;
+    o[3] = a11 * db1 + a12 * db2;
+    o[4] = a12 * db1 + a22 * db2;
 }
 
-// 13x13 box sums of the five matrix planes and the 2x2 solve, per 32x32
-// tile of one frame pair: each plane's tile plus a 6-pixel halo (zero
-// outside the image) goes to shared memory, rows are summed along x, the row
-// sums along y (both in ascending index order, so the sums equal those of
-// separate x and y passes), and each thread solves its four pixels.
-#define FB_T 32
-__global__ void __launch_bounds__(256) k_fl_box_solve(const float *__restrict__ M, float *__restrict__ flow,
-                                                      int W, int H, int P)
+// One iteration for a TW x TH tile of one frame pair: the five matrix planes
+// of the tile and its 6-pixel halo are computed from the flow `fin` straight
+// into shared memory (zero outside the frame), summed over the 13x13 window
+// -- rows along x, then the row sums along y, both in ascending index order,
+// so the sums equal those of separate x and y passes -- and each pixel's 2x2
+// system is solved into `fout`.  fin and fout are separate buffers: halo
+// pixels read flow that neighbouring tiles overwrite.
+template <int TW, int TH, int NT>
+__global__ void __launch_bounds__(NT) k_fl_iter(const float4 *__restrict__ polyA, const float *__restrict__ polyB,
+                                                const float *__restrict__ fin, float *__restrict__ fout, int W,
+                                                int H, int D, int P)
 {
-    __shared__ float S[FB_T + 2 * FL_BOX][FB_T + 2 * FL_BOX + 1];
-    __shared__ float T[FB_T + 2 * FL_BOX][FB_T + 1];
+    constexpr int RPT = TH / (NT / 32);              // output rows per thread
+    static_assert(TW % 32 == 0 && RPT >= 1 && RPT * (NT / 32) == TH, "tile shape");
+    extern __shared__ float fl_sm[];
+    constexpr int RW = TW + 2 * FL_BOX, RH = TH + 2 * FL_BOX, SP = RW + 1, TP = TW + 1;
+    float *S = fl_sm;                                  // [5][RH][SP]
+    float *T = fl_sm + 5 * RH * SP;                    // [RH][TP]
     const long long fr = (long long)W * H, mplane = fr * P;
-    const int tiles_x = (W + FB_T - 1) / FB_T, tiles_y = (H + FB_T - 1) / FB_T;
+    const int tiles_x = (W + TW - 1) / TW, tiles_y = (H + TH - 1) / TH;
     const int pr = blockIdx.x / (tiles_x * tiles_y);
     const int rem = blockIdx.x - pr * tiles_x * tiles_y;
-    const int x0 = (rem % tiles_x) * FB_T, y0 = (rem / tiles_x) * FB_T;
-    const int tx = threadIdx.x % FB_T, ty = threadIdx.x / FB_T;          // 32 x 8 threads
-    constexpr int R = FB_T + 2 * FL_BOX;
-    float acc[4][5];
+    const int x0 = (rem % tiles_x) * TW, y0 = (rem / tiles_x) * TH;
+    int src, dst;
+    fl_pair(pr, D, src, dst);
+    const float4 *sA = polyA + fr * src, *dA = polyA + fr * dst;
+    const float *sB = polyB + fr * src, *dB = polyB + fr * dst;
+    const float *fx_in = fin + fr * pr, *fy_in = fin + mplane + fr * pr;
+    for (int i = threadIdx.x; i < RW * RH; i += NT) {
+        const int r = i / RW, q = i - r * RW;
+        const int gy = y0 - FL_BOX + r, gx = x0 - FL_BOX + q;
+        float o[5] = { 0.f, 0.f, 0.f, 0.f, 0.f };
+        if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+            const int e = gy * W + gx;
+            fl_matrix(sA, sB, dA, dB, W, H, gx, gy, __ldg(fx_in + e), __ldg(fy_in + e), o);
+        }
+#pragma unroll
+        for (int c = 0; c < 5; c++) S[(c * RH + r) * SP + q] = o[c];
+    }
+    __syncthreads();
+    const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;            // 32 x NT/32 threads
+    float acc[TW / 32][RPT][5];
+    // window sums several at a time from registers: a thread loads the
+    // values of adjacent windows once (horizontal: four windows, lanes on
+    // rows, so a warp's loads fall in distinct banks; vertical: RPT rows)
 #pragma unroll
     for (int c = 0; c < 5; c++) {
-        const float *src = M + c * mplane + fr * pr;
-        for (int i = threadIdx.x; i < R * R; i += blockDim.x) {
-            const int r = i / R, q = i - r * R;
-            const int gy = y0 - FL_BOX + r, gx = x0 - FL_BOX + q;
-            S[r][q] = (gx >= 0 && gx < W && gy >= 0 && gy < H) ? src[(long long)gy * W + gx] : 0.f;
+        const float *Sc = S + c * RH * SP;
+        for (int i = threadIdx.x; i < RH * (TW / 4); i += NT) {
+            const int g = i / RH, r = i - g * RH, q = 4 * g;
+            float w[16];
+#pragma unroll
+            for (int k = 0; k < 16; k++) w[k] = Sc[r * SP + q + k];
+#pragma unroll
+            for (int m = 0; m < 4; m++) {
+                float v = 0.f;
+#pragma unroll
+                for (int k = 0; k <= 2 * FL_BOX; k++) v += w[m + k];
+                T[r * TP + q + m] = v;
+            }
         }
         __syncthreads();
-        for (int i = threadIdx.x; i < R * FB_T; i += blockDim.x) {
-            const int r = i / FB_T, q = i - r * FB_T;
-            float v = 0.f;
 #pragma unroll
-            for (int k = 0; k <= 2 * FL_BOX; k++) v += S[r][q + k];
-            T[r][q] = v;
-        }
-        __syncthreads();
+        for (int a = 0; a < TW / 32; a++) {
+            const int q = tx + 32 * a;
+            float w[RPT + 2 * FL_BOX];
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const int r = ty + 8 * j;
-            float v = 0.f;
+            for (int k = 0; k < RPT + 2 * FL_BOX; k++) w[k] = T[(RPT * ty + k) * TP + q];
 #pragma unroll
-            for (int k = 0; k <= 2 * FL_BOX; k++) v += T[r + k][tx];
-            acc[j][c] = v;
+            for (int j = 0; j < RPT; j++) {
+                float v = 0.f;
+#pragma unroll
+                for (int k = 0; k <= 2 * FL_BOX; k++) v += w[j + k];
+                acc[a][j][c] = v;
+            }
         }
         __syncthreads();
     }
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
-        const int x = x0 + tx, y = y0 + ty + 8 * j;
-        if (x >= W || y >= H) continue;
-        const float g11 = acc[j][0], g12 = acc[j][1], g22 = acc[j][2], h1 = acc[j][3], h2 = acc[j][4];
-        const float idet = 1.f / (g11 * g22 - g12 * g12 + 1e-3f);
-        const long long e = fr * pr + (long long)y * W + x;
-        flow[e] = (g22 * h1 - g12 * h2) * idet;
-        flow[mplane + e] = (g11 * h2 - g12 * h1) * idet;
-    }
+    for (int a = 0; a < TW / 32; a++)
+#pragma unroll
+        for (int j = 0; j < RPT; j++) {
+            const int x = x0 + tx + 32 * a, y = y0 + RPT * ty + j;
+            if (x >= W || y >= H) continue;
+            const float g11 = acc[a][j][0], g12 = acc[a][j][1], g22 = acc[a][j][2];
+            const float h1 = acc[a][j][3], h2 = acc[a][j][4];
+            const float idet = 1.f / (g11 * g22 - g12 * g12 + 1e-3f);
+            const long long e = fr * pr + (long long)y * W + x;
+            fout[e] = (g22 * h1 - g12 * h2) * idet;
+            fout[mplane + e] = (g11 * h2 - g12 * h1) * idet;
+        }
+}
+
+#define FL_TW 64
+#define FL_TH 32
+#define FL_NT 512
+static constexpr size_t fl_iter_smem(int tw, int th)
+{
+    return sizeof(float) * (size_t)(5 * (th + 2 * FL_BOX) * (tw + 2 * FL_BOX + 1) + (th + 2 * FL_BOX) * (tw + 1));
 }
 
 // flow of level k from level k+1: bilinear, scaled by the size ratio
@@ -296,7 +340,7 @@ size_t asv_flow_scratch_bytes(int W, int H, int D)
         b += (size_t)fr * P * 2 * 4;               // flow
     }
     const long long fr0 = (long long)W * H;
-    b += (size_t)fr0 * P * 5 * 4;                  // matrices
+    b += (size_t)fr0 * P * 2 * 4;                  // second flow buffer (iterations alternate)
     return b + 64 * 256;
 }
 
@@ -367,16 +411,22 @@ int asv_launch_flow(const uint8_t *rgb, int W, int H, int D, float2 *fwd, float2
     const int L = fl_levels(W, H, Ws, Hs);
     const int P = 2 * (D - 1);
     unsigned char *p = (unsigned char *)scratch;
-    float *img[FL_MAX_LEVELS], *hm[FL_MAX_LEVELS], *poly[FL_MAX_LEVELS], *flow[FL_MAX_LEVELS];
+    float *img[FL_MAX_LEVELS], *hm[FL_MAX_LEVELS], *polyB[FL_MAX_LEVELS], *flow[FL_MAX_LEVELS];
+    float4 *polyA[FL_MAX_LEVELS];
     for (int k = 0; k < L; k++) {
         const size_t fr = (size_t)Ws[k] * Hs[k];
         img[k] = fl_carve(p, fr * D);
         hm[k] = fl_carve(p, fr * D * 3);
-        poly[k] = fl_carve(p, fr * D * 5);
+        polyA[k] = (float4 *)fl_carve(p, fr * D * 4);      // 256-byte aligned
+        polyB[k] = fl_carve(p, fr * D);
         flow[k] = fl_carve(p, fr * P * 2);
     }
     const size_t fr0 = (size_t)W * H;
-    float *M = fl_carve(p, fr0 * P * 5);
+    float *alt = fl_carve(p, fr0 * P * 2);
+    const size_t smem = fl_iter_smem(FL_TW, FL_TH);
+    if (cudaFuncSetAttribute(k_fl_iter<FL_TW, FL_TH, FL_NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+        return -1;
 
     k_fl_gray<<<fl_blocks((long long)fr0 * D), FL_T, 0, st>>>(rgb, img[0], (long long)fr0 * D);
     for (int k = 1; k < L; k++)
@@ -385,17 +435,18 @@ int asv_launch_flow(const uint8_t *rgb, int W, int H, int D, float2 *fwd, float2
     for (int k = 0; k < L; k++) {
         const long long n = (long long)Ws[k] * Hs[k] * D;
         k_fl_poly_h<<<fl_blocks(n), FL_T, 0, st>>>(img[k], Ws[k], Hs[k], D, hm[k]);
-        k_fl_poly_v<<<fl_blocks(n), FL_T, 0, st>>>(hm[k], Ws[k], Hs[k], D, poly[k]);
+        k_fl_poly_v<<<fl_blocks(n), FL_T, 0, st>>>(hm[k], Ws[k], Hs[k], D, polyA[k], polyB[k]);
     }
     for (int k = L - 1; k >= 0; k--) {
         const int w = Ws[k], h = Hs[k];
         const long long mplane = (long long)w * h * P;
         if (k == L - 1) cudaMemsetAsync(flow[k], 0, sizeof(float) * mplane * 2, st);
         else k_fl_up<<<fl_blocks(mplane), FL_T, 0, st>>>(flow[k + 1], Ws[k + 1], Hs[k + 1], flow[k], w, h, P);
-        for (int it = 0; it < 10; it++) {
-            k_fl_update<<<fl_blocks(mplane), FL_T, 0, st>>>(poly[k], flow[k], w, h, D, P, M);
-            const unsigned tiles = (unsigned)(((w + FB_T - 1) / FB_T) * ((h + FB_T - 1) / FB_T) * P);
-            k_fl_box_solve<<<tiles, 256, 0, st>>>(M, flow[k], w, h, P);
+        const unsigned tiles = (unsigned)(((w + FL_TW - 1) / FL_TW) * ((h + FL_TH - 1) / FL_TH) * P);
+        for (int it = 0; it < 10; it++) {                 // even count: the result ends in flow[k]
+            const float *fin = (it & 1) ? alt : flow[k];
+            float *fout = (it & 1) ? flow[k] : alt;
+            k_fl_iter<FL_TW, FL_TH, FL_NT><<<tiles, FL_NT, smem, st>>>(polyA[k], polyB[k], fin, fout, w, h, D, P);
         }
     }
     k_fl_store<<<fl_blocks((long long)fr0 * D), FL_T, 0, st>>>(flow[0], W, H, D, fwd, bwd, keep_first_bwd);
