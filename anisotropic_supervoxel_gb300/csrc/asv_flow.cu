@@ -128,18 +128,19 @@ __device__ __forceinline__ void fl_pair(int p, int D, int &src, int &dst)
 }
 
 // the per-pixel products A^T A (g11, g12, g22) and A^T db (h1, h2) at pixel
-// (x, y) with the current flow (dx, dy), from the expansions sA/sB of the
-// source frame and dA/dB of the destination frame; zero when x + d falls
-// outside the frame
+// (x, y) of the frame with the current flow (dx, dy), from the expansions
+// sA/sB of the source frame and dA/dB of the destination frame; zero when
+// x + d falls outside the frame
 __device__ __forceinline__ void fl_matrix(const float4 *__restrict__ sA, const float *__restrict__ sB,
                                           const float4 *__restrict__ dA, const float *__restrict__ dB, int W,
                                           int H, int x, int y, float dx, float dy, float o[5])
 {
-#pragma unroll
-    for (int k = 0; k < 5; k++) o[k] = 0.f;
+    // no early exit: the sample indices are clamped into the frame whatever
+    // the flow (also NaN), every load is issued, and the result is zeroed by
+    // a select, so a thread's evaluations overlap their loads
     const float qx = (float)x + dx, qy = (float)y + dy;
-    if (!(qx >= 0.f && qy >= 0.f && qx <= (float)(W - 1) && qy <= (float)(H - 1))) return;
-    const int x0 = min((int)qx, W - 2 < 0 ? 0 : W - 2), y0 = min((int)qy, H - 2 < 0 ? 0 : H - 2);
+    const bool inside = qx >= 0.f && qy >= 0.f && qx <= (float)(W - 1) && qy <= (float)(H - 1);
+    const int x0 = min(max((int)qx, 0), W - 2 < 0 ? 0 : W - 2), y0 = min(max((int)qy, 0), H - 2 < 0 ? 0 : H - 2);
     const int x1 = min(x0 + 1, W - 1), y1 = min(y0 + 1, H - 1);
     const float fx = qx - (float)x0, fy = qy - (float)y0;
     const float w00 = (1.f - fx) * (1.f - fy), w01 = fx * (1.f - fy), w10 = (1.f - fx) * fy, w11 = fx * fy;
@@ -160,11 +161,11 @@ __device__ __forceinline__ void fl_matrix(const float4 *__restrict__ sA, const f
     const float a12 = 0.5f * (sb + q[4]);
     const float db1 = -0.5f * (q[0] - sa.x) + a11 * dx + a12 * dy;
     const float db2 = -0.5f * (q[1] - sa.y) + a12 * dx + a22 * dy;
-    o[0] = a11 * a11 + a12 * a12;
-    o[1] = a11 * a12 + a12 * a22;
-    o[2] = a12 * a12 + a22 * a22;
-    o[3] = a11 * db1 + a12 * db2;
-    o[4] = a12 * db1 + a22 * db2;
+    o[0] = inside ? a11 * a11 + a12 * a12 : 0.f;
+    o[1] = inside ? a11 * a12 + a12 * a22 : 0.f;
+    o[2] = inside ? a12 * a12 + a22 * a22 : 0.f;
+    o[3] = inside ? a11 * db1 + a12 * db2 : 0.f;
+    o[4] = inside ? a12 * db1 + a22 * db2 : 0.f;
 }
 
 // One iteration for a TW x TH tile of one frame pair: the five matrix planes
@@ -187,47 +188,64 @@ __global__ void __launch_bounds__(NT) k_fl_iter(const float4 *__restrict__ polyA
     float *T = fl_sm + 5 * RH * SP;                    // [RH][TP]
     const long long fr = (long long)W * H, mplane = fr * P;
     const int tiles_x = (W + TW - 1) / TW, tiles_y = (H + TH - 1) / TH;
-    const int pr = blockIdx.x / (tiles_x * tiles_y);
-    const int rem = blockIdx.x - pr * tiles_x * tiles_y;
+    // blocks take the pairs as z -> z+1, z+1 -> z, z+1 -> z+2, ...: the two
+    // pairs of a frame pair read the same two expansions while both are in L2
+    const int j = blockIdx.x / (tiles_x * tiles_y);
+    const int pr = (j & 1) ? D - 1 + (j >> 1) : (j >> 1);
+    const int rem = blockIdx.x - j * tiles_x * tiles_y;
     const int x0 = (rem % tiles_x) * TW, y0 = (rem / tiles_x) * TH;
     int src, dst;
     fl_pair(pr, D, src, dst);
     const float4 *sA = polyA + fr * src, *dA = polyA + fr * dst;
     const float *sB = polyB + fr * src, *dB = polyB + fr * dst;
     const float *fx_in = fin + fr * pr, *fy_in = fin + mplane + fr * pr;
-    for (int i = threadIdx.x; i < RW * RH; i += NT) {
-        const int r = i / RW, q = i - r * RW;
-        const int gy = y0 - FL_BOX + r, gx = x0 - FL_BOX + q;
-        float o[5] = { 0.f, 0.f, 0.f, 0.f, 0.f };
-        if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
-            const int e = gy * W + gx;
-            fl_matrix(sA, sB, dA, dB, W, H, gx, gy, __ldg(fx_in + e), __ldg(fy_in + e), o);
+    for (int i0 = threadIdx.x; i0 < RW * RH; i0 += 2 * NT) {     // two pixels per trip
+        int cell[2];
+        bool keep[2];
+        float o[2][5];
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            const int i = i0 + u * NT;
+            cell[u] = i < RW * RH ? i : 0;
+            const int r = cell[u] / RW, q = cell[u] - r * RW;
+            const int gy = y0 - FL_BOX + r, gx = x0 - FL_BOX + q;
+            keep[u] = gx >= 0 && gx < W && gy >= 0 && gy < H;       // zero outside the frame
+            const int cx = min(max(gx, 0), W - 1), cy = min(max(gy, 0), H - 1);
+            const int e = cy * W + cx;
+            fl_matrix(sA, sB, dA, dB, W, H, cx, cy, __ldg(fx_in + e), __ldg(fy_in + e), o[u]);
         }
 #pragma unroll
-        for (int c = 0; c < 5; c++) S[(c * RH + r) * SP + q] = o[c];
+        for (int u = 0; u < 2; u++) {
+            if (i0 + u * NT >= RW * RH) continue;
+            const int r = cell[u] / RW, q = cell[u] - r * RW;
+#pragma unroll
+            for (int c = 0; c < 5; c++) S[(c * RH + r) * SP + q] = keep[u] ? o[u][c] : 0.f;
+        }
     }
     __syncthreads();
     const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;            // 32 x NT/32 threads
     float acc[TW / 32][RPT][5];
     // window sums several at a time from registers: a thread loads the
-    // values of adjacent windows once (horizontal: four windows, lanes on
-    // rows, so a warp's loads fall in distinct banks; vertical: RPT rows)
+    // values of adjacent windows once (horizontal: four windows, one column
+    // group per warp with lanes on rows, so with the odd row pitches a
+    // warp's loads and stores fall in distinct banks; vertical: RPT rows)
 #pragma unroll
     for (int c = 0; c < 5; c++) {
         const float *Sc = S + c * RH * SP;
-        for (int i = threadIdx.x; i < RH * (TW / 4); i += NT) {
-            const int g = i / RH, r = i - g * RH, q = 4 * g;
-            float w[16];
+        for (int g = threadIdx.x / 32; g < TW / 4; g += NT / 32)
+            for (int r = threadIdx.x % 32; r < RH; r += 32) {
+                const int q = 4 * g;
+                float w[16];
 #pragma unroll
-            for (int k = 0; k < 16; k++) w[k] = Sc[r * SP + q + k];
+                for (int k = 0; k < 16; k++) w[k] = Sc[r * SP + q + k];
 #pragma unroll
-            for (int m = 0; m < 4; m++) {
-                float v = 0.f;
+                for (int m = 0; m < 4; m++) {
+                    float v = 0.f;
 #pragma unroll
-                for (int k = 0; k <= 2 * FL_BOX; k++) v += w[m + k];
-                T[r * TP + q + m] = v;
+                    for (int k = 0; k <= 2 * FL_BOX; k++) v += w[m + k];
+                    T[r * TP + q + m] = v;
+                }
             }
-        }
         __syncthreads();
 #pragma unroll
         for (int a = 0; a < TW / 32; a++) {
