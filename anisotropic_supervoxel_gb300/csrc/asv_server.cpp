@@ -1,7 +1,8 @@
 // asv_server.cpp -- request pool on one GPU (include/asv.h, "serving").
 //
 // Clip requests wait in one FIFO; a worker thread per slot takes the first
-// request it can admit: one of its own shape (its context keeps the device
+// request it can admit (slot 0 only small clips when there are two or more
+// slots): one of its own shape (its context keeps the device
 // layout and the captured graph, no new memory), or one whose memory fits
 // the free part of the HBM budget after the worker drops its current layout.
 // Each slot's context runs on its own CUDA streams, so admitted requests
@@ -77,12 +78,20 @@ static double ms_between(Clock::time_point a, Clock::time_point b)
     return std::chrono::duration<double, std::milli>(b - a).count();
 }
 
+static bool is_small(const asv_request &r) { return (long long)r.W * r.H * r.D <= kSmallClipVoxels; }
+
+// with two or more slots, slot 0 serves small clips only: they are half of
+// a typical mix but a few per cent of its GPU time, and would otherwise
+// wait behind bursts of large clips holding every slot
+static bool small_only(const asv_server *s, int w) { return w == 0 && s->slots.size() >= 2; }
+
 // first queued request slot w can take; extra = new bytes it would need.  A
 // request of the slot's own shape among the next few is preferred (no
 // re-layout), then the first that fits the budget.
 static bool pick(asv_server *s, int w, long long *id, size_t *extra)
 {
     Slot &sl = s->slots[w];
+    const bool small = small_only(s, w);
     size_t look = s->slots.size();
     for (auto it = s->queue.begin(); it != s->queue.end() && look; ++it, --look) {
         const asv_request &r = s->reqs[*it]->r;
@@ -92,6 +101,7 @@ static bool pick(asv_server *s, int w, long long *id, size_t *extra)
     }
     for (auto it = s->queue.begin(); it != s->queue.end(); ++it) {
         Req &q = *s->reqs[*it];
+        if (small && !is_small(q.r)) continue;
         size_t need = q.bytes;
         size_t freed = sl.bytes;
         if (!s->budget || s->used - freed + need <= s->budget) {
@@ -99,6 +109,13 @@ static bool pick(asv_server *s, int w, long long *id, size_t *extra)
         }
     }
     return false;
+}
+
+// the head request does not fit in the free part of the budget
+static bool head_blocked(asv_server *s)
+{
+    if (!s->budget || s->queue.empty()) return false;
+    return s->used + s->reqs[s->queue.front()]->bytes > s->budget;
 }
 
 static size_t held_by_slots(const asv_server *s)
@@ -117,9 +134,10 @@ static void worker(asv_server *s, int w)
         size_t extra = 0;
         while (!pick(s, w, &id, &extra)) {
             if (s->stop) return;
-            if (!s->queue.empty() && sl.ctx) {
+            if (!s->queue.empty() && sl.ctx && (!small_only(s, w) || head_blocked(s))) {
                 // a queued request cannot be admitted and this slot's layout is
-                // not wanted: give its memory back so the request can fit
+                // not wanted: give its memory back so the request can fit (the
+                // small-clip slot keeps its layout unless the budget blocks)
                 asv_ctx *c = sl.ctx;
                 sl.ctx = nullptr;
                 sl.W = sl.H = sl.D = sl.K = 0;
@@ -162,7 +180,7 @@ static void worker(asv_server *s, int w)
         }
         if (st == ASV_OK) {
             const asv_request &r = q.r;
-            asv::set_stream(sl.ctx, (long long)r.W * r.H * r.D <= kSmallClipVoxels ? sl.small : sl.large);
+            asv::set_stream(sl.ctx, is_small(r) ? sl.small : sl.large);
             st = asv_segment_clip(sl.ctx, r.rgb, r.fwd, r.bwd, r.W, r.H, r.D, r.K, r.labels_out);
             if (st == ASV_OK) { sl.W = r.W; sl.H = r.H; sl.D = r.D; sl.K = r.K; }
             else { sl.W = sl.H = sl.D = sl.K = 0; }

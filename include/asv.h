@@ -353,7 +353,8 @@ typedef struct asv_server_stats {
 } asv_server_stats;
 
 /* max_slots: concurrent clip requests; hbm_budget: bytes all slots and
- * sessions together may hold (0 = no limit).  cfg applies to every slot. */
+ * sessions together may hold (0 = no limit).  cfg applies to every slot.
+ * With two or more slots, slot 0 serves clips of up to 4 Mi voxels only. */
 asv_status asv_server_create(const asv_config *cfg, int max_slots, size_t hbm_budget, asv_server **out);
 /* runs what is queued, then frees everything; no asv_server_wait may be in
  * progress on another thread.  A clip request that cannot fit beside the
