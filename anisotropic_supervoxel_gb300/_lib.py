@@ -30,7 +30,7 @@ class Config(ctypes.Structure):
     _fields_ = [("variant", c_int), ("lloyd_iters", c_int), ("full_ladder", c_int),
                 ("middlebury", c_int), ("density_adjust", c_int), ("device", c_int),
                 ("stream", c_void_p), ("hbm_budget", c_size_t), ("use_graph", c_int),
-                ("instrument", c_int), ("jfa_zrun", c_int)]
+                ("instrument", c_int), ("jfa_zrun", c_int), ("jfa_tile_blocks", c_int)]
 
 
 class Info(ctypes.Structure):

@@ -206,10 +206,31 @@ static asv_status cuda_fail(asv_ctx *c, cudaError_t e, const char *where)
         if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call);     \
     } while (0)
 
+// JFA grid: a persistent grid of the resident blocks, or one block per tile
+static int jfa_blocks_for(const asv_ctx *ctx, int tiles)
+{
+    tiles = std::max(tiles, 1);
+    return ctx->cfg.jfa_tile_blocks ? tiles : asv_jfa_grid_blocks(tiles);
+}
+
+// Device memory of a context is stream-ordered: cudaMallocAsync and
+// cudaFreeAsync on the context's stream, from the device's default memory
+// pool.  A free waits for the context's own earlier work only, so a context
+// that changes shape or is destroyed never synchronizes the device and the
+// other contexts sharing the GPU (the server's slots) keep running.  The
+// context's stream changes only after a synchronize (asv::set_stream), so a
+// buffer is always allocated, used and freed in stream order.
+static cudaError_t ctx_malloc(asv_ctx *ctx, void **p, size_t b) { return cudaMallocAsync(p, b, ctx->st); }
+
+static void ctx_free(asv_ctx *ctx, void *p)
+{
+    if (p) cudaFreeAsync(p, ctx->st);
+}
+
 static void free_layout(asv_ctx *ctx)
 {
     if (ctx->gexec) { cudaGraphExecDestroy(ctx->gexec); ctx->gexec = nullptr; }
-    for (void *p : ctx->allocs) cudaFree(p);
+    for (void *p : ctx->allocs) ctx_free(ctx, p);
     ctx->allocs.clear();
     ctx->bytes = 0;
     ctx->d = AsvDev{};
@@ -226,8 +247,8 @@ static asv_status dalloc(asv_ctx *ctx, T **p, size_t n)
     if (ctx->cfg.hbm_budget && ctx->bytes + b > ctx->cfg.hbm_budget)
         return fail(ctx, ASV_ERR_OVER_BUDGET, "allocation exceeds the configured HBM budget");
     void *q = nullptr;
-    cudaError_t e = cudaMalloc(&q, b);
-    if (e != cudaSuccess) { cudaGetLastError(); return fail(ctx, ASV_ERR_OOM, std::string("cudaMalloc: ") + cudaGetErrorString(e)); }
+    cudaError_t e = ctx_malloc(ctx, &q, b);
+    if (e != cudaSuccess) { cudaGetLastError(); return fail(ctx, ASV_ERR_OOM, std::string("cudaMallocAsync: ") + cudaGetErrorString(e)); }
     ctx->allocs.push_back(q);
     ctx->bytes += b;
     *p = (T *)q;
@@ -389,7 +410,7 @@ asv_status asv_build_layout(asv_ctx *ctx)
     asv_launch_srgb_table(d, ctx->st);
     CK(cudaGetLastError());
     d.lablut = asv_lab_table(ctx->cfg.device);
-    ctx->jfa_blocks = asv_jfa_grid_blocks(std::max(tiles, 1));
+    ctx->jfa_blocks = jfa_blocks_for(ctx, tiles);
     return ASV_OK;
 }
 
@@ -499,14 +520,17 @@ static asv_status read_post(asv_ctx *ctx)
 // ---------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------
-// device buffers of one evaluation, freed on return
+// device buffers of one evaluation, stream-ordered on the context's stream
+// and freed on return
 struct EvalBuffers {
+    asv_ctx *ctx;
     std::vector<void *> p;
-    ~EvalBuffers() { for (void *q : p) cudaFree(q); }
+    explicit EvalBuffers(asv_ctx *c) : ctx(c) {}
+    ~EvalBuffers() { for (void *q : p) ctx_free(ctx, q); }
     template <typename T> cudaError_t get(T **out, size_t n)
     {
         void *q = nullptr;
-        cudaError_t e = cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T));
+        cudaError_t e = ctx_malloc(ctx, &q, std::max<size_t>(n, 1) * sizeof(T));
         if (e == cudaSuccess) { p.push_back(q); *out = (T *)q; }
         return e;
     }
@@ -570,8 +594,9 @@ asv_status asv_destroy(asv_ctx *ctx)
     cudaSetDevice(ctx->cfg.device);
     cudaStreamSynchronize(ctx->st);
     free_layout(ctx);
-    if (ctx->cc) cudaFree(ctx->cc);
-    if (ctx->fl) cudaFree(ctx->fl);
+    ctx_free(ctx, ctx->cc);
+    ctx_free(ctx, ctx->fl);
+    cudaStreamSynchronize(ctx->st);
     for (auto e : ctx->ev) cudaEventDestroy(e);
     if (ctx->own_st) cudaStreamDestroy(ctx->st);
     delete ctx;
@@ -669,12 +694,12 @@ asv_status asv_compute_flow(asv_ctx *ctx)
     if (ctx->fl_bytes < need) {
         if (ctx->cfg.hbm_budget && ctx->bytes + ctx->cc_bytes + need > ctx->cfg.hbm_budget)
             return fail(ctx, ASV_ERR_OVER_BUDGET, "optical-flow scratch exceeds the configured HBM budget");
-        if (ctx->fl) { cudaFree(ctx->fl); ctx->fl = nullptr; ctx->fl_bytes = 0; }
-        cudaError_t e = cudaMalloc(&ctx->fl, need);
+        if (ctx->fl) { ctx_free(ctx, ctx->fl); ctx->fl = nullptr; ctx->fl_bytes = 0; }
+        cudaError_t e = ctx_malloc(ctx, &ctx->fl, need);
         if (e != cudaSuccess) {
             cudaGetLastError();
             ctx->fl = nullptr;
-            return fail(ctx, ASV_ERR_OOM, "cudaMalloc: optical-flow scratch");
+            return fail(ctx, ASV_ERR_OOM, "cudaMallocAsync: optical-flow scratch");
         }
         ctx->fl_bytes = need;
     }
@@ -854,7 +879,7 @@ static asv_status set_zrun(asv_ctx *ctx, int z)
                        ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
     ctx->d.total_tiles = tiles;
-    ctx->jfa_blocks = asv_jfa_grid_blocks(std::max(tiles, 1));
+    ctx->jfa_blocks = jfa_blocks_for(ctx, tiles);
     if (ctx->gexec) { cudaGraphExecDestroy(ctx->gexec); ctx->gexec = nullptr; }
     return ASV_OK;
 }
@@ -902,12 +927,12 @@ static asv_status connect_scratch(asv_ctx *ctx, long long n, int32_t **out, int3
     if (ctx->cc_bytes < need) {
         if (ctx->cfg.hbm_budget && ctx->bytes + need > ctx->cfg.hbm_budget)
             return fail(ctx, ASV_ERR_OVER_BUDGET, "connectivity scratch exceeds the configured HBM budget");
-        if (ctx->cc) { cudaFree(ctx->cc); ctx->cc = nullptr; ctx->cc_bytes = 0; }
-        cudaError_t e = cudaMalloc(&ctx->cc, need);
+        if (ctx->cc) { ctx_free(ctx, ctx->cc); ctx->cc = nullptr; ctx->cc_bytes = 0; }
+        cudaError_t e = ctx_malloc(ctx, &ctx->cc, need);
         if (e != cudaSuccess) {
             cudaGetLastError();
             ctx->cc = nullptr;
-            return fail(ctx, ASV_ERR_OOM, "cudaMalloc: connectivity scratch");
+            return fail(ctx, ASV_ERR_OOM, "cudaMallocAsync: connectivity scratch");
         }
         ctx->cc_bytes = need;
     }
@@ -976,12 +1001,12 @@ asv_status asv_evaluate(asv_ctx *ctx, const int32_t *labels, const int32_t *trut
     cudaSetDevice(ctx->cfg.device);
     const long long n = (long long)W * H * D;
     cudaStream_t st = ctx->st;
-    EvalBuffers b;
+    EvalBuffers b(ctx);
     int32_t *lab, *gt;
     int *meta;
     if (b.get(&lab, n) != cudaSuccess || b.get(&gt, n) != cudaSuccess || b.get(&meta, 4) != cudaSuccess) {
         cudaGetLastError();
-        return fail(ctx, ASV_ERR_OOM, "cudaMalloc: evaluation buffers");
+        return fail(ctx, ASV_ERR_OOM, "cudaMallocAsync: evaluation buffers");
     }
     CK(cudaMemcpyAsync(lab, labels, sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(gt, truth, sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
@@ -998,7 +1023,7 @@ asv_status asv_evaluate(asv_ctx *ctx, const int32_t *labels, const int32_t *trut
     if (b.get(&cnt, (size_t)rows * NG) != cudaSuccess || b.get(&zmin, rows) != cudaSuccess ||
         b.get(&zmax, rows) != cudaSuccess || b.get(&sb, n) != cudaSuccess || b.get(&tot, 2) != cudaSuccess) {
         cudaGetLastError();
-        return fail(ctx, ASV_ERR_OOM, "cudaMalloc: evaluation counts");
+        return fail(ctx, ASV_ERR_OOM, "cudaMallocAsync: evaluation counts");
     }
     if (asv_launch_eval(lab, gt, W, H, D, rows, NG, cnt, zmin, zmax, sb, tot, st) != 0)
         return cuda_fail(ctx, cudaGetLastError(), "evaluation kernels");
@@ -1464,12 +1489,12 @@ asv_status asv_stream_push(asv_ctx *ctx, const uint8_t *rgb, const float *fwd, c
         const int zf = z0 > 0 ? z0 - 1 : 0;
         const size_t need = asv_flow_scratch_bytes(m.W, m.H, Db - zf);
         if (ctx->fl_bytes < need) {
-            if (ctx->fl) { cudaFree(ctx->fl); ctx->fl = nullptr; ctx->fl_bytes = 0; }
-            cudaError_t e = cudaMalloc(&ctx->fl, need);
+            if (ctx->fl) { ctx_free(ctx, ctx->fl); ctx->fl = nullptr; ctx->fl_bytes = 0; }
+            cudaError_t e = ctx_malloc(ctx, &ctx->fl, need);
             if (e != cudaSuccess) {
                 cudaGetLastError();
                 ctx->fl = nullptr;
-                return fail(ctx, ASV_ERR_OOM, "cudaMalloc: optical-flow scratch");
+                return fail(ctx, ASV_ERR_OOM, "cudaMallocAsync: optical-flow scratch");
             }
             ctx->fl_bytes = need;
         }
@@ -1512,7 +1537,7 @@ asv_status asv_stream_push(asv_ctx *ctx, const uint8_t *rgb, const float *fwd, c
         grid[k] = make_float4(h.grid[4 * k], h.grid[4 * k + 1], h.grid[4 * k + 2], h.grid[4 * k + 3]);
     CK(cudaMemcpyAsync(d.grid, grid.data(), sizeof(float4) * Kn, cudaMemcpyHostToDevice, st));
     ctx->maxpass = h.npass;
-    ctx->jfa_blocks = asv_jfa_grid_blocks(tiles);
+    ctx->jfa_blocks = jfa_blocks_for(ctx, tiles);
 
     asv_launch_rgb2lab(d, st);                                   // new frames only (lab_from)
     CK(cudaMemsetAsync(d.dacc, 0, sizeof(unsigned long long) * d.total_seeds, st));

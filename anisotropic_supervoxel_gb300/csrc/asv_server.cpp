@@ -8,7 +8,9 @@
 // Each slot's context runs on its own CUDA streams, so admitted requests
 // overlap on the device; small clips run on a higher-priority stream than
 // large ones, and streaming windows on the device's highest priority, so the
-// block scheduler serves them first when the GPU is shared.  A streaming
+// block scheduler serves them first when the GPU is shared; the contexts
+// launch the JFA with one block per tile, so no pass holds the SMs for its
+// whole length and the priorities act between tiles.  A streaming
 // session owns a resident streaming context and a worker that runs its
 // windows in submission order.
 #include "asv.h"
@@ -237,6 +239,7 @@ asv_status asv_server_create(const asv_config *cfg, int max_slots, size_t hbm_bu
     asv_server *s = new asv_server();
     if (cfg) s->cfg = *cfg; else asv_config_default(&s->cfg);
     s->cfg.stream = nullptr;          // every slot gets its own streams
+    s->cfg.jfa_tile_blocks = 1;       // JFA blocks retire per tile: priorities can act between them
     s->budget = hbm_budget;
     s->slots.resize(max_slots);
     cudaSetDevice(s->cfg.device);

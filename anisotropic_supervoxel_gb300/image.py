@@ -48,12 +48,12 @@ def synth_truth(W, H, D, n_ellipses=12, noise_sigma=5.0, vmax=3.0, jitter=0.0, d
 
 def config(variant=_lib.VARIANT_PLAIN, lloyd_iters=20, full_ladder=0, middlebury=0,
            density_adjust=1, device=0, stream=None, hbm_budget=0, use_graph=1, instrument=0,
-           jfa_zrun=0):
+           jfa_zrun=0, jfa_tile_blocks=0):
     c = Config()
     _lib.load().asv_config_default(ctypes.byref(c))
     c.variant, c.lloyd_iters, c.full_ladder, c.middlebury = variant, lloyd_iters, full_ladder, middlebury
     c.density_adjust, c.device, c.stream, c.hbm_budget = density_adjust, device, stream, hbm_budget
-    c.use_graph, c.instrument, c.jfa_zrun = use_graph, instrument, jfa_zrun
+    c.use_graph, c.instrument, c.jfa_zrun, c.jfa_tile_blocks = use_graph, instrument, jfa_zrun, jfa_tile_blocks
     return c
 
 

@@ -593,10 +593,11 @@ def run_serve_mix(args):
             w = mix[k][1]
             ids.append((k, srv.submit_clip(*pools[k][j], w["K"])))
             vox += w["W"] * w["H"] * w["D"] * 10
-    lat = {0: [], 1: [], 2: []}
+    lat, qd = {0: [], 1: [], 2: []}, {0: [], 1: [], 2: []}
     for k, rid in ids:
-        _, ms, _ = srv.wait(rid)
+        _, ms, qms = srv.wait(rid)
         lat[k].append(ms)
+        qd[k].append(qms)
     t_end = time.perf_counter()
     clk = clocks.stop()
     st = srv.stats()
@@ -611,7 +612,8 @@ def run_serve_mix(args):
            "hbm_budget_gb": 120, "slots": 6, "sessions": n_sess, "lloyd_iters": 10,
            "parallelism": "replicas1", "l2": "inputs larger than L2"},
           {"latency_ms": {"p50": _pct(allv, 50), "p99": _pct(allv, 99),
-                          **{nm: {"p50": _pct(lat[i], 50), "p99": _pct(lat[i], 99), "n": len(lat[i])}
+                          **{nm: {"p50": _pct(lat[i], 50), "p99": _pct(lat[i], 99), "n": len(lat[i]),
+                                  "queue_p50": _pct(qd[i], 50), "queue_p99": _pct(qd[i], 99)}
                              for i, nm in enumerate(names)}},
            "requests_per_s": n / span, "failed": st.failed,
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": None,

@@ -65,6 +65,10 @@ typedef struct asv_config {
     int jfa_zrun;       /* JFA tile depth (voxels of a column per tile, walked along the
                            step's chains); 0: chosen from the clip sizes; asv_autotune
                            measures it */
+    int jfa_tile_blocks; /* 1: a JFA pass launches one block per tile, so its blocks retire
+                           after each tile and kernels on higher-priority streams get SMs
+                           between them (the server's contexts); 0: a persistent grid of
+                           the resident blocks loops over the tiles (fastest alone) */
 } asv_config;
 
 typedef struct asv_info {

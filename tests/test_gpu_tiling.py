@@ -28,3 +28,14 @@ def test_autotune_keeps_labels(asv):
         assert np.array_equal(im.labels(), want)
         im.run_lloyd()
         assert np.array_equal(im.labels(), want)
+
+
+@pytest.mark.parametrize("z", [0, 4, 32])
+def test_tile_blocks_grid_keeps_labels(asv, orc, z):
+    """One block per tile (the server's grid) instead of the persistent grid:
+    the same labels."""
+    W, H, D, K = 72, 40, 45, 220
+    rgb, fwd, bwd = small_clip(asv, W=W, H=H, D=D, seed=11, jitter=0.3, drift=1.0)
+    want, _, _, _ = orc.run_clip(rgb, fwd, bwd, K, iters=3, nthreads=8)
+    with asv.Image(lloyd_iters=3, jfa_zrun=z, jfa_tile_blocks=1) as im:
+        assert np.array_equal(im.segment(rgb, fwd, bwd, K), want)
