@@ -13,20 +13,42 @@
 
 #define EV_T 256
 
-// label ranges and bounds violations
+#define EV_RANGE_PER_THREAD 8
+
+// label ranges and bounds violations: a block reduces EV_T * 8 voxels (warp
+// reductions, then the block's warps through shared memory) and issues one
+// atomic per quantity, so the three global words see few updates
 __global__ void k_ev_range(const int32_t *__restrict__ lab, const int32_t *__restrict__ gt, long long n, int *meta)
 {
-    const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ int red[3][EV_T / 32];
+    const long long base = (long long)blockIdx.x * blockDim.x * EV_RANGE_PER_THREAD + threadIdx.x;
     int ls = -1, lg = -1, bad = 0;
-    if (v < n) {
-        ls = lab[v];
-        lg = gt[v];
-        bad = (ls < -1 || ls >= EV_MAX_LABELS || lg < 0 || lg >= EV_MAX_TRUTH) ? 1 : 0;
+#pragma unroll
+    for (int k = 0; k < EV_RANGE_PER_THREAD; k++) {
+        const long long v = base + (long long)k * blockDim.x;
+        if (v < n) {
+            const int a = lab[v], b = gt[v];
+            ls = max(ls, a);
+            lg = max(lg, b);
+            bad |= (a < -1 || a >= EV_MAX_LABELS || b < 0 || b >= EV_MAX_TRUTH) ? 1 : 0;
+        }
     }
     ls = __reduce_max_sync(0xffffffffu, ls);
     lg = __reduce_max_sync(0xffffffffu, lg);
     bad = __reduce_or_sync(0xffffffffu, bad);
+    const int w = threadIdx.x >> 5;
     if ((threadIdx.x & 31) == 0) {
+        red[0][w] = ls;
+        red[1][w] = lg;
+        red[2][w] = bad;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int i = 1; i < EV_T / 32; i++) {
+            ls = max(ls, red[0][i]);
+            lg = max(lg, red[1][i]);
+            bad |= red[2][i];
+        }
         atomicMax(meta + 0, ls);
         atomicMax(meta + 1, lg);
         if (bad) atomicOr(meta + 2, 1);
@@ -34,7 +56,8 @@ __global__ void k_ev_range(const int32_t *__restrict__ lab, const int32_t *__res
 }
 
 // overlap counts (label -1 is row 0) and per-supervoxel frame range; lanes
-// with the same (s, g) pair add once per warp
+// with the same (s, g) pair form one group, whose leader adds the group's
+// count and its frame range once
 __global__ void k_ev_overlap(const int32_t *__restrict__ lab, const int32_t *__restrict__ gt, int W, int H, int D,
                              int NG, unsigned *__restrict__ cnt, int *__restrict__ zmin, int *__restrict__ zmax)
 {
@@ -44,12 +67,14 @@ __global__ void k_ev_overlap(const int32_t *__restrict__ lab, const int32_t *__r
     const int s = in ? lab[v] + 1 : 0, g = in ? gt[v] : 0;
     const int key = in ? s * NG + g : -1;
     const unsigned grp = __match_any_sync(0xffffffffu, key);
-    const int lead = __ffs(grp) - 1;
-    if (in && (int)(threadIdx.x & 31) == lead) atomicAdd(cnt + key, (unsigned)__popc(grp));
-    if (in && s > 0) {
-        const int z = (int)(v / fr);
-        atomicMin(zmin + s, z);
-        atomicMax(zmax + s, z);
+    const unsigned z = in ? (unsigned)(v / fr) : 0u;
+    const unsigned zlo = __reduce_min_sync(grp, z), zhi = __reduce_max_sync(grp, z);
+    if (in && (int)(threadIdx.x & 31) == __ffs(grp) - 1) {
+        atomicAdd(cnt + key, (unsigned)__popc(grp));
+        if (s > 0) {
+            atomicMin(zmin + s, (int)zlo);
+            atomicMax(zmax + s, (int)zhi);
+        }
     }
 }
 
@@ -108,9 +133,22 @@ __global__ void k_ev_recall(const int32_t *__restrict__ gt, const uint8_t *__res
     }
     isb = __reduce_add_sync(0xffffffffu, isb);
     rec = __reduce_add_sync(0xffffffffu, rec);
-    if ((threadIdx.x & 31) == 0 && isb) {
-        atomicAdd(tot + 0, (unsigned long long)isb);
-        atomicAdd(tot + 1, (unsigned long long)rec);
+    __shared__ unsigned red[2][EV_T / 32];                 // then the block's warps: one atomic pair per block
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        red[0][w] = isb;
+        red[1][w] = rec;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int i = 1; i < EV_T / 32; i++) {
+            isb += red[0][i];
+            rec += red[1][i];
+        }
+        if (isb) {
+            atomicAdd(tot + 0, (unsigned long long)isb);
+            atomicAdd(tot + 1, (unsigned long long)rec);
+        }
     }
 }
 
@@ -120,7 +158,8 @@ int asv_launch_eval_range(const int32_t *lab, const int32_t *gt, long long n, in
 {
     cudaMemsetAsync(meta, 0xff, 2 * sizeof(int), st);       // -1
     cudaMemsetAsync(meta + 2, 0, sizeof(int), st);
-    k_ev_range<<<ev_blocks(n), EV_T, 0, st>>>(lab, gt, n, meta);
+    k_ev_range<<<(unsigned)((n + EV_T * EV_RANGE_PER_THREAD - 1) / (EV_T * EV_RANGE_PER_THREAD)), EV_T, 0, st>>>(
+        lab, gt, n, meta);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
