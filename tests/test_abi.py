@@ -132,3 +132,20 @@ def test_render_ppm(asv, tmp_path):
     px = np.frombuffer(data[len(b"P6\n2 2\n255\n"):], np.uint8).reshape(2, 2, 3)
     assert (px[0, 0] == 0).all()          # label -1 (row y=1 shown first) is black
     assert (px[0, 1] == px[1, 1]).all()   # both label 1
+
+
+def test_shape_limits_agree_with_oracle(asv):
+    """The library and the CPU restatement accept and refuse the same clip
+    shapes: one frame, one-pixel-wide or -high frames are refused by both."""
+    from oracle import oracle
+    lib = asv.load()
+    for (W, H, D, K) in [(40, 30, 1, 20), (1, 40, 10, 8), (40, 1, 10, 8), (1, 1, 50, 5),
+                         (40, 30, 2, 30), (2, 2, 2, 1), (64, 64, 64, 32767)]:
+        accepted = lib.asv_clip_bytes(W, H, D, K) > 0
+        rgb, fwd, bwd = asv.synth_clip(W, H, D, n_ellipses=3, noise_sigma=3.0, seed=W + H + D)
+        try:
+            oracle.run_clip(rgb, fwd, bwd, K, iters=1, nthreads=4)
+            ran = True
+        except ValueError:
+            ran = False
+        assert accepted == ran, (W, H, D, K)

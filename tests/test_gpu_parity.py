@@ -212,3 +212,23 @@ def test_clip_320x240x85_properties(asv, orc):
     labels, raw, seeds, info = orc.run_clip(rgb, fwd, bwd, w["K"] // 4, iters=w["iters"], nthreads=8)
     assert mismatch(img.raw_labels(), raw) == 0
     assert mismatch(img.labels(), labels) == 0
+
+
+EXTREMES = [
+    (40, 30, 2, 30),          # two frames: one forward and one backward flow field
+    (2, 2, 2, 1),             # one seed in a 2x2x2 clip
+    (160, 128, 8, 30000),     # K' = 29952: more seeds than a label per 6 voxels
+    (64, 64, 64, 32767),      # K' = 32736, next to the 32767-seed limit; -1 voxels remain
+]
+
+
+@pytest.mark.parametrize("W,H,D,K", EXTREMES)
+def test_clip_extremes_bit_exact(asv, orc, W, H, D, K):
+    rgb, fwd, bwd = asv.synth_clip(W, H, D, n_ellipses=3, noise_sigma=3.0, seed=W + H + D)
+    img = _gpu_clip(asv, rgb, fwd, bwd, K, 2)
+    img.run_lloyd()
+    labels, raw, seeds, info = orc.run_clip(rgb, fwd, bwd, K, iters=2, nthreads=8)
+    assert img.info().Kp == seeds.shape[0]
+    assert np.array_equal(img.raw_labels(), raw)
+    assert np.array_equal(img.labels(), labels)
+    img.close()
