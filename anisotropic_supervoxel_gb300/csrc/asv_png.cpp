@@ -530,6 +530,10 @@ int decode_png(const std::vector<uint8_t> &file, int W, int H, uint8_t *bgr)
         }
         off[p + 1] = off[p] + ((pw[p] && ph[p]) ? (size_t)ph[p] * (rowbytes(pw[p]) + 1) : 0);
     }
+    // DEFLATE expands by at most 258 bytes per 2-bit-minimum match code (about
+    // 1032:1): a header claiming more pixels than the stream can hold is refused
+    // before the buffer is allocated
+    if (off[npass] / 1032 > im.idat.size() + 64) return PNG_FORMAT;
     std::vector<uint8_t> raw(off[npass]);
     st = zlib_decode(im.idat.data(), im.idat.size(), raw.data(), raw.size());
     if (st != PNG_OK) return st;

@@ -268,6 +268,10 @@ def test_errors(tmp_path):
     bad("pal.png", pal)                                   # index 3 of a 2-entry palette
     with pytest.raises(OSError):
         asv.read_png(str(tmp_path / "missing.png"))
+    huge = _corrupt_chunk(good, b"IHDR", lambda b: struct.pack(">II", 16384, 16384) + b[8:])
+    p = _write(tmp_path, "huge.png", huge)
+    with pytest.raises(ValueError, match="malformed"):          # 2^28 pixels claimed by a tiny stream
+        asv.read_png(p)
     s2, _ = random_image(rng, 21, 10, 8, 2)
     other = _write(tmp_path, "other.png", make_png(s2, 8, 2, 0, None, None, rng))
     with pytest.raises(ValueError, match="size"):
