@@ -6,9 +6,10 @@ and noise (generator: asv_synth_clip).
 """
 import numpy as np
 
-# plain single clip: 240x160x30, 12 ellipses, sigma 5, K=200, 10 iterations
+# plain single clip: 240x160x30, 12 ellipses, sigma 5, K=200, 10 iterations, the
+# full JFA ladder (powers of two from log2 of the largest dimension, then 2, 1)
 CLIP_240x160x30 = dict(W=240, H=160, D=30, n_ellipses=12, noise_sigma=5.0, vmax=3.0,
-                       jitter=0.0, K=200, iters=10, seed=20240601)
+                       jitter=0.0, K=200, iters=10, full_ladder=1, seed=20240601)
 # single clip: 320x240x85, 30 ellipses with +-0.5 px/frame jitter, sigma 8, K=1000, 15 iterations
 CLIP_320x240x85 = dict(W=320, H=240, D=85, n_ellipses=30, noise_sigma=8.0, vmax=3.0,
                        jitter=0.5, K=1000, iters=15, seed=20240602)

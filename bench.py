@@ -148,7 +148,7 @@ def cpu_baseline(w, rgb, fwd, bwd, iters):
     from oracle import oracle
     n = os.cpu_count() or 1
     t = time.perf_counter()
-    oracle.run_clip(rgb, fwd, bwd, w["K"], iters=iters, nthreads=n)
+    oracle.run_clip(rgb, fwd, bwd, w["K"], iters=iters, nthreads=n, full_ladder=w.get("full_ladder", 0))
     dt = time.perf_counter() - t
     vox = rgb.shape[0] * rgb.shape[1] * rgb.shape[2]
     return {"value": vox * iters / dt / 1e6, "unit": UNIT, "cores": n, "kind": "port",
@@ -160,7 +160,8 @@ def cpu_baseline(w, rgb, fwd, bwd, iters):
 def config_of(w, name, N):
     return {"workload": f"{name}_K{w['K']}_I{w['iters']}", "W": w["W"], "H": w["H"], "D": w["D"],
             "K": w["K"], "lloyd_iters": w["iters"], "ellipses": w["n_ellipses"],
-            "noise_sigma": w["noise_sigma"], "jitter": w["jitter"], "jfa_ladder": "reference",
+            "noise_sigma": w["noise_sigma"], "jitter": w["jitter"],
+            "jfa_ladder": "full (log2 of the largest dimension)" if w.get("full_ladder") else "reference",
             "variant": "plain", "parallelism": f"replicas{N}",
             "l2": "flushed before every step (512 MiB write)"}
 
@@ -222,7 +223,8 @@ def run_ours(args):
             torch.distributed.barrier()
 
     # --- device-resident value ----------------------------------------------
-    img = asv.Image(lloyd_iters=I, device=local)
+    full = w.get("full_ladder", 0)
+    img = asv.Image(lloyd_iters=I, device=local, full_ladder=full)
     img.init_gpu(rgb, K)
     img.upload_flow(fwd, bwd)
     img.initialization()
@@ -257,7 +259,7 @@ def run_ours(args):
     info = img.info()
 
     # --- JFA kernel: per-launch device time (CUDA events around each pass) ----
-    prof = asv.Image(lloyd_iters=I, device=local, instrument=1, use_graph=0)
+    prof = asv.Image(lloyd_iters=I, device=local, instrument=1, use_graph=0, full_ladder=full)
     prof.init_gpu(rgb, K)
     prof.upload_flow(fwd, bwd)
     prof.initialization()
@@ -285,7 +287,7 @@ def run_ours(args):
 
     prgb, pfwd, pbwd = pinned(rgb), pinned(fwd), pinned(bwd)
     plab = torch.empty((D, H, W), dtype=torch.int32, pin_memory=True).numpy()
-    e2e = asv.Image(lloyd_iters=I, device=local)
+    e2e = asv.Image(lloyd_iters=I, device=local, full_ladder=full)
 
     def e2e_step():
         e2e.init_gpu(prgb, K)
@@ -386,6 +388,7 @@ def run_batch16(args):
     for i, c in enumerate(clips):
         b.upload(i, *c)
     b.prepare()
+    zrun = b.autotune()                 # tile depth measured on this batch (asv_autotune)
     b.synchronize()
     st = torch.cuda.ExternalStream(b.stream(), device=torch.device("cuda", 0))
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda:0")
@@ -459,6 +462,7 @@ def run_batch16(args):
           {"workload": "batch16_uneven", "clips": len(dims),
            "voxels": sum(W * H * D for W, H, D, _ in dims), "K_total": sum(d[3] for d in dims),
            "lloyd_iters": I, "variant": "plain", "parallelism": "replicas1",
+           "jfa_zrun": zrun, "tiles": "autotuned (asv_autotune over depths 4/8/16/32)",
            "l2": "flushed before every step (512 MiB write)"},
           {"e2e": {"value": vox_it * args.steps / e2e_s / 1e6, "unit": UNIT,
                    "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},

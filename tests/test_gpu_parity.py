@@ -126,15 +126,20 @@ def test_clip_bit_exact(asv, orc, W, H, D, K, iters, variant, full, dens):
                                                            info["final_label_num"])
 
 
-def test_clip_240x160x30(asv, orc):
-    """The 240x160x30 K=200 10-iteration workload, bit-exact end to end."""
+@pytest.mark.parametrize("full", [1, 0])
+def test_clip_240x160x30(asv, orc, full):
+    """The 240x160x30 K=200 10-iteration workload (its full JFA ladder, and the
+    reference ladder), bit-exact end to end."""
     from anisotropic_supervoxel_gb300 import workloads
     w = workloads.CLIP_240x160x30
+    assert w["full_ladder"] == 1
     rgb, fwd, bwd = workloads.make_clip(w)
-    img = _gpu_clip(asv, rgb, fwd, bwd, w["K"], w["iters"])
+    img = _gpu_clip(asv, rgb, fwd, bwd, w["K"], w["iters"], full_ladder=full)
     img.run_lloyd()
-    labels, raw, seeds, info = orc.run_clip(rgb, fwd, bwd, w["K"], iters=w["iters"], nthreads=8)
+    labels, raw, seeds, info = orc.run_clip(rgb, fwd, bwd, w["K"], iters=w["iters"], nthreads=8,
+                                            full_ladder=full)
     assert img.info().Kp == 187
+    assert img.info().passes == (11 if full else 7)          # [1, 128, 64, ..., 1, 2, 1] or [1, 8, 4, 2, 1, 2, 1]
     assert mismatch(img.raw_labels(), raw) == 0
     assert mismatch(img.labels(), labels) == 0
 
