@@ -43,6 +43,38 @@ __device__ __forceinline__ float asv_tie_gap(float x)
 // 1e-6 relative, i.e. below 6e-4 on the scaled L, a, b); only when a scaled
 // value lies within 4e-3 of a rounding boundary is the voxel recomputed with
 // the correctly rounded FP64 path, so the bytes equal the exact ones.
+// asv_lab_of_fp32 is the first part alone: it returns the FP32 bytes and
+// whether asv_lab_of would recompute them.
+__device__ __forceinline__ bool asv_lab_of_fp32(const float *__restrict__ tab, unsigned r, unsigned g, unsigned b,
+                                                uchar4 &out)
+{
+    float t0 = tab[r], t1 = tab[g], t2 = tab[b];
+    float X = (t0 * 0.412453f + t1 * 0.357580f) + t2 * 0.180423f;
+    float Y = (t0 * 0.212671f + t1 * 0.715160f) + t2 * 0.072169f;
+    float Z = (t0 * 0.019334f + t1 * 0.119193f) + t2 * 0.950227f;
+    float rr[3] = { X / 0.950456f, Y / 1.0f, Z / 1.088754f };
+    float f[3];
+    bool cube[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        cube[k] = rr[k] > 0.008856f;
+        if (cube[k]) f[k] = exp2f(log2f(rr[k]) * (1.0f / 3.0f));
+        else f[k] = (903.3f * rr[k] + 16.0f) / 116.0f;
+    }
+    float L = 116.0f * f[1] - 16.0f;
+    float A = 500.0f * (f[0] - f[1]);
+    float B = 200.0f * (f[1] - f[2]);
+    L = L * 2.55f; A = A + 128.0f; B = B + 128.0f;
+    const bool fix = (cube[0] || cube[1] || cube[2]) &&
+                     fminf(asv_tie_gap(L), fminf(asv_tie_gap(A), asv_tie_gap(B))) < 4e-3f;
+    float v0 = floorf(L + 0.5f), v1 = floorf(A + 0.5f), v2 = floorf(B + 0.5f);
+    v0 = fminf(fmaxf(v0, 0.0f), 255.0f);
+    v1 = fminf(fmaxf(v1, 0.0f), 255.0f);
+    v2 = fminf(fmaxf(v2, 0.0f), 255.0f);
+    out = make_uchar4((unsigned char)v0, (unsigned char)v1, (unsigned char)v2, 0);
+    return fix;
+}
+
 __device__ __forceinline__ uchar4 asv_lab_of(const float *__restrict__ tab, unsigned r, unsigned g,
                                              unsigned b)
 {
@@ -98,16 +130,43 @@ __global__ void __launch_bounds__(256) k_rgb2lab(AsvDev d)
     }
 }
 
-// The LAB bytes of all 2^24 RGB values, indexed r << 16 | g << 8 | b: built
-// once per device by asv_lab_of itself, so a lookup returns exactly what the
-// computation would (the exhaustive RGB2LAB test covers every entry).
-__global__ void __launch_bounds__(256) k_lab_table(const float *__restrict__ srgb, uchar4 *__restrict__ lut)
+// The LAB bytes of all 2^24 RGB values, indexed r << 16 | g << 8 | b, built
+// once per device in two passes: every entry in FP32, the entries near a
+// rounding tie listed (about 2 %), then those entries again by asv_lab_of
+// itself.  So a lookup returns exactly what the computation would (the
+// exhaustive RGB2LAB test covers every entry), and the FP64 recomputations
+// run in full warps instead of stalling half of all warps on one lane each.
+__global__ void __launch_bounds__(256) k_lab_table(const float *__restrict__ srgb, uchar4 *__restrict__ lut,
+                                                   unsigned *__restrict__ fix, unsigned *__restrict__ nfix)
 {
     __shared__ float tab[256];
     tab[threadIdx.x] = srgb[threadIdx.x];
     __syncthreads();
     const unsigned c = blockIdx.x * 256u + threadIdx.x;              // 65536 blocks x 256
-    lut[c] = asv_lab_of(tab, c >> 16, (c >> 8) & 255u, c & 255u);
+    uchar4 v;
+    const bool again = asv_lab_of_fp32(tab, c >> 16, (c >> 8) & 255u, c & 255u, v);
+    lut[c] = v;
+    const unsigned m = __ballot_sync(0xffffffffu, again);            // one atomic per warp
+    if (!m) return;
+    const int lane = threadIdx.x & 31;
+    unsigned at = 0;
+    if (lane == __ffs(m) - 1) at = atomicAdd(nfix, (unsigned)__popc(m));
+    at = __shfl_sync(0xffffffffu, at, __ffs(m) - 1);
+    if (again) fix[at + __popc(m & ((1u << lane) - 1u))] = c;
+}
+
+__global__ void __launch_bounds__(256) k_lab_table_fix(const float *__restrict__ srgb, uchar4 *__restrict__ lut,
+                                                       const unsigned *__restrict__ fix,
+                                                       const unsigned *__restrict__ nfix)
+{
+    __shared__ float tab[256];
+    tab[threadIdx.x] = srgb[threadIdx.x];
+    __syncthreads();
+    const unsigned n = *nfix;
+    for (unsigned i = blockIdx.x * 256u + threadIdx.x; i < n; i += gridDim.x * 256u) {
+        const unsigned c = fix[i];
+        lut[c] = asv_lab_of(tab, c >> 16, (c >> 8) & 255u, c & 255u);
+    }
 }
 
 // RGB -> LAB through the table: one 4-byte gather per voxel
@@ -971,20 +1030,27 @@ const uchar4 *asv_lab_table(int device)
     tried[device] = true;
     float *srgb = nullptr;
     uchar4 *lut = nullptr;
+    unsigned *fix = nullptr;                       // entries to recompute, then their count
     cudaStream_t st = nullptr;
     if (cudaMalloc(&srgb, 256 * sizeof(float)) != cudaSuccess ||
         cudaMalloc(&lut, sizeof(uchar4) << 24) != cudaSuccess ||
+        cudaMalloc(&fix, (sizeof(unsigned) << 24) + sizeof(unsigned)) != cudaSuccess ||
         cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
         cudaGetLastError();
         if (srgb) cudaFree(srgb);
         if (lut) cudaFree(lut);
+        if (fix) cudaFree(fix);
         return nullptr;
     }
+    unsigned *nfix = fix + (1u << 24);
+    cudaMemsetAsync(nfix, 0, sizeof(unsigned), st);
     k_srgb_table<<<1, 256, 0, st>>>(srgb);
-    k_lab_table<<<65536, 256, 0, st>>>(srgb, lut);
+    k_lab_table<<<65536, 256, 0, st>>>(srgb, lut, fix, nfix);
+    k_lab_table_fix<<<2048, 256, 0, st>>>(srgb, lut, fix, nfix);
     const bool ok = cudaStreamSynchronize(st) == cudaSuccess && cudaGetLastError() == cudaSuccess;
     cudaStreamDestroy(st);
     cudaFree(srgb);
+    cudaFree(fix);
     if (!ok) { cudaFree(lut); return nullptr; }
     tabs[device] = lut;
     return lut;
