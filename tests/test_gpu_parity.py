@@ -237,3 +237,17 @@ def test_clip_extremes_bit_exact(asv, orc, W, H, D, K):
     assert np.array_equal(img.raw_labels(), raw)
     assert np.array_equal(img.labels(), labels)
     img.close()
+
+
+@pytest.mark.parametrize("W,H,D,K", [(64, 48, 12, 60), (90, 50, 8, 120)])
+def test_clip_middlebury_bit_exact(asv, orc, W, H, D, K):
+    """middlebury = 1: base step s = floor(sqrt(W*H/K)) (GPU-AS/Image.cpp:25-29)."""
+    rgb, fwd, bwd = small_clip(asv, W, H, D, seed=W + 3 * K, jitter=0.4, drift=1.0)
+    img = _gpu_clip(asv, rgb, fwd, bwd, K, 3, middlebury=1)
+    img.run_lloyd()
+    labels, raw, seeds, info = orc.run_clip(rgb, fwd, bwd, K, iters=3, middlebury=1, nthreads=8)
+    _, g = orc.grid_seeds(W, H, D, K, middlebury=1)
+    assert img.info().s == g.s and img.info().Kp == seeds.shape[0]
+    assert np.array_equal(img.raw_labels(), raw)
+    assert np.array_equal(img.labels(), labels)
+    img.close()

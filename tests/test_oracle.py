@@ -375,3 +375,14 @@ def test_evaluate_known_answers():
     same = ev.evaluate(truth, truth)
     assert same["undersegmentation"] == 0.0 and same["segmentation_accuracy"] == 1.0
     assert same["boundary_recall"] == 1.0
+
+
+def test_middlebury_step_known_answers(orc):
+    """GPU-AS/Image.cpp:25-29: s = int(floor(pow(1.0 * W * H / K, 0.5))) for the
+    MiddleburyFlow dataset, s = int(floor(pow(N / K, 1/3))) (N / K integer) otherwise."""
+    import math
+    for (W, H, D, K) in [(64, 48, 12, 60), (90, 50, 8, 120), (640, 480, 2, 1000), (37, 23, 9, 25)]:
+        _, g = orc.grid_seeds(W, H, D, K, middlebury=1)
+        assert g.s == int(math.floor(math.pow(1.0 * W * H / K, 0.5))), (W, H, D, K)
+        _, g0 = orc.grid_seeds(W, H, D, K, middlebury=0)
+        assert g0.s == int(math.floor(math.pow((W * H * D) // K, 1.0 / 3))), (W, H, D, K)
