@@ -1,7 +1,7 @@
 /*
  * asv_oracle.h -- CPU restatement of the reference supervoxel path.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker for the CUDA path:
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle the CUDA path is tested against:
  * only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg (and
  * the `--impl reference` arm) may load it.  The product (libasv) never links
  * or calls it.

@@ -1,6 +1,6 @@
 """Compiles the reference's own GLSL shaders as C++ into
-oracle/_ref/libref_shaders.so, the checker of the CPU restatement's shader
-maths.  GLSL's vector types and swizzles come from a small header this
+oracle/_ref/libref_shaders.so, against which the CPU restatement's shader
+maths are pinned.  GLSL's vector types and swizzles come from a small header this
 project writes (not from a third-party math library).
 
 TEST INFRASTRUCTURE ONLY.  The shader files are read where they lie under

@@ -1,6 +1,6 @@
 """NumPy restatement of the supervoxel quality measures (asv_evaluate).
 
-TEST INFRASTRUCTURE ONLY: the checker of anisotropic_supervoxel_gb300's
+TEST INFRASTRUCTURE ONLY: the oracle for anisotropic_supervoxel_gb300's
 asv_evaluate.  The definitions (LIBSVX's 3D undersegmentation error, 3D
 segmentation accuracy, 3D boundary recall and mean duration, Xu & Corso,
 CVPR 2012; LIBSVX's own code is not available, so parity with it is

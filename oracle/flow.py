@@ -1,6 +1,6 @@
 """NumPy restatement of the device optical flow (asv_compute_flow).
 
-TEST INFRASTRUCTURE ONLY: the checker of anisotropic_supervoxel_gb300's
+TEST INFRASTRUCTURE ONLY: the oracle for anisotropic_supervoxel_gb300's
 csrc/asv_flow.cu, never called by the library.  Every step uses the same
 float32 operations in the same order as the CUDA kernels (built with
 -fmad=false), so the two agree bit for bit: grey conversion, the binomial

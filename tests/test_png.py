@@ -1,6 +1,6 @@
 """PNG frame input/output (csrc/asv_png.cpp) against an independent codec.
 
-The checker is Python's own zlib (a different DEFLATE implementation) plus a
+The independent codec here is Python's own zlib (a different DEFLATE implementation) plus a
 NumPy restatement of the PNG filters and Adam7 passes: test images are
 encoded here with every zlib strategy (stored, fixed, dynamic Huffman, RLE,
 Huffman-only), every colour type and bit depth, random row filters and
@@ -182,7 +182,7 @@ def test_decode_large_dynamic(tmp_path):
 
 
 def _decode_here(data):
-    """the library's PNG output decoded by the checker: chunk CRCs, zlib,
+    """the library's PNG output decoded independently: chunk CRCs, zlib,
     NumPy unfiltering"""
     assert data[:8] == SIG
     at, idat, hdr = 8, b"", None
