@@ -285,11 +285,14 @@ int inflate_raw(BitIn &state, uint8_t *out, size_t cap, size_t *olen)
             if (lens[256] == 0) return PNG_FORMAT;         // no end-of-block code
             if (!lit.build(lens, nlit) || !dist.build(lens + nlit, ndist)) return PNG_FORMAT;
         }
+        // Past the end of the input the reader yields zero bits, so a
+        // truncated stream still ends here: at an end-of-block code, at the
+        // output bound or at a match; the overrun is checked there rather
+        // than after every literal.
         while (true) {
             int s = lit.decode(in);
-            if (s < 0 || in.overrun()) return PNG_FORMAT;
             if (s < 256) {
-                if (o >= cap) return PNG_FORMAT;
+                if (s < 0 || o >= cap) return PNG_FORMAT;
                 out[o++] = (uint8_t)s;
                 continue;
             }
@@ -301,8 +304,16 @@ int inflate_raw(BitIn &state, uint8_t *out, size_t cap, size_t *olen)
             if (ds < 0 || ds >= 30) return PNG_FORMAT;
             const size_t d = kDistBase[ds] + in.get(kDistExtra[ds]);
             if (in.overrun() || d > o || len > cap - o) return PNG_FORMAT;
-            for (size_t k = 0; k < len; k++, o++) out[o] = out[o - d];
+            if (d == 1) {
+                std::memset(out + o, out[o - 1], len);              // a run of one byte
+            } else if (d >= len) {
+                std::memcpy(out + o, out + o - d, len);              // source and target apart
+            } else {
+                for (size_t k = 0; k < len; k++) out[o + k] = out[o + k - d];
+            }
+            o += len;
         }
+        if (in.overrun()) return PNG_FORMAT;
     }
     *olen = o;
     state = in;
