@@ -115,7 +115,12 @@ __global__ void __launch_bounds__(1024) k_na_stats(NaScratch s, const int32_t *_
             warp_tot[threadIdx.x] = incl - v;
         }
         __syncthreads();
-        if (i < Kp) s.rank[i] = alive ? carry + warp_tot[w] + pre : -1;
+        if (i < Kp) {
+            const int live_before = carry + warp_tot[w] + pre;
+            s.rank[i] = alive ? live_before : -1;
+            const int dead_before = i - live_before;        // the first four dead seeds, in order
+            if (!alive && dead_before < 4) s.rec[R_DEAD0 + dead_before] = i;
+        }
         __syncthreads();
         if (threadIdx.x == blockDim.x - 1) carry += warp_tot[w] + pre + alive;
         __syncthreads();
@@ -128,9 +133,6 @@ __global__ void __launch_bounds__(1024) k_na_stats(NaScratch s, const int32_t *_
         int l0 = raw[0];
         s.rec[R_L0] = l0;
         s.rec[R_M0] = (l0 >= 0 && l0 < Kp && s.rank[l0] >= 0) ? s.rank[l0] : 0;
-        int nd = 0;
-        for (int i = 0; i < Kp && nd < 4; i++)
-            if (s.counts[i] < 1) s.rec[R_DEAD0 + nd++] = i;
     }
 }
 

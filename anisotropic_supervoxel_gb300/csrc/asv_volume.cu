@@ -814,7 +814,12 @@ __global__ void __launch_bounds__(1024) k_post_stats(AsvDev d)
             warp_tot[threadIdx.x] = incl - v;   // exclusive
         }
         __syncthreads();
-        if (i < Kp) rank[i] = alive ? carry + warp_tot[w] + pre : -1;
+        if (i < Kp) {
+            const int live_before = carry + warp_tot[w] + pre;
+            rank[i] = alive ? live_before : -1;
+            const int dead_before = i - live_before;        // the first four dead seeds, in order
+            if (!alive && dead_before < 4) rec[POST_DEAD0 + dead_before] = i;
+        }
         __syncthreads();
         if (threadIdx.x == blockDim.x - 1) carry += warp_tot[w] + pre + alive;
         __syncthreads();
@@ -832,9 +837,6 @@ __global__ void __launch_bounds__(1024) k_post_stats(AsvDev d)
         int l0 = lbl[0];
         rec[POST_L0] = l0;
         rec[POST_M0] = (l0 >= 0 && l0 < Kp && rank[l0] >= 0) ? rank[l0] : 0;
-        int nd = 0;
-        for (int i = 0; i < Kp && nd < 4; i++)
-            if (sums[8ull * i + 3] < 1) rec[POST_DEAD0 + nd++] = i;
     }
 }
 
