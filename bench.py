@@ -132,16 +132,21 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def jfa_traffic_per_voxel():
-    """DRAM bytes per voxel of one JFA pass from the committed ncu summary."""
+def profile_value(key):
+    """A `key: value` line of the committed k_jfa ncu summary."""
     try:
         with open(TRAFFIC) as f:
             for line in f:
-                if line.startswith("dram_bytes_per_voxel:"):
+                if line.startswith(key + ":"):
                     return float(line.split(":")[1])
     except OSError:
         pass
     return None
+
+
+def jfa_traffic_per_voxel():
+    """DRAM bytes per voxel of one JFA pass from the committed ncu summary."""
+    return profile_value("dram_bytes_per_voxel")
 
 
 def cpu_baseline(w, rgb, fwd, bwd, iters):
@@ -344,6 +349,7 @@ def run_ours(args):
                          "kernel": "k_jfa", "bytes_per_launch": JFA_BYTES_PER_VOXEL * nvox,
                          "launch_ms": jfa_launch_s * 1e3,
                          "traffic": tpv * nvox if tpv is not None else None,
+                         "issue_active_ncu": profile_value("issue_active"),
                          "fp32_nominal_tflops": JFA_FLOP_PER_VOXEL * nvox / jfa_launch_s / 1e12,
                          "jfa_share_of_loop": jfa_ms / loop_ms if loop_ms else None},
             "clocks": clk,
