@@ -21,6 +21,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "asv_host.h"
@@ -855,9 +856,15 @@ extern "C" int asv_png_write_rgb(const char *path, const uint8_t *rgb, int W, in
 extern "C" int asv_render_rgb(const int32_t *labels, int W, int H, int D, int n_labels, uint8_t *rgb)
 {
     if (!labels || !rgb || W <= 0 || H <= 0 || D < 0 || n_labels < 0) return PNG_BAD_ARG;
-    std::srand(1);        // the default state of rand() when the reference's process starts
     std::vector<int> col((size_t)n_labels * 3);
-    for (auto &c : col) c = std::rand() % 256;
+    {
+        // rand() is one process-wide sequence: renders on several host
+        // threads take the palette one at a time
+        static std::mutex mu;
+        std::lock_guard<std::mutex> lk(mu);
+        std::srand(1);    // the default state of rand() when the reference's process starts
+        for (auto &c : col) c = std::rand() % 256;
+    }
     const size_t fr = (size_t)W * H;
 #pragma omp parallel for schedule(static)
     for (int t = 0; t < D; t++)

@@ -247,25 +247,17 @@ extern "C" int asv_write_labels_txt(const char *path, const int32_t *labels, int
 extern "C" int asv_write_render_ppm(const char *prefix, const int32_t *labels, int W, int H, int D,
                                     int n_labels)
 {
-    if (!prefix || !labels || n_labels < 0) return -1;
-    std::srand(1);   // the default state of rand() when the reference's process starts
-    std::vector<int> col((size_t)n_labels * 3);
-    for (auto &c : col) c = std::rand() % 256;
-    std::vector<uint8_t> img((size_t)W * H * 3);
+    if (!prefix || !labels || n_labels < 0 || W <= 0 || H <= 0 || D < 0) return -1;
+    std::vector<uint8_t> rgb((size_t)W * H * 3 * D);
+    if (asv_render_rgb(labels, W, H, D, n_labels, rgb.data()) != 0) return -1;   // the same palette
+    const size_t frame = (size_t)W * H * 3;
     for (int t = 0; t < D; t++) {
-        for (int y = 0; y < H; y++)
-            for (int x = 0; x < W; x++) {
-                int l = labels[((size_t)t * H + y) * W + x];
-                uint8_t *o = &img[3 * ((size_t)(H - 1 - y) * W + x)];   // un-flip
-                if (l < 0 || l >= n_labels) { o[0] = o[1] = o[2] = 0; }
-                else { o[0] = (uint8_t)col[3 * l]; o[1] = (uint8_t)col[3 * l + 1]; o[2] = (uint8_t)col[3 * l + 2]; }
-            }
         char name[4096];
         std::snprintf(name, sizeof(name), "%s%05d.ppm", prefix, t);
         FILE *f = std::fopen(name, "wb");
         if (!f) return -2;
         std::fprintf(f, "P6\n%d %d\n255\n", W, H);
-        std::fwrite(img.data(), 1, img.size(), f);
+        std::fwrite(rgb.data() + frame * t, 1, frame, f);
         if (std::fclose(f) != 0) return -3;
     }
     return 0;
