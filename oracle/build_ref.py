@@ -287,11 +287,22 @@ def build(force=False):
 # ---------------------------------------------------------------------------
 HOST_LIB = os.path.join(OUT, "libref_host.so")
 HOST_FUNCS = [
-    # (file, signature start, shim struct, members)
+    # (file, signature start, shim struct, members, stop marker): a function is
+    # cut whole, or up to the stop marker (the first GL call that follows its
+    # host arithmetic) and closed there.  A member `cout` shadows std::cout so
+    # the functions' progress messages stay out of the test output.
     ("GPU-AS/Image.cpp", "void Image::EnforceLabelConnectivity3D(", "ImageShim",
-     "int texel_num, depth, height, width, slice_num;"),
+     "int texel_num, depth, height, width, slice_num;", None),
     ("streamGPU-AS/Render.cpp", "void Render::label_connected3D(", "RenderShim",
-     "int width, height, depth_all;"),
+     "int width, height, depth_all;", None),
+    # Image::init_seeds (GPU-AS/Image.cpp:20-92): the regular seed grid
+    ("GPU-AS/Image.cpp", "void Image::init_seeds(", "SeedShim",
+     "int texel_num, seeds_num, width, height, depth, s, max_s, ac_seeds_num, dNum, wNum, hNum;\n"
+     "    string dbname; vector<float> seeds_lsc; ostringstream cout;", "glGenVertexArrays"),
+    # Image::sequence_label (GPU-AS/Image.cpp:1727-1778): the > 3 dead-seed remap
+    # and the raster-order fill of label -1
+    ("GPU-AS/Image.cpp", "void Image::sequence_label(", "SequenceShim",
+     "int texel_num; ostringstream cout;", None),
 ]
 
 HOST_WRAPPERS = r"""
@@ -312,6 +323,34 @@ extern "C" int ref_label_connected3D(const int *labels, int W, int H, int D, int
     int num = 0;
     s.label_connected3D(const_cast<int *>(labels), out, num, supsz);
     return num;
+}
+
+// the seed grid: (x, y, z, id) per seed into out (room for cap seeds), and
+// s, dNum, hNum, wNum, ac_seeds_num into g5; returns the seeds placed
+extern "C" int ref_init_seeds(int W, int H, int D, int K, int middlebury, float *out, int cap, int *g5)
+{
+    SeedShim s;
+    s.width = W; s.height = H; s.depth = D; s.seeds_num = K; s.texel_num = W * H * D;
+    s.dbname = middlebury ? "MiddleburyFlow" : "";
+    s.init_seeds();
+    const int n = (int)(s.seeds_lsc.size() / 4);
+    for (int i = 0; i < n && i < cap; i++)
+        for (int k = 0; k < 4; k++) out[4 * i + k] = s.seeds_lsc[4 * i + k];
+    g5[0] = s.s; g5[1] = s.dNum; g5[2] = s.hNum; g5[3] = s.wNum; g5[4] = s.ac_seeds_num;
+    return n;
+}
+
+// check_dead_seeds' map (GPU-AS/Image.cpp:1597-1617: live seeds numbered in
+// seed order, from their voxel counts), then sequence_label on the labels
+extern "C" void ref_sequence_label(int *labels, long n, const long long *counts, int Kp, int dead_seed)
+{
+    map<int, int> m;
+    int valid = 0;
+    for (int i = 0; i < Kp; i++)
+        if (int(float(counts[i])) >= 1) m.insert(pair<int, int>(i, valid++));
+    SequenceShim s;
+    s.texel_num = (int)n;
+    s.sequence_label(labels, m, dead_seed != 0);
 }
 """
 
@@ -338,17 +377,22 @@ def _cut_function(src, start):
 def build_host(force=False):
     """Compiles the reference's host functions listed above; returns the
     library path, or None when the reference tree is not present."""
-    srcs = [os.path.join(REF, f) for f, _, _, _ in HOST_FUNCS]
+    srcs = [os.path.join(REF, f) for f, _, _, _, _ in HOST_FUNCS]
     if not all(os.path.exists(f) for f in srcs):
         return None
     if not force and os.path.exists(HOST_LIB) and os.path.getmtime(HOST_LIB) >= max(
             [os.path.getmtime(f) for f in srcs] + [os.path.getmtime(__file__)]):
         return HOST_LIB
     os.makedirs(OUT, exist_ok=True)
-    parts = ["#include <cstring>\n"]
-    for path, start, shim, members in HOST_FUNCS:
+    parts = ["#include <cmath>\n#include <cstring>\n#include <iostream>\n#include <map>\n"
+             "#include <sstream>\n#include <string>\n#include <vector>\nusing namespace std;\n"]
+    for path, start, shim, members, stop in HOST_FUNCS:
         text = _strip_comments(open(os.path.join(REF, path), encoding="latin-1").read())
-        fn = _cut_function(text, start)
+        if stop is None:
+            fn = _cut_function(text, start)
+        else:                                      # the host part, closed at the marker
+            i = text.index(start)
+            fn = text[i:text.index(stop, i)] + "}"
         fn = re.sub(r"\b\w+::(\w+\s*\()", r"\1", fn, count=1)
         parts.append(f"struct {shim} {{\n    {members}\n{fn}\n}};\n")
     parts.append(HOST_WRAPPERS)

@@ -6,7 +6,9 @@ shaders compiled as C++ (oracle/build_ref.py; needs the reference tree).
 Fixtures (npz): inputs plus the compiled reference shaders' outputs for
 RGB2LAB.fs (a seeded sample of RGB values), derivative_t.gs, flood.gs (one
 pass at several steps) and aver_exception.vs, and of the reference's
-Image::EnforceLabelConnectivity3D compiled from its C++ (connectivity.npz).
+Image::EnforceLabelConnectivity3D (connectivity.npz), Image::init_seeds
+(seed_grid.npz) and Image::sequence_label (sequence_label.npz) compiled from
+its C++.
 tests/test_golden.py checks the CPU restatement and the CUDA path against
 them.
 """
@@ -100,6 +102,32 @@ def main():
         n = host.ref_enforce_connectivity(P(labels), W, H, D, supsz, P(out))
         arrays.update({f"labels_{i}": labels, f"out_{i}": out, f"supsz_{i}": supsz, f"n_{i}": n})
     np.savez_compressed(os.path.join(HERE, "connectivity.npz"), **arrays)
+
+    # Image::init_seeds and Image::sequence_label, compiled from the reference's C++
+    host.ref_init_seeds.argtypes = [ctypes.c_int] * 5 + [V, ctypes.c_int, V]
+    host.ref_init_seeds.restype = ctypes.c_int
+    host.ref_sequence_label.argtypes = [V, ctypes.c_long, V, ctypes.c_int, ctypes.c_int]
+    arrays = {}
+    for i, (W, H, D, K) in enumerate(pin.GRID_SHAPES):
+        if K > 3000:
+            continue                                   # fixtures stay small; the pin test covers these
+        for mb in (0, 1):
+            g5 = np.zeros(5, np.int32)
+            n = host.ref_init_seeds(W, H, D, K, mb, None, 0, P(g5))
+            seeds = np.zeros((n, 4), np.float32)
+            host.ref_init_seeds(W, H, D, K, mb, P(seeds), n, P(g5))
+            arrays.update({f"shape_{i}_{mb}": np.array([W, H, D, K, mb]), f"seeds_{i}_{mb}": seeds,
+                           f"grid_{i}_{mb}": g5})
+    np.savez_compressed(os.path.join(HERE, "seed_grid.npz"), **arrays)
+    arrays = {}
+    for i, (labels, counts, kp) in enumerate(pin.sequence_label_cases(np.random.default_rng(41))):
+        dead = int((counts[:kp] < 1).sum())
+        if dead in (1, 2, 3):
+            continue
+        out = labels.copy()
+        host.ref_sequence_label(P(out), out.size, P(counts), kp, 1 if dead > 3 else 0)
+        arrays.update({f"labels_{i}": labels, f"counts_{i}": counts, f"kp_{i}": kp, f"out_{i}": out})
+    np.savez_compressed(os.path.join(HERE, "sequence_label.npz"), **arrays)
     print("fixtures written to", HERE)
 
 

@@ -86,3 +86,38 @@ def test_cuda_connectivity(asv):
         for labels, supsz, out, n in _connectivity_cases():
             got, m = img.enforce_connectivity_labels(labels, supsz)
             assert m == n and np.array_equal(got, out), labels.shape
+
+
+def test_oracle_seed_grid():
+    """the restatement's seed grid against Image::init_seeds' own output"""
+    from oracle import oracle
+    f = load("seed_grid.npz")
+    n = 0
+    for key in f.files:
+        if not key.startswith("shape_"):
+            continue
+        W, H, D, K, mb = (int(v) for v in f[key])
+        tag = key[len("shape_"):]
+        s4, g = oracle.grid_seeds(W, H, D, K, middlebury=mb)
+        assert (g.s, g.dNum, g.hNum, g.wNum, g.Kp) == tuple(int(v) for v in f["grid_" + tag])
+        assert np.array_equal(s4, f["seeds_" + tag])
+        n += 1
+    assert n >= 20
+
+
+def test_oracle_sequence_label(orc):
+    """the restatement's post-processing against Image::sequence_label's own output"""
+    f = load("sequence_label.npz")
+    n = 0
+    for key in f.files:
+        if not key.startswith("labels_"):
+            continue
+        i = key[len("labels_"):]
+        labels, counts, kp = f[key], f["counts_" + i], int(f["kp_" + i])
+        sums = np.zeros((kp + 1, 7), np.int64)
+        sums[:, 3] = counts
+        got, _ = orc.postprocess(labels, sums, kp)
+        assert np.array_equal(got, f["out_" + i]), i
+        n += 1
+    assert n >= 10
+

@@ -211,3 +211,74 @@ def test_connectivity_on_jfa_labels(ref_host, orc, asv):
     n = ref_host.ref_enforce_connectivity(P(raw), 48, 36, 10, supsz, P(want))
     got, m = orc.enforce_connectivity(raw, supsz)
     assert m == n and np.array_equal(got, want)
+
+
+@pytest.fixture(scope="module")
+def ref_grid(ref_host):
+    V = ctypes.c_void_p
+    ref_host.ref_init_seeds.argtypes = [ctypes.c_int] * 5 + [V, ctypes.c_int, V]
+    ref_host.ref_init_seeds.restype = ctypes.c_int
+    ref_host.ref_sequence_label.argtypes = [V, ctypes.c_long, V, ctypes.c_int, ctypes.c_int]
+    return ref_host
+
+
+GRID_SHAPES = [(240, 160, 30, 200), (320, 240, 85, 1000), (1280, 720, 30, 2000), (64, 48, 12, 60),
+               (37, 23, 9, 25), (17, 9, 3, 2), (2, 2, 2, 1), (40, 30, 2, 30), (160, 128, 8, 30000),
+               (64, 64, 64, 32767), (640, 480, 120, 2000), (50, 50, 5, 3000), (90, 50, 8, 120)]
+
+
+@pytest.mark.parametrize("middlebury", [0, 1])
+def test_seed_grid_matches_reference(ref_grid, orc, middlebury):
+    """Image::init_seeds compiled from the reference tree against the restatement:
+    the same seeds, ids, base step s and grid counts."""
+    for (W, H, D, K) in GRID_SHAPES:
+        g5 = np.zeros(5, np.int32)
+        n = ref_grid.ref_init_seeds(W, H, D, K, middlebury, None, 0, P(g5))
+        want = np.zeros((max(n, 1), 4), np.float32)
+        ref_grid.ref_init_seeds(W, H, D, K, middlebury, P(want), n, P(g5))
+        s4, g = orc.grid_seeds(W, H, D, K, middlebury=middlebury)
+        assert (g.s, g.dNum, g.hNum, g.wNum, g.Kp) == tuple(g5), (W, H, D, K)
+        assert np.array_equal(s4, want[:n]), (W, H, D, K)
+
+
+def sequence_label_cases(rng):
+    """label volumes with the voxel count of every label (as the centroid pass
+    gives them): more than 3 labels absent (dead seeds), or all present with
+    label -1 in places; some with long runs of one label"""
+    out = []
+    for case in range(24):
+        D, H, W = int(rng.integers(1, 6)), int(rng.integers(1, 12)), int(rng.integers(2, 14))
+        kp = int(rng.integers(9, 40))
+        many_dead = case % 2 == 0
+        if many_dead:
+            used = np.sort(rng.choice(kp, kp - 4 - int(rng.integers(0, 3)), replace=False))
+            labels = used[rng.integers(0, used.size, (D, H, W))].astype(np.int32)
+        else:
+            labels = rng.integers(0, kp, (D, H, W)).astype(np.int32)
+            labels.ravel()[:kp] = np.arange(kp) if labels.size >= kp else labels.ravel()[:kp]
+        if case % 3 == 0:
+            labels[:, :, : W // 2] = labels[0, 0, 0]                 # runs of one label
+        labels[rng.random(labels.shape) < 0.1] = -1
+        counts = np.bincount(np.where(labels < 0, kp, labels).ravel(), minlength=kp + 1).astype(np.int64)
+        out.append((labels, counts, kp))
+    return out
+
+
+def test_sequence_label_matches_reference(ref_grid, orc):
+    """Image::sequence_label compiled from the reference tree against the
+    restatement's post-processing: the > 3 dead-seed remap (with its
+    unchanging last_label) and the raster-order fill of label -1."""
+    seen = set()
+    for labels, counts, kp in sequence_label_cases(np.random.default_rng(41)):
+        dead = int((counts[:kp] < 1).sum())
+        if dead in (1, 2, 3):
+            continue                                   # that branch is a shader (label_replace.gs)
+        sums = np.zeros((kp + 1, 7), np.int64)
+        sums[:, 3] = counts
+        got, stats = orc.postprocess(labels, sums, kp)
+        want = labels.copy()
+        ref_grid.ref_sequence_label(P(want), want.size, P(counts), kp, 1 if dead > 3 else 0)
+        assert stats[0] == dead
+        assert np.array_equal(got, want)
+        seen.add("remap" if dead > 3 else "fill")
+    assert seen == {"remap", "fill"}
