@@ -303,7 +303,23 @@ HOST_FUNCS = [
     # and the raster-order fill of label -1
     ("GPU-AS/Image.cpp", "void Image::sequence_label(", "SequenceShim",
      "int texel_num; ostringstream cout;", None),
+    # Image::initialization (GPU-AS/Image.cpp:350-620): its host code before the
+    # first GL call (cell ranges, the cell-id grid) and after the readback of
+    # the density sums (the redistribution); the GL part in between is the
+    # two density shaders, pinned on their own, and is replaced by the glue
+    # INIT_GLUE, which keeps the grid and supplies the sums as `res`
+    ("GPU-AS/Image.cpp", "void Image::initialization(", "InitShim",
+     "int texel_num, slice_num, width, height, depth, ac_seeds_num, dNum, hNum, wNum;\n"
+     "    vector<float> seeds_lsc, seeds_lsc_adjust; float *grid_out; const float *res_in;\n"
+     "    ostringstream cout;", ("glBindFramebuffer", "vector<float> seed_density;")),
 ]
+
+INIT_GLUE = """
+    memcpy(grid_out, grid, sizeof(float) * texel_num);
+    delete[] grid;
+    float *res = new float[4 * ac_seeds_num];
+    for (int q = 0; q < ac_seeds_num; q++) res[4 * q] = res_in[q];
+"""
 
 HOST_WRAPPERS = r"""
 extern "C" int ref_enforce_connectivity(const int *labels, int W, int H, int D, int supsz, int *out)
@@ -342,6 +358,28 @@ extern "C" int ref_init_seeds(int W, int H, int D, int K, int middlebury, float 
 
 // check_dead_seeds' map (GPU-AS/Image.cpp:1597-1617: live seeds numbered in
 // seed order, from their voxel counts), then sequence_label on the labels
+// Image::init_seeds, then the host parts of Image::initialization with the
+// density sums given (one per grid cell); writes the cell-id grid (W*H*D)
+// and the redistributed seeds (x, y, z, id), returns how many
+extern "C" int ref_initialization(int W, int H, int D, int K, int middlebury, const float *density,
+                                  float *grid_out, float *seeds_out, int cap)
+{
+    SeedShim g;
+    g.width = W; g.height = H; g.depth = D; g.seeds_num = K; g.texel_num = W * H * D;
+    g.dbname = middlebury ? "MiddleburyFlow" : "";
+    g.init_seeds();
+    InitShim s;
+    s.width = W; s.height = H; s.depth = D; s.texel_num = W * H * D; s.slice_num = W * H;
+    s.ac_seeds_num = g.ac_seeds_num; s.dNum = g.dNum; s.hNum = g.hNum; s.wNum = g.wNum;
+    s.seeds_lsc = g.seeds_lsc; s.grid_out = grid_out; s.res_in = density;
+    Shader a, b;
+    s.initialization(a, b);
+    const int n = (int)(s.seeds_lsc_adjust.size() / 4);
+    for (int i = 0; i < n && i < cap; i++)
+        for (int k = 0; k < 4; k++) seeds_out[4 * i + k] = s.seeds_lsc_adjust[4 * i + k];
+    return n;
+}
+
 extern "C" void ref_sequence_label(int *labels, long n, const long long *counts, int Kp, int dead_seed)
 {
     map<int, int> m;
@@ -385,11 +423,15 @@ def build_host(force=False):
         return HOST_LIB
     os.makedirs(OUT, exist_ok=True)
     parts = ["#include <cmath>\n#include <cstring>\n#include <iostream>\n#include <map>\n"
-             "#include <sstream>\n#include <string>\n#include <vector>\nusing namespace std;\n"]
+             "#include <sstream>\n#include <string>\n#include <vector>\nusing namespace std;\n"
+             "struct Shader {};                         // the GL programs' type, unused here\n"]
     for path, start, shim, members, stop in HOST_FUNCS:
         text = _strip_comments(open(os.path.join(REF, path), encoding="latin-1").read())
         if stop is None:
             fn = _cut_function(text, start)
+        elif isinstance(stop, tuple):              # host code, glue, host code to the end
+            whole = _cut_function(text, start)
+            fn = whole[:whole.index(stop[0])] + INIT_GLUE + whole[whole.index(stop[1]):]
         else:                                      # the host part, closed at the marker
             i = text.index(start)
             fn = text[i:text.index(stop, i)] + "}"

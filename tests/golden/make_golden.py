@@ -7,8 +7,8 @@ Fixtures (npz): inputs plus the compiled reference shaders' outputs for
 RGB2LAB.fs (a seeded sample of RGB values), derivative_t.gs, flood.gs (one
 pass at several steps) and aver_exception.vs, and of the reference's
 Image::EnforceLabelConnectivity3D (connectivity.npz), Image::init_seeds
-(seed_grid.npz) and Image::sequence_label (sequence_label.npz) compiled from
-its C++.
+(seed_grid.npz), Image::sequence_label (sequence_label.npz) and the host
+parts of Image::initialization (density_placement.npz) compiled from its C++.
 tests/test_golden.py checks the CPU restatement and the CUDA path against
 them.
 """
@@ -128,7 +128,28 @@ def main():
         host.ref_sequence_label(P(out), out.size, P(counts), kp, 1 if dead > 3 else 0)
         arrays.update({f"labels_{i}": labels, f"counts_{i}": counts, f"kp_{i}": kp, f"out_{i}": out})
     np.savez_compressed(os.path.join(HERE, "sequence_label.npz"), **arrays)
+
+    # the host parts of Image::initialization (cell-id grid, redistribution)
+    host.ref_initialization.argtypes = [ctypes.c_int] * 5 + [V, V, V, ctypes.c_int]
+    host.ref_initialization.restype = ctypes.c_int
+    arrays = {}
+    for i, (W, H, D, K, mb) in enumerate(DENSITY_CASES):
+        rgb, _, _ = asv.synth_clip(W, H, D, n_ellipses=5, noise_sigma=4.0, seed=W * D + K)
+        s4, g = oracle.grid_seeds(W, H, D, K, middlebury=mb)
+        _, dens = oracle.density_adjust(rgb, s4, g)
+        dens = np.ascontiguousarray(dens, np.float32)
+        grid = np.empty((D, H, W), np.float32)
+        seeds = np.zeros((g.Kp, 4), np.float32)
+        n = host.ref_initialization(W, H, D, K, mb, P(dens), P(grid), P(seeds), g.Kp)
+        arrays.update({f"case_{i}": np.array([W, H, D, K, mb]), f"seeds_{i}": seeds[:n], f"grid_{i}": grid})
+    np.savez_compressed(os.path.join(HERE, "density_placement.npz"), **arrays)
     print("fixtures written to", HERE)
+
+
+# clips of the density-placement fixture (W, H, D, K, middlebury); the clip is
+# asv_synth_clip(W, H, D, n_ellipses=5, noise_sigma=4.0, seed=W * D + K)
+DENSITY_CASES = [(64, 48, 12, 60, 0), (37, 23, 9, 25, 0), (120, 80, 15, 300, 0), (50, 50, 5, 3000, 0),
+                 (64, 48, 12, 60, 1)]
 
 
 if __name__ == "__main__":

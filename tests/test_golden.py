@@ -121,3 +121,31 @@ def test_oracle_sequence_label(orc):
         n += 1
     assert n >= 10
 
+
+def test_oracle_density_placement(asv):
+    """the restatement's seed redistribution and cell-id grid against the host
+    parts of Image::initialization's own output"""
+    import ctypes
+    from oracle import oracle
+    from oracle.oracle import GridInfo
+    f = load("density_placement.npz")
+    lib = oracle.load()
+    V = ctypes.c_void_p
+    lib.orc_grid_cell_tables.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, V,
+                                         ctypes.POINTER(GridInfo), V, V, V]
+    n = 0
+    while f"case_{n}" in f:
+        W, H, D, K, mb = (int(v) for v in f[f"case_{n}"])
+        rgb, _, _ = asv.synth_clip(W, H, D, n_ellipses=5, noise_sigma=4.0, seed=W * D + K)
+        s4, g = oracle.grid_seeds(W, H, D, K, middlebury=mb)
+        adj, _ = oracle.density_adjust(rgb, s4, g)
+        assert np.array_equal(adj, f[f"seeds_{n}"]), (W, H, D, K, mb)
+        xc, yc, zc = np.empty(W, np.int32), np.empty(H, np.int32), np.empty(D, np.int32)
+        s4c = np.ascontiguousarray(s4)
+        lib.orc_grid_cell_tables(W, H, D, s4c.ctypes.data_as(V), ctypes.byref(g), xc.ctypes.data_as(V),
+                                 yc.ctypes.data_as(V), zc.ctypes.data_as(V))
+        cell = (zc[:, None, None] * g.hNum + yc[None, :, None]) * g.wNum + xc[None, None, :]
+        assert np.array_equal(f[f"grid_{n}"], cell.astype(np.float32))
+        n += 1
+    assert n >= 5
+

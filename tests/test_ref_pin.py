@@ -282,3 +282,32 @@ def test_sequence_label_matches_reference(ref_grid, orc):
         assert np.array_equal(got, want)
         seen.add("remap" if dead > 3 else "fill")
     assert seen == {"remap", "fill"}
+
+
+@pytest.mark.parametrize("W,H,D,K,mb", [(64, 48, 12, 60, 0), (37, 23, 9, 25, 0), (120, 80, 15, 300, 0),
+                                        (50, 50, 5, 3000, 0), (64, 48, 12, 60, 1), (240, 160, 30, 200, 0)])
+def test_density_placement_matches_reference(ref_grid, orc, asv, W, H, D, K, mb):
+    """The host parts of Image::initialization compiled from the reference tree
+    (cell ranges, the cell-id grid, the redistribution over the density sums)
+    against the restatement, given the restatement's density sums (the sums
+    themselves come from derivative_t / density_grid, pinned above)."""
+    from oracle.oracle import GridInfo
+    V = ctypes.c_void_p
+    ref_grid.ref_initialization.argtypes = [ctypes.c_int] * 5 + [V, V, V, ctypes.c_int]
+    ref_grid.ref_initialization.restype = ctypes.c_int
+    rgb, _, _ = asv.synth_clip(W, H, D, n_ellipses=5, noise_sigma=4.0, seed=W * D + K)
+    s4, g = orc.grid_seeds(W, H, D, K, middlebury=mb)
+    adj, dens = orc.density_adjust(rgb, s4, g)
+    grid = np.empty((D, H, W), np.float32)
+    seeds = np.zeros((g.Kp, 4), np.float32)
+    dens = np.ascontiguousarray(dens, np.float32)
+    n = ref_grid.ref_initialization(W, H, D, K, mb, P(dens), P(grid), P(seeds), g.Kp)
+    assert n == adj.shape[0]
+    assert np.array_equal(seeds[:n], adj)
+    lib = orc.load()
+    lib.orc_grid_cell_tables.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, V,
+                                         ctypes.POINTER(GridInfo), V, V, V]
+    xc, yc, zc = np.empty(W, np.int32), np.empty(H, np.int32), np.empty(D, np.int32)
+    lib.orc_grid_cell_tables(W, H, D, P(np.ascontiguousarray(s4)), ctypes.byref(g), P(xc), P(yc), P(zc))
+    cell = (zc[:, None, None] * g.hNum + yc[None, :, None]) * g.wNum + xc[None, None, :]
+    assert np.array_equal(grid, cell.astype(np.float32))
