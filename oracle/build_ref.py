@@ -223,6 +223,31 @@ extern "C" void ref_centroid_target(float id, int W, int H, float ac_seeds_num, 
     *ty = (int)std::floor((p.y + 1.0f) * 0.5f * (float)H);
 }
 
+// one label_replace pass (Image.cpp:1650-1672): labels4 is the RGBA32F flood
+// volume (the label in .w); texels labelled last_seed_index take
+// dead_seed_index
+extern "C" void ref_label_replace(const float *labels4, int W, int H, int D, int dead_seed_index,
+                                  int last_seed_index, float *out4)
+{
+    Sampler3D t; t.data = labels4; t.W = W; t.H = H; t.D = D;
+    label_replace_vs::width_ratio = wr_of(W);
+    label_replace_vs::height_ratio = wr_of(H);
+    label_replace_vs::depth_ratio = wr_of(D);
+    label_replace_gs::texels = t;
+    label_replace_gs::dead_seed_index = dead_seed_index;
+    label_replace_gs::last_seed_index = last_seed_index;
+    for (int z = 0; z < D; z++) for (int y = 0; y < H; y++) for (int x = 0; x < W; x++) {
+        label_replace_vs::aPos = ivec3(x, y, z);
+        label_replace_vs::shader_main();
+        label_replace_gs::gs_in[0].gPos = label_replace_vs::vs_out.gPos;
+        label_replace_gs::gs_in[0].gTex = label_replace_vs::vs_out.gTex;
+        label_replace_gs::shader_main();
+        float *o = out4 + 4 * (((size_t)z * H + y) * W + x);
+        vec4 c = label_replace_gs::f_color;
+        o[0] = c.x; o[1] = c.y; o[2] = c.z; o[3] = c.w;
+    }
+}
+
 // sum_pos, sum_color: RGBA32F W x H x D volumes (slice 0 holds the sums);
 // image: LAB 3 floats / voxel.  For seed `id`: centroid position (x, y, z, id)
 // and colour.

@@ -8,7 +8,9 @@ RGB2LAB.fs (a seeded sample of RGB values), derivative_t.gs, flood.gs (one
 pass at several steps) and aver_exception.vs, and of the reference's
 Image::EnforceLabelConnectivity3D (connectivity.npz), Image::init_seeds
 (seed_grid.npz), Image::sequence_label (sequence_label.npz) and the host
-parts of Image::initialization (density_placement.npz) compiled from its C++.
+parts of Image::initialization (density_placement.npz) compiled from its C++,
+and check_dead_seeds' 1-3 dead-seed branch (label_replace.gs with its host
+loop, then sequence_label: few_dead.npz).
 tests/test_golden.py checks the CPU restatement and the CUDA path against
 them.
 """
@@ -143,6 +145,14 @@ def main():
         n = host.ref_initialization(W, H, D, K, mb, P(dens), P(grid), P(seeds), g.Kp)
         arrays.update({f"case_{i}": np.array([W, H, D, K, mb]), f"seeds_{i}": seeds[:n], f"grid_{i}": grid})
     np.savez_compressed(os.path.join(HERE, "density_placement.npz"), **arrays)
+
+    # check_dead_seeds with 1-3 dead seeds: label_replace.gs and sequence_label
+    lib.ref_label_replace.argtypes = [V] + [ctypes.c_int] * 5 + [V]
+    arrays = {}
+    for i, (labels, counts, kp, dead) in enumerate(pin.few_dead_cases(np.random.default_rng(47))):
+        out = pin.reference_few_dead(lib, host, labels, counts, kp, dead)
+        arrays.update({f"labels_{i}": labels, f"counts_{i}": counts, f"kp_{i}": kp, f"out_{i}": out})
+    np.savez_compressed(os.path.join(HERE, "few_dead.npz"), **arrays)
     print("fixtures written to", HERE)
 
 

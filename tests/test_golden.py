@@ -105,9 +105,12 @@ def test_oracle_seed_grid():
     assert n >= 20
 
 
-def test_oracle_sequence_label(orc):
-    """the restatement's post-processing against Image::sequence_label's own output"""
-    f = load("sequence_label.npz")
+@pytest.mark.parametrize("fixture", ["sequence_label.npz", "few_dead.npz"])
+def test_oracle_sequence_label(orc, fixture):
+    """the restatement's post-processing against the reference's own output:
+    Image::sequence_label (> 3 dead seeds, the -1 fill) and label_replace.gs
+    with its host loop (1-3 dead seeds)"""
+    f = load(fixture)
     n = 0
     for key in f.files:
         if not key.startswith("labels_"):

@@ -311,3 +311,60 @@ def test_density_placement_matches_reference(ref_grid, orc, asv, W, H, D, K, mb)
     lib.orc_grid_cell_tables(W, H, D, P(np.ascontiguousarray(s4)), ctypes.byref(g), P(xc), P(yc), P(zc))
     cell = (zc[:, None, None] * g.hNum + yc[None, :, None]) * g.wNum + xc[None, None, :]
     assert np.array_equal(grid, cell.astype(np.float32))
+
+
+def few_dead_cases(rng):
+    """label volumes with 1 to 3 seeds absent (dead), every other seed present,
+    label -1 in half of them: (labels, counts, kp, dead ids)"""
+    out = []
+    for case in range(18):
+        D, H, W = int(rng.integers(1, 6)), int(rng.integers(1, 10)), int(rng.integers(2, 12))
+        kp = int(rng.integers(6, 30))
+        ndead = 1 + case % 3
+        dead = np.sort(rng.choice(kp, ndead, replace=False))
+        used = np.setdiff1d(np.arange(kp), dead)
+        labels = used[rng.integers(0, used.size, (D, H, W))].astype(np.int32)
+        labels.ravel()[:used.size] = used[: labels.size]             # every live seed present
+        if case % 2:
+            labels[rng.random(labels.shape) < 0.1] = -1
+        counts = np.bincount(np.where(labels < 0, kp, labels).ravel(), minlength=kp + 1).astype(np.int64)
+        if int((counts[:kp] < 1).sum()) == ndead:
+            out.append((labels, counts, kp, dead))
+    return out
+
+
+def reference_few_dead(ref, ref_grid, labels, counts, kp, dead):
+    """check_dead_seeds' 1-3 dead branch with the reference's own code: one
+    label_replace pass per dead seed (GPU-AS/Image.cpp:1647-1672: seeds in
+    order, last_seed_index counting down from K'), then sequence_label's fill
+    of label -1 when -1 is present"""
+    D, H, W = labels.shape
+    vol = np.zeros(labels.shape + (4,), np.float32)
+    vol[..., 3] = labels
+    last = kp
+    for d in dead:
+        last -= 1
+        nxt = np.empty_like(vol)
+        ref.ref_label_replace(P(vol), W, H, D, int(d), last, P(nxt))
+        vol = nxt
+    want = vol[..., 3].astype(np.int32)
+    if counts[kp] > 0:
+        ref_grid.ref_sequence_label(P(want), want.size, P(counts), kp, 0)
+    return want
+
+
+def test_few_dead_seeds_match_reference(ref, ref_grid, orc):
+    """1 to 3 dead seeds: label_replace.gs compiled from the reference tree and
+    its host loop, against the restatement's post-processing."""
+    V = ctypes.c_void_p
+    ref.ref_label_replace.argtypes = [V] + [ctypes.c_int] * 5 + [V]
+    seen = set()
+    for labels, counts, kp, dead in few_dead_cases(np.random.default_rng(47)):
+        sums = np.zeros((kp + 1, 7), np.int64)
+        sums[:, 3] = counts
+        got, stats = orc.postprocess(labels, sums, kp)
+        want = reference_few_dead(ref, ref_grid, labels, counts, kp, dead)
+        assert stats[0] == len(dead)
+        assert np.array_equal(got, want)
+        seen.add(len(dead))
+    assert seen == {1, 2, 3}
