@@ -337,6 +337,15 @@ HOST_FUNCS = [
      "int texel_num, slice_num, width, height, depth, ac_seeds_num, dNum, hNum, wNum;\n"
      "    vector<float> seeds_lsc, seeds_lsc_adjust; float *grid_out; const float *res_in;\n"
      "    ostringstream cout;", ("glBindFramebuffer", "vector<float> seed_density;")),
+    # the streaming program's per-window grid and density placement
+    # (streamGPU-AS/Image.cpp:26-120, 321-595): the same host code shapes
+    ("streamGPU-AS/Image.cpp", "void Image::initialization_grid(", "StreamGridShim",
+     "int texel_num, seeds_num, width, height, depth, s, max_s, ac_seeds_num, dNum, wNum, hNum;\n"
+     "    vector<float> seeds_lsc, seeds_lsc_adjust; ostringstream cout;", "glGenVertexArrays"),
+    ("streamGPU-AS/Image.cpp", "void Image::initialization_adjust(", "StreamInitShim",
+     "int texel_num, slice_num, width, height, depth, ac_seeds_num, dNum, hNum, wNum;\n"
+     "    vector<float> seeds_lsc, seeds_lsc_adjust; float *grid_out; const float *res_in;\n"
+     "    ostringstream cout;", ("glBindFramebuffer", "vector<float> seed_density;")),
 ]
 
 INIT_GLUE = """
@@ -399,6 +408,33 @@ extern "C" int ref_initialization(int W, int H, int D, int K, int middlebury, co
     s.seeds_lsc = g.seeds_lsc; s.grid_out = grid_out; s.res_in = density;
     Shader a, b;
     s.initialization(a, b);
+    const int n = (int)(s.seeds_lsc_adjust.size() / 4);
+    for (int i = 0; i < n && i < cap; i++)
+        for (int k = 0; k < 4; k++) seeds_out[4 * i + k] = s.seeds_lsc_adjust[4 * i + k];
+    return n;
+}
+
+// the streaming program's window grid and density placement, as above
+extern "C" int ref_stream_initialization(int W, int H, int D, int K, const float *density, float *grid_out,
+                                         float *seeds_out, int cap, int *g5)
+{
+    StreamGridShim g;
+    g.width = W; g.height = H; g.depth = D; g.seeds_num = K; g.texel_num = W * H * D;
+    int kp = 0;
+    g.initialization_grid(kp);
+    g5[0] = g.s; g5[1] = g.dNum; g5[2] = g.hNum; g5[3] = g.wNum; g5[4] = kp;
+    if (!density) {                                      // the grid alone
+        const int n = (int)(g.seeds_lsc.size() / 4);
+        for (int i = 0; i < n && i < cap; i++)
+            for (int k = 0; k < 4; k++) seeds_out[4 * i + k] = g.seeds_lsc[4 * i + k];
+        return n;
+    }
+    StreamInitShim s;
+    s.width = W; s.height = H; s.depth = D; s.texel_num = W * H * D; s.slice_num = W * H;
+    s.ac_seeds_num = g.ac_seeds_num; s.dNum = g.dNum; s.hNum = g.hNum; s.wNum = g.wNum;
+    s.seeds_lsc = g.seeds_lsc; s.grid_out = grid_out; s.res_in = density;
+    Shader a, b;
+    s.initialization_adjust(a, b);
     const int n = (int)(s.seeds_lsc_adjust.size() / 4);
     for (int i = 0; i < n && i < cap; i++)
         for (int k = 0; k < 4; k++) seeds_out[4 * i + k] = s.seeds_lsc_adjust[4 * i + k];

@@ -368,3 +368,29 @@ def test_few_dead_seeds_match_reference(ref, ref_grid, orc):
         assert np.array_equal(got, want)
         seen.add(len(dead))
     assert seen == {1, 2, 3}
+
+
+@pytest.mark.parametrize("W,H,D,K", [(48, 40, 30, 60), (64, 48, 30, 150), (37, 23, 20, 25), (1280, 720, 30, 2000)])
+def test_stream_window_placement_matches_reference(ref_grid, orc, asv, W, H, D, K):
+    """The streaming program's per-window grid (initialization_grid) and density
+    placement (the host parts of initialization_adjust), compiled from the
+    reference tree, against the restatement (the same grid and placement
+    functions serve the windows)."""
+    V = ctypes.c_void_p
+    ref_grid.ref_stream_initialization.argtypes = [ctypes.c_int] * 4 + [V, V, V, ctypes.c_int, V]
+    ref_grid.ref_stream_initialization.restype = ctypes.c_int
+    s4, g = orc.grid_seeds(W, H, D, K)
+    g5 = np.zeros(5, np.int32)
+    grid_only = np.zeros((g.Kp, 4), np.float32)
+    n = ref_grid.ref_stream_initialization(W, H, D, K, None, None, P(grid_only), g.Kp, P(g5))
+    assert (g.s, g.dNum, g.hNum, g.wNum, g.Kp) == tuple(g5)
+    assert np.array_equal(grid_only[:n], s4)
+    if W * H * D > 4_000_000:
+        return                                        # the grid only at 720p (the placement needs a clip)
+    rgb, _, _ = asv.synth_clip(W, H, D, n_ellipses=5, noise_sigma=4.0, drift_amp=2.0, seed=W + D + K)
+    adj, dens = orc.density_adjust(rgb, s4, g)
+    dens = np.ascontiguousarray(dens, np.float32)
+    grid = np.empty((D, H, W), np.float32)
+    seeds = np.zeros((g.Kp, 4), np.float32)
+    n = ref_grid.ref_stream_initialization(W, H, D, K, P(dens), P(grid), P(seeds), g.Kp, P(g5))
+    assert n == adj.shape[0] and np.array_equal(seeds[:n], adj)
