@@ -337,6 +337,14 @@ HOST_FUNCS = [
      "int texel_num, slice_num, width, height, depth, ac_seeds_num, dNum, hNum, wNum;\n"
      "    vector<float> seeds_lsc, seeds_lsc_adjust; float *grid_out; const float *res_in;\n"
      "    ostringstream cout;", ("glBindFramebuffer", "vector<float> seed_density;")),
+    # Image::init_variables (the ratio), reset_variables and flood
+    # (GPU-AS/Image.cpp:1048-1190): compiled whole against the GL stubs of
+    # HOST_PRELUDE, the recording Shader returns the step and ratio of every pass
+    ("GPU-AS/Image.cpp", "void Image::init_variables(", "FloodShim",
+     "int s, texel_num, current_buffer, seed_range, flood_iter; float compactness, ratio, step_length;\n"
+     "    float width_ratio, height_ratio, depth_ratio; GLuint frameBuffer_flood, VAO_all_t;\n"
+     "    GLuint texture_flood[5], texture_image[4]; GLenum buffers_flood[5]; ostringstream cout;\n"
+     "    @void Image::reset_variables(@void Image::flood(", None),
     # the streaming program's per-window grid and density placement
     # (streamGPU-AS/Image.cpp:26-120, 321-595): the same host code shapes
     ("streamGPU-AS/Image.cpp", "void Image::initialization_grid(", "StreamGridShim",
@@ -347,6 +355,37 @@ HOST_FUNCS = [
      "    vector<float> seeds_lsc, seeds_lsc_adjust; float *grid_out; const float *res_in;\n"
      "    ostringstream cout;", ("glBindFramebuffer", "vector<float> seed_density;")),
 ]
+
+HOST_PRELUDE = """#include <cmath>
+#include <cstring>
+#include <iostream>
+#include <map>
+#include <sstream>
+#include <string>
+#include <utility>
+#include <vector>
+using namespace std;
+// GL calls of the compiled functions, as no-ops (no context exists here), and
+// the shader program type as a recorder of the float uniforms set on it
+typedef unsigned int GLuint;
+typedef unsigned int GLenum;
+enum { GL_FRAMEBUFFER, GL_COLOR_BUFFER_BIT, GL_TEXTURE_3D, GL_POINTS, GL_TEXTURE0, GL_TEXTURE1, GL_TEXTURE2,
+       GL_TEXTURE3, GL_TEXTURE4 };
+static inline void glBindFramebuffer(GLenum, GLuint) {}
+static inline void glDrawBuffers(int, const GLenum *) {}
+static inline void glClearColor(float, float, float, float) {}
+static inline void glClear(GLenum) {}
+static inline void glActiveTexture(GLenum) {}
+static inline void glBindTexture(GLenum, GLuint) {}
+static inline void glBindVertexArray(GLuint) {}
+static inline void glDrawArrays(GLenum, int, int) {}
+struct Shader {
+    vector<pair<string, float>> floats;
+    void use() {}
+    void setInt(const string &, int) {}
+    void setFloat(const string &name, float v) { floats.push_back(make_pair(name, v)); }
+};
+"""
 
 INIT_GLUE = """
     memcpy(grid_out, grid, sizeof(float) * texel_num);
@@ -441,6 +480,26 @@ extern "C" int ref_stream_initialization(int W, int H, int D, int K, const float
     return n;
 }
 
+// the JFA passes of one Lloyd iteration for base step s: Image::init_variables
+// (compactness 8, ratio), then Image::flood with the uniforms recorded; writes
+// each pass's step and ratio, returns the pass count, *ratio_out the ratio
+extern "C" int ref_flood_ladder(int s_, float *steps, float *ratios, int cap, float *ratio_out)
+{
+    FloodShim f;
+    f.s = s_; f.texel_num = 1; f.current_buffer = 0;
+    f.init_variables();
+    Shader sh;
+    f.flood(sh, 1);
+    int n = 0;
+    for (size_t i = 0; i + 1 < sh.floats.size(); i++)
+        if (sh.floats[i].first == "step" && sh.floats[i + 1].first == "ratio") {
+            if (n < cap) { steps[n] = sh.floats[i].second; ratios[n] = sh.floats[i + 1].second; }
+            n++;
+        }
+    *ratio_out = f.ratio;
+    return n;
+}
+
 extern "C" void ref_sequence_label(int *labels, long n, const long long *counts, int Kp, int dead_seed)
 {
     map<int, int> m;
@@ -483,11 +542,15 @@ def build_host(force=False):
             [os.path.getmtime(f) for f in srcs] + [os.path.getmtime(__file__)]):
         return HOST_LIB
     os.makedirs(OUT, exist_ok=True)
-    parts = ["#include <cmath>\n#include <cstring>\n#include <iostream>\n#include <map>\n"
-             "#include <sstream>\n#include <string>\n#include <vector>\nusing namespace std;\n"
-             "struct Shader {};                         // the GL programs' type, unused here\n"]
+    parts = [HOST_PRELUDE]
     for path, start, shim, members, stop in HOST_FUNCS:
         text = _strip_comments(open(os.path.join(REF, path), encoding="latin-1").read())
+        if "@" in members:                         # more member functions of the same shim
+            members, *more = members.split("@")
+            fns = [_cut_function(text, f) for f in [start] + more]
+            fns = [re.sub(r"\b\w+::(\w+\s*\()", r"\1", f, count=1) for f in fns]
+            parts.append(f"struct {shim} {{\n    {members}\n" + "\n".join(fns) + "\n};\n")
+            continue
         if stop is None:
             fn = _cut_function(text, start)
         elif isinstance(stop, tuple):              # host code, glue, host code to the end

@@ -10,7 +10,8 @@ Image::EnforceLabelConnectivity3D (connectivity.npz), Image::init_seeds
 (seed_grid.npz), Image::sequence_label (sequence_label.npz) and the host
 parts of Image::initialization (density_placement.npz) compiled from its C++,
 and check_dead_seeds' 1-3 dead-seed branch (label_replace.gs with its host
-loop, then sequence_label: few_dead.npz).
+loop, then sequence_label: few_dead.npz) and the JFA pass ladder with its ratio
+uniforms (Image::init_variables and Image::flood: flood_ladder.npz).
 tests/test_golden.py checks the CPU restatement and the CUDA path against
 them.
 """
@@ -153,6 +154,17 @@ def main():
         out = pin.reference_few_dead(lib, host, labels, counts, kp, dead)
         arrays.update({f"labels_{i}": labels, f"counts_{i}": counts, f"kp_{i}": kp, f"out_{i}": out})
     np.savez_compressed(os.path.join(HERE, "few_dead.npz"), **arrays)
+
+    # Image::init_variables + Image::flood: the pass ladder and ratio uniforms
+    n = len(pin.LADDER_S)
+    steps, ratios = np.zeros((n, 64), np.float32), np.zeros((n, 64), np.float32)
+    count, ratio = np.zeros(n, np.int32), np.zeros(n, np.float32)
+    for i, s in enumerate(pin.LADDER_S):
+        st, ra, ratio[i] = pin.reference_ladder(host, s)
+        count[i] = st.size
+        steps[i, :st.size], ratios[i, :st.size] = st, ra
+    np.savez_compressed(os.path.join(HERE, "flood_ladder.npz"), s=np.int32(pin.LADDER_S), count=count,
+                        ratio=ratio, steps=steps, ratios=ratios)
     print("fixtures written to", HERE)
 
 

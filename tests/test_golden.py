@@ -152,3 +152,17 @@ def test_oracle_density_placement(asv):
         n += 1
     assert n >= 5
 
+
+
+def test_oracle_flood_ladder(orc):
+    """the restatement's JFA ladder and ratio against Image::flood's own uniforms"""
+    f = load("flood_ladder.npz")
+    assert f["s"].size >= 100
+    for i, s in enumerate(f["s"]):
+        r = np.float32(orc.ratio(int(s), 8.0))
+        assert r == f["ratio"][i]
+        steps, rmul = orc.ladder(int(s))
+        n = int(f["count"][i])
+        assert len(steps) == n, s
+        assert np.array_equal(np.float32(steps), f["steps"][i, :n]), s
+        assert np.array_equal(np.float32(rmul) * r, f["ratios"][i, :n]), s

@@ -394,3 +394,32 @@ def test_stream_window_placement_matches_reference(ref_grid, orc, asv, W, H, D, 
     seeds = np.zeros((g.Kp, 4), np.float32)
     n = ref_grid.ref_stream_initialization(W, H, D, K, P(dens), P(grid), P(seeds), g.Kp, P(g5))
     assert n == adj.shape[0] and np.array_equal(seeds[:n], adj)
+
+
+LADDER_S = list(range(1, 130)) + [150, 200, 255, 256, 257, 400, 511, 512, 1000]
+
+
+def reference_ladder(lib, s):
+    """the (step, ratio) uniforms of every flood pass of one Lloyd iteration,
+    and the ratio, from Image::init_variables and Image::flood compiled whole"""
+    V = ctypes.c_void_p
+    lib.ref_flood_ladder.argtypes = [ctypes.c_int, V, V, ctypes.c_int, V]
+    lib.ref_flood_ladder.restype = ctypes.c_int
+    steps = np.zeros(64, np.float32)
+    ratios = np.zeros(64, np.float32)
+    r = np.zeros(1, np.float32)
+    n = lib.ref_flood_ladder(s, P(steps), P(ratios), 64, P(r))
+    assert 0 < n <= 64
+    return steps[:n], ratios[:n], r[0]
+
+
+def test_flood_ladder_matches_reference(ref_host, orc):
+    """JFA pass ladder (1, floor(s/2) halving, then 2, 1) and the per-pass ratio
+    uniform, against the reference's own Image::flood for every base step s"""
+    for s in LADDER_S:
+        steps, ratios, r = reference_ladder(ref_host, s)
+        want_r = orc.ratio(s, 8.0)
+        assert np.float32(want_r) == r, s
+        got_steps, rmul = orc.ladder(s)
+        assert np.array_equal(np.float32(got_steps), steps), (s, got_steps, steps)
+        assert np.array_equal(np.float32(rmul) * np.float32(want_r), ratios), s
