@@ -313,6 +313,47 @@ def test_fuzz_corrupt_streams(tmp_path):
             pass
 
 
+def test_sanitized_fuzz(tmp_path):
+    """the decoder built with AddressSanitizer and UndefinedBehaviorSanitizer
+    (tests/png_fuzz.cpp) runs 100 000 damaged files made from a corpus of
+    every colour type, bit depth, interlacing and zlib strategy: no
+    out-of-bounds access, no undefined behaviour, every case a status code"""
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no g++")
+    csrc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                        "anisotropic_supervoxel_gb300", "csrc")
+    inc = os.path.join(os.path.dirname(csrc), "..", "include")
+    exe = str(tmp_path / "png_fuzz")
+    build = subprocess.run([gxx, "-O1", "-g", "-fsanitize=address,undefined", "-fno-sanitize-recover=all",
+                            "-fopenmp", "-I", csrc, "-I", inc,
+                            os.path.join(os.path.dirname(os.path.abspath(__file__)), "png_fuzz.cpp"),
+                            "-o", exe], capture_output=True, text=True)
+    if build.returncode != 0:
+        pytest.skip("sanitizer runtime unavailable: " + build.stderr[-200:])
+    corpus = tmp_path / "corpus"
+    corpus.mkdir()
+    rng = np.random.default_rng(17)
+    n = 0
+    for ctype, depth in COMBOS:
+        for interlace in (0, 1):
+            for W, H in ((1, 1), (7, 5), (33, 17)):
+                comp = STRATEGIES[n % len(STRATEGIES)]
+                s, plte = random_image(rng, W, H, depth, ctype, smooth=bool(n % 2))
+                (corpus / f"c{n:03d}.png").write_bytes(make_png(s, depth, ctype, interlace, plte, comp, rng,
+                                                                idat_pieces=1 + n % 3))
+                n += 1
+    run = subprocess.run([exe, str(corpus), "100000", "7"], capture_output=True, text=True, timeout=600,
+                         env=dict(os.environ, ASAN_OPTIONS="detect_leaks=1"))
+    assert run.returncode == 0, run.stderr[-2000:]
+    counts = [int(v) for v in run.stdout.split()[3:4] + run.stdout.split()[5:]]
+    ok, fails = counts[0], counts[1:]
+    assert ok > 5000 and sum(fails) > 50000 and ok + sum(fails) == 100000, run.stdout
+    assert fails[0] == fails[1] == fails[2] == fails[6] == fails[7] == 0, run.stdout   # only -3, -4, -5
+
+
 def test_frames_and_render_files(tmp_path):
     rng = np.random.default_rng(2)
     frames = rng.integers(0, 256, (5, 12, 16, 3), dtype=np.uint8)
