@@ -14,8 +14,8 @@
 // PSD matrix.
 //
 // One warp per solve: lane i holds row i of the system; column dot products
-// are accumulated row by row in order (shuffles), so every lane computes the
-// same scalars with the same operation sequence as a sequential solver.
+// are butterfly sums over the lanes (asv_lane_sum), which leave the same bits
+// on every lane, so all lanes apply the same rotations.
 // Launches: k_metric_self (a warp per seed), k_metric_psd (a thread per
 // solve: the FP64 PSD tests), k_metric_ring (a warp per seed and neighbour,
 // only for non-PSD seeds), k_metric_psd again, k_metric_combine (a thread per
@@ -30,19 +30,17 @@
 #define SVD_SWEEPS 30
 #define FULL 0xffffffffu
 
-#define ASV_MAX_ROWS 18      // 9 neighbours x (forward, backward)
-
-// Sequential sum over rows 0..m-1 of a per-lane value.  Lanes at or beyond
-// m hold +0 (their rows are zero), and adding +0 leaves any sum that is not
-// -0 unchanged; these sums start at +0 and, in round-to-nearest, never reach
-// -0.  So the loop always runs ASV_MAX_ROWS rows, fully unrolled: every
-// shuffle is issued up front and only the additions form a chain.
-__device__ __forceinline__ float asv_row_sum(float v)
+// Sum of a per-lane value over the warp as a butterfly: at each level a lane
+// adds its partner's partial sum (lane ^ 16, 8, 4, 2, 1) to its own.  Both
+// partners add the same two operands and IEEE addition commutes, so every
+// lane ends with the same bits: slot i takes t[i] + t[i + off] for
+// off = 16, 8, 4, 2, 1 over the 32 slots (rows 0..m-1, then +0), the order
+// the oracle restates.  Lanes at or beyond m hold +0 (their rows are zero).
+__device__ __forceinline__ float asv_lane_sum(float v)
 {
-    float a = 0.0f;
 #pragma unroll
-    for (int i = 0; i < ASV_MAX_ROWS; i++) a = a + __shfl_sync(FULL, v, i);
-    return a;
+    for (int off = 16; off > 0; off >>= 1) v = v + __shfl_xor_sync(FULL, v, off);
+    return v;
 }
 
 // min-norm least squares in FP32; u = this lane's row (zero beyond m),
@@ -59,14 +57,9 @@ __device__ void asv_lsq_minnorm_warp(int m, float u[6], float bl, float x[6])
         for (int p = 0; p < 5; p++)
 #pragma unroll
             for (int q = p + 1; q < 6; q++) {
-                const float pa = u[p] * u[p], pb = u[q] * u[q], pg = u[p] * u[q];
-                float al = 0.0f, be = 0.0f, ga = 0.0f;
-#pragma unroll
-                for (int i = 0; i < ASV_MAX_ROWS; i++) {      // rows >= m add +0 (asv_row_sum)
-                    al = al + __shfl_sync(FULL, pa, i);
-                    be = be + __shfl_sync(FULL, pb, i);
-                    ga = ga + __shfl_sync(FULL, pg, i);
-                }
+                const float al = asv_lane_sum(u[p] * u[p]);
+                const float be = asv_lane_sum(u[q] * u[q]);
+                const float ga = asv_lane_sum(u[p] * u[q]);
                 if (ga == 0.0f) continue;
                 if (fabsf(ga) <= FLT_EPSILON * sqrtf(al * be)) continue;
                 float zeta = (be - al) / (2.0f * ga);
@@ -87,7 +80,7 @@ __device__ void asv_lsq_minnorm_warp(int m, float u[6], float bl, float x[6])
     float sig[6], smax = 0.0f;
 #pragma unroll
     for (int j = 0; j < 6; j++) {
-        sig[j] = sqrtf(asv_row_sum(u[j] * u[j]));
+        sig[j] = sqrtf(asv_lane_sum(u[j] * u[j]));
         if (sig[j] > smax) smax = sig[j];
     }
     float thr = smax * ((float)(m < 6 ? m : 6) * FLT_EPSILON);
@@ -96,7 +89,7 @@ __device__ void asv_lsq_minnorm_warp(int m, float u[6], float bl, float x[6])
 #pragma unroll
     for (int j = 0; j < 6; j++) {
         if (!(sig[j] >= thr)) continue;
-        float ub = asv_row_sum(u[j] * bl);
+        float ub = asv_lane_sum(u[j] * bl);
         float coef = (ub / sig[j]) / sig[j];
         xr = xr + v[j] * coef;
     }

@@ -296,24 +296,38 @@ int orc_density_adjust(const uint8_t *rgb, int W, int H, int D, const float *gri
  * Min-norm least squares in FP32, the reference's precision (it calls
  * Eigen's float BDCSVD::solve, :946-961), computed here with a one-sided
  * Jacobi SVD and Eigen's rank rule: keep singular values
- * >= max(sigma_max * min(m,6) * FLT_EPSILON, FLT_MIN).
+ * >= max(sigma_max * min(m,6) * FLT_EPSILON, FLT_MIN).  Column dot products
+ * are summed in a fixed pairwise order (lane_sum).
  * ==================================================================== */
 #define SVD_SWEEPS 30
 
+/* Sum of v[0..m-1] in the CUDA solver's warp butterfly order: 32 slots
+ * (the values, then +0); for off = 16, 8, 4, 2, 1 slot i < off takes
+ * t[i] + t[i + off]; the sum is slot 0. */
+static float lane_sum(const float *v, int m)
+{
+    float t[32];
+    for (int i = 0; i < 32; i++) t[i] = i < m ? v[i] : 0.0f;
+    for (int off = 16; off > 0; off >>= 1)
+        for (int i = 0; i < off; i++) t[i] = t[i] + t[i + off];
+    return t[0];
+}
+
 static void lsq_minnorm(int m, float U[18][6], const float *b, float x[6])
 {
+    float tmp[18];
     float V[6][6];
     for (int r = 0; r < 6; r++) for (int c = 0; c < 6; c++) V[r][c] = r == c ? 1.0f : 0.0f;
     for (int sw = 0; sw < SVD_SWEEPS; sw++) {
         int rot = 0;
         for (int p = 0; p < 5; p++)
             for (int q = p + 1; q < 6; q++) {
-                float al = 0.0f, be = 0.0f, ga = 0.0f;
-                for (int i = 0; i < m; i++) {
-                    al = al + U[i][p] * U[i][p];
-                    be = be + U[i][q] * U[i][q];
-                    ga = ga + U[i][p] * U[i][q];
-                }
+                for (int i = 0; i < m; i++) tmp[i] = U[i][p] * U[i][p];
+                const float al = lane_sum(tmp, m);
+                for (int i = 0; i < m; i++) tmp[i] = U[i][q] * U[i][q];
+                const float be = lane_sum(tmp, m);
+                for (int i = 0; i < m; i++) tmp[i] = U[i][p] * U[i][q];
+                const float ga = lane_sum(tmp, m);
                 if (ga == 0.0f) continue;
                 if (fabsf(ga) <= FLT_EPSILON * sqrtf(al * be)) continue;
                 float zeta = (be - al) / (2.0f * ga);
@@ -337,9 +351,8 @@ static void lsq_minnorm(int m, float U[18][6], const float *b, float x[6])
     }
     float sig[6], smax = 0.0f;
     for (int j = 0; j < 6; j++) {
-        float a = 0.0f;
-        for (int i = 0; i < m; i++) a = a + U[i][j] * U[i][j];
-        sig[j] = sqrtf(a);
+        for (int i = 0; i < m; i++) tmp[i] = U[i][j] * U[i][j];
+        sig[j] = sqrtf(lane_sum(tmp, m));
         if (sig[j] > smax) smax = sig[j];
     }
     float thr = smax * ((float)(m < 6 ? m : 6) * FLT_EPSILON);
@@ -347,8 +360,8 @@ static void lsq_minnorm(int m, float U[18][6], const float *b, float x[6])
     for (int r = 0; r < 6; r++) x[r] = 0.0f;
     for (int j = 0; j < 6; j++) {
         if (!(sig[j] >= thr)) continue;
-        float ub = 0.0f;
-        for (int i = 0; i < m; i++) ub = ub + U[i][j] * b[i];
+        for (int i = 0; i < m; i++) tmp[i] = U[i][j] * b[i];
+        const float ub = lane_sum(tmp, m);
         float coef = (ub / sig[j]) / sig[j];
         for (int r = 0; r < 6; r++) x[r] = x[r] + V[r][j] * coef;
     }
