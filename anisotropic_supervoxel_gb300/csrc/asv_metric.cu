@@ -220,39 +220,43 @@ __device__ void asv_metric_solve_warp(const float2 *__restrict__ fwd, const floa
                                       int W, int H, int D, float sx, float sy, int frame, float M[6])
 {
     const int lane = threadIdx.x & 31;
-    const float expected_b[9] = { 3, 2, 3, 2, 1, 2, 3, 2, 3 };
+    // rows: each in-bounds neighbour in order gives a forward row (unless
+    // the last frame) then a backward row (unless the first frame); lane r
+    // finds its row's neighbour and direction, so all flow reads issue at once
+    const bool hf = frame != D - 1, hb = frame != 0;     // D >= 2: at least one
+    const int per = (int)hf + (int)hb;
+    unsigned inb = 0;
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+        const int nx = (int)sx + (k % 3 - 1), ny = (int)sy + (k / 3 - 1);
+        if (nx >= 0 && nx < W && ny >= 0 && ny < H) inb |= 1u << k;
+    }
+    const int m = per * __popc(inb);
     float u[6] = { 0, 0, 0, 0, 0, 0 }, bl = 0.0f;
-    int m = 0, id_b = 0;
-    for (int oy = -1; oy < 2; oy++)
-        for (int ox = -1; ox < 2; ox++, id_b++) {
-            int nx = (int)sx + ox, ny = (int)sy + oy;
-            if (!(nx >= 0 && nx < W && ny >= 0 && ny < H)) continue;
-            long long o = ((long long)frame * H + ny) * W + nx;
-            if (frame != D - 1) {
-                if (lane == m) {
-                    float2 f = __ldg(fwd + o);
-                    float dx = (float)ox + asv_round_half_up(f.x);
-                    float dy = (float)oy + asv_round_half_up(f.y);
-                    u[0] = dx * dx; u[1] = 2.0f * dx * dy;
-                    u[2] = 2.0f * dx; u[3] = dy * dy;
-                    u[4] = 2.0f * dy; u[5] = 1.0f;
-                    bl = expected_b[id_b];
-                }
-                m++;
-            }
-            if (frame != 0) {
-                if (lane == m) {
-                    float2 f = __ldg(bwd + o);
-                    float dx = asv_round_half_up(f.x) + (float)ox;
-                    float dy = asv_round_half_up(f.y) + (float)oy;
-                    u[0] = dx * dx; u[1] = 2.0f * dx * dy;
-                    u[2] = -2.0f * dx; u[3] = dy * dy;
-                    u[4] = -2.0f * dy; u[5] = 1.0f;
-                    bl = expected_b[id_b];
-                }
-                m++;
-            }
+    if (lane < m) {
+        const int j = per == 2 ? lane >> 1 : lane;
+        const bool back = per == 2 ? (lane & 1) != 0 : hb;
+        unsigned rest = inb;
+        for (int k = 0; k < j; k++) rest &= rest - 1;    // drop the j lower neighbours
+        const int id_b = __ffs(rest) - 1;
+        const int ox = id_b % 3 - 1, oy = id_b / 3 - 1;
+        const long long o = ((long long)frame * H + ((int)sy + oy)) * W + ((int)sx + ox);
+        const float2 f = __ldg((back ? bwd : fwd) + o);
+        if (!back) {
+            float dx = (float)ox + asv_round_half_up(f.x);
+            float dy = (float)oy + asv_round_half_up(f.y);
+            u[0] = dx * dx; u[1] = 2.0f * dx * dy;
+            u[2] = 2.0f * dx; u[3] = dy * dy;
+            u[4] = 2.0f * dy; u[5] = 1.0f;
+        } else {
+            float dx = asv_round_half_up(f.x) + (float)ox;
+            float dy = asv_round_half_up(f.y) + (float)oy;
+            u[0] = dx * dx; u[1] = 2.0f * dx * dy;
+            u[2] = -2.0f * dx; u[3] = dy * dy;
+            u[4] = -2.0f * dy; u[5] = 1.0f;
         }
+        bl = (float)(ox * ox + oy * oy + 1);             // expected_b of :884: 3 2 3 / 2 1 2 / 3 2 3
+    }
     float x[6];
     if (m == 0) {
         for (int k = 0; k < 6; k++) x[k] = 0.0f;
