@@ -239,6 +239,21 @@ def test_clip_extremes_bit_exact(asv, orc, W, H, D, K):
     img.close()
 
 
+def test_clip_full_size_bit_exact(asv, orc):
+    """a 1280x720x36 clip (33.2 M voxels, next to the 2^25-voxel limit of the
+    fixed-memory path) with K=2000, two Lloyd iterations: labels identical
+    before and after post-processing"""
+    W, H, D, K = 1280, 720, 36, 2000
+    rgb, fwd, bwd = asv.synth_clip(W, H, D, n_ellipses=60, noise_sigma=5.0, vmax=3.0, seed=20240605)
+    img = _gpu_clip(asv, rgb, fwd, bwd, K, 2)
+    img.run_lloyd()
+    labels, raw, seeds, info = orc.run_clip(rgb, fwd, bwd, K, iters=2, nthreads=16)
+    assert img.info().Kp == seeds.shape[0] == info["Kp"]
+    assert np.array_equal(img.raw_labels(), raw)
+    assert np.array_equal(img.labels(), labels)
+    img.close()
+
+
 @pytest.mark.parametrize("W,H,D,K", [(64, 48, 12, 60), (90, 50, 8, 120)])
 def test_clip_middlebury_bit_exact(asv, orc, W, H, D, K):
     """middlebury = 1: base step s = floor(sqrt(W*H/K)) (GPU-AS/Image.cpp:25-29)."""

@@ -34,3 +34,17 @@ def test_stream_matches_oracle(asv, orc, W, H, D, seeds100, iters):
     assert placed == info["placed"]
     assert (got != -7).all()
     assert np.array_equal(got, want)
+
+
+def test_stream_720p_windows_match_oracle(asv, orc):
+    """the 1280x720 streaming configuration (windows of 30 frames, 10 overlap,
+    seeds_num_100 = 10000) over its first two windows, three Lloyd
+    iterations each: video-wide labels identical"""
+    rgb, fwd, bwd = asv.synth_clip(1280, 720, 50, n_ellipses=60, noise_sigma=5.0, vmax=3.0,
+                                   drift_amp=6.0, drift_period=90.0, seed=20240604)
+    got, nb, placed = _run_stream(asv, rgb, fwd, bwd, 10000, 3)
+    want, info = orc.run_stream(rgb, fwd, bwd, seeds_num_100=10000, iters=3, nthreads=16)
+    assert nb == info["blocks"] == 2
+    assert placed == info["placed"]
+    assert (got != -7).all()
+    assert np.array_equal(got, want)
