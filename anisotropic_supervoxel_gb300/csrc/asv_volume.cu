@@ -413,11 +413,13 @@ __global__ void k_draw(AsvDev d)
     if (i >= S.Kp) return;
     float4 p = d.pos[g], c = d.slab[g];
     const float *m = d.M + 8 * g;
-    // table: (x, y, z, L) (a, b, M00, 2M01) (2M02, M11, 2M12, M22); doubling
-    // is exact, so (dx*dy)*(2*M01) == ((2*dx)*dy)*M01 (flood.gs:85).
-    d.jtab[3 * g + 0] = make_float4(p.x, p.y, p.z, c.x);
-    d.jtab[3 * g + 1] = make_float4(c.y, c.z, m[0], 2.0f * m[1]);
-    d.jtab[3 * g + 2] = make_float4(2.0f * m[2], m[3], 2.0f * m[4], m[5]);
+    // table: (-x, -y, -z, -L) (M00, M11, 2M01, 2M12) (2M02, M22, -a, -b),
+    // laid out for asv_jfa_dist's paired operations.  v - s == v + (-s) in
+    // IEEE arithmetic, and doubling is exact, so
+    // (dx*dy)*(2*M01) == ((2*dx)*dy)*M01 (flood.gs:85).
+    d.jtab[3 * g + 0] = make_float4(-p.x, -p.y, -p.z, -c.x);
+    d.jtab[3 * g + 1] = make_float4(m[0], m[3], 2.0f * m[1], 2.0f * m[4]);
+    d.jtab[3 * g + 2] = make_float4(2.0f * m[2], m[5], -c.y, -c.z);
     if (!(p.x >= 0.0f && p.y >= 0.0f && p.z >= 0.0f)) return;
     int x = (int)p.x, y = (int)p.y, z = (int)p.z;
     if (x >= S.W || y >= S.H || z >= S.D) return;
@@ -509,23 +511,34 @@ __device__ __forceinline__ int asv_merge_lists(const asv_list_t *__restrict__ A,
     return nx;
 }
 
-// flood.gs:72-94: anisotropic distance of the voxel centre (vx, vy, vz) with
-// LAB (cL, ca, cb) to seed l of the table, in the shader's operation order
-__device__ __forceinline__ float asv_jfa_dist(const float4 *__restrict__ tab, int l, float vx, float vy,
-                                              float vz, float cL, float ca, float cb, float ratio)
+// flood.gs:72-94: anisotropic distance of the voxel centre to seed l of the
+// table, in the shader's operation order.  The voxel side comes packed as
+// vxy = (x, y), vzl = (z, L), vab = (a, b); the table holds the seed's
+// negated position and colour, so the six differences are three two-wide
+// FP32 additions (__fadd2_rn: each half rounds like the scalar addition, and
+// v + (-s) is v - s).  Only these additions are paired: their operands are
+// loads, never products, so nothing can be fused into them.  Products and
+// the sums they feed stay scalar (kept apart by -fmad=false): a two-wide
+// product feeding a two-wide sum is fused into a two-wide FMA by the
+// assembler even when both are written with explicit .rn rounding, which
+// changes the result.
+__device__ __forceinline__ float asv_jfa_dist(const float4 *__restrict__ tab, int l, float2 vxy, float2 vzl,
+                                              float2 vab, float ratio)
 {
     const float4 t0 = __ldg(tab + 3 * l), t1 = __ldg(tab + 3 * l + 1), t2 = __ldg(tab + 3 * l + 2);
-    const float dx = vx - t0.x, dy = vy - t0.y, dz = vz - t0.z;
-    float p1 = (dx * dx) * t1.z + (dx * dy) * t1.w;                  // flood.gs:85
+    const float2 dxy = __fadd2_rn(vxy, make_float2(t0.x, t0.y));              // (dx, dy)
+    const float2 dzl = __fadd2_rn(vzl, make_float2(t0.z, t0.w));              // (dz, eL)
+    const float2 eab = __fadd2_rn(vab, make_float2(t2.z, t2.w));              // (ea, eb)
+    const float dx = dxy.x, dy = dxy.y, dz = dzl.x;
+    float p1 = (dx * dx) * t1.x + (dx * dy) * t1.z;                            // flood.gs:85
     p1 = p1 + (dx * dz) * t2.x;
-    float p2 = (dy * dy) * t2.y + (dy * dz) * t2.z;
-    p2 = p2 + (dz * dz) * t2.w;
+    float p2 = (dy * dy) * t1.y + (dy * dz) * t1.w;
+    p2 = p2 + (dz * dz) * t2.y;
     float pos = p1 + p2;
-    const float eL = cL - t0.w, ea = ca - t1.x, eb = cb - t1.y;
-    float col = eL * eL + ea * ea;                                     // flood.gs:89
-    col = col + eb * eb;
-    pos = (pos < 0.0f) ? 0.0f : pos;                                   // flood.gs:90-93
-    return ratio * pos + col;                                          // flood.gs:94
+    float col = dzl.y * dzl.y + eab.x * eab.x;                                 // flood.gs:89
+    col = col + eab.y * eab.y;
+    pos = (pos < 0.0f) ? 0.0f : pos;                                           // flood.gs:90-93
+    return ratio * pos + col;                                                  // flood.gs:94
 }
 
 // distance loop over the concatenated lists A (na) and X (nx): the first
@@ -535,7 +548,8 @@ __device__ __forceinline__ int32_t asv_jfa_eval(const asv_list_t *__restrict__ A
                                                 const float4 *__restrict__ tab, uchar4 c, float vx, float vy,
                                                 float vz, float ratio)
 {
-    const float cL = (float)c.x, ca = (float)c.y, cb = (float)c.z;
+    const float2 vxy = make_float2(vx, vy), vzl = make_float2(vz, (float)c.x);
+    const float2 vab = make_float2((float)c.y, (float)c.z);
     float mind = 100000000.0f;
     int32_t best = -1;
     const int n = na + nx;
@@ -543,14 +557,14 @@ __device__ __forceinline__ int32_t asv_jfa_eval(const asv_list_t *__restrict__ A
     for (; i + 1 < n; i += 2) {          // two candidates per trip: their loads overlap
         const int32_t la = i < na ? A[i * ASV_JFA_THREADS] : X[(i - na) * ASV_JFA_THREADS];
         const int32_t lb = i + 1 < na ? A[(i + 1) * ASV_JFA_THREADS] : X[(i + 1 - na) * ASV_JFA_THREADS];
-        const float da = asv_jfa_dist(tab, la, vx, vy, vz, cL, ca, cb, ratio);
-        const float db = asv_jfa_dist(tab, lb, vx, vy, vz, cL, ca, cb, ratio);
+        const float da = asv_jfa_dist(tab, la, vxy, vzl, vab, ratio);
+        const float db = asv_jfa_dist(tab, lb, vxy, vzl, vab, ratio);
         if (da < mind) { mind = da; best = la; }     // compared in list order
         if (db < mind) { mind = db; best = lb; }
     }
     if (i < n) {
         const int32_t l = i < na ? A[i * ASV_JFA_THREADS] : X[(i - na) * ASV_JFA_THREADS];
-        const float dist = asv_jfa_dist(tab, l, vx, vy, vz, cL, ca, cb, ratio);
+        const float dist = asv_jfa_dist(tab, l, vxy, vzl, vab, ratio);
         if (dist < mind) { mind = dist; best = l; }
     }
     return best;
