@@ -152,6 +152,7 @@ struct asv_ctx {
     // state
     bool have_rgb = false, have_flow = false, have_pos0 = false, have_M0 = false, have_lab = false;
     bool seeded = false, ran = false;
+    bool drawn = false;          // labA holds a fresh seed draw: the first pass may scatter
     int post_host[ASV_POST_WORDS];
     // graph
     cudaGraphExec_t gexec = nullptr;
@@ -235,7 +236,7 @@ static void free_layout(asv_ctx *ctx)
     ctx->bytes = 0;
     ctx->d = AsvDev{};
     ctx->have_rgb = ctx->have_flow = ctx->have_pos0 = ctx->have_M0 = ctx->have_lab = false;
-    ctx->seeded = ctx->ran = false;
+    ctx->seeded = ctx->ran = ctx->drawn = false;
     ctx->sm.on = false;
 }
 
@@ -293,8 +294,8 @@ size_t asv_layout_bytes(const std::vector<SegHost> &seg)
         seeds += (size_t)((s.Kp + 64 + 31) / 32) * 32;
         cells += s.W + s.H + s.D + 2 * s.g.wNum;
     }
-    // rgb 3 + lab 4 + fwd/bwd 16 + two label buffers 8
-    size_t per_vox = 3 + 4 + 8 + 8 + 4 + 4;
+    // rgb 3 + lab 4 + fwd/bwd 16 + two label buffers 8 + first-pass keys 8
+    size_t per_vox = 3 + 4 + 8 + 8 + 4 + 4 + 8;
     // float4 pos0/pos/slab/grid, 8-float M0/M/Mself/Mmemo, jtab 3 float4, 8 u64
     // sums, int neg/mkey/rank, u64 dacc, the metric ring
     size_t per_seed = 4 * 16 + 4 * 32 + 3 * 16 + 8 * 8 + 3 * 4 + 8 + ASV_RING * (32 + 4);
@@ -371,6 +372,8 @@ asv_status asv_build_layout(asv_ctx *ctx)
     AL(d.bwd, (size_t)vox);
     AL(d.labA, (size_t)vox);
     AL(d.labB, (size_t)vox);
+    AL(d.jkeys, (size_t)vox);
+    CK(cudaMemsetAsync(d.jkeys, 0xff, sizeof(unsigned long long) * (size_t)vox, ctx->st));
     AL(d.pos0, seeds); AL(d.M0, (size_t)seeds * 8);
     AL(d.pos, seeds); AL(d.slab, seeds); AL(d.M, (size_t)seeds * 8);
     AL(d.jtab, (size_t)seeds * 3);
@@ -437,6 +440,7 @@ static void do_first_init(asv_ctx *ctx)
     asv_launch_first_init(ctx->d, ctx->st);
     cudaMemsetAsync(ctx->d.labA, 0xff, sizeof(int32_t) * (size_t)ctx->d.total_chunks * ASV_CHUNK, ctx->st);
     asv_launch_draw(ctx->d, ctx->st);
+    ctx->drawn = true;
     ctx->launches += 2;
 }
 
@@ -446,10 +450,16 @@ static void do_flood(asv_ctx *ctx, int evbase)
     cudaMemsetAsync(ctx->d.sums, 0, sizeof(unsigned long long) * 8 * (size_t)ctx->d.total_seeds, ctx->st);
     for (int p = 0; p < ctx->maxpass; p++) {
         if (evbase >= 0) rec_begin(ctx, evbase + 2 * p);
-        asv_launch_jfa(ctx->d, p, ctx->jfa_blocks, ctx->st);
+        if (p == 0 && ctx->drawn) {
+            asv_launch_jfa_first_scatter(ctx->d, ctx->st);   // step 1 from the drawn seeds
+            ctx->launches += 2;
+        } else {
+            asv_launch_jfa(ctx->d, p, ctx->jfa_blocks, ctx->st);
+            ctx->launches++;
+        }
         if (evbase >= 0) rec_begin(ctx, evbase + 2 * p + 1);
-        ctx->launches++;
     }
+    ctx->drawn = false;
 }
 
 // the reseed of centroids_next_seeds (the sums came with the flood)
@@ -471,6 +481,7 @@ static void do_next_seeds(asv_ctx *ctx)
     asv_launch_metric(ctx->d, 1, ctx->st);
     cudaMemsetAsync(ctx->d.labA, 0xff, sizeof(int32_t) * (size_t)ctx->d.total_chunks * ASV_CHUNK, ctx->st);
     asv_launch_draw(ctx->d, ctx->st);
+    ctx->drawn = true;
     ctx->launches += 6;       // five metric kernels + the seed draw
 }
 
@@ -824,16 +835,21 @@ asv_status asv_run_lloyd(asv_ctx *ctx)
         CK(cudaEventRecord(ctx->ev[tot + 1], ctx->st));
         CK(cudaGetLastError());
         CK(cudaEventSynchronize(ctx->ev[tot + 1]));
+        // every iteration draws its seeds, so its first pass is the seed
+        // scatter; jfa_ms / jfa_launches cover the k_jfa gather passes
         double jfa = 0.0;
+        int gathers = 0;
         for (size_t k = 0; k < tot; k += 2) {
+            if ((k / 2) % (size_t)ctx->maxpass == 0) continue;
             float ms = 0.f;
             CK(cudaEventElapsedTime(&ms, ctx->ev[k], ctx->ev[k + 1]));
             jfa += ms;
+            gathers++;
         }
         float all = 0.f;
         CK(cudaEventElapsedTime(&all, ctx->ev[tot], ctx->ev[tot + 1]));
         ctx->stats.jfa_ms = jfa;
-        ctx->stats.jfa_launches = (int)(tot / 2);
+        ctx->stats.jfa_launches = gathers;
         ctx->stats.total_ms = all;
         ctx->stats.launches = ctx->launches;
     } else if (ctx->cfg.use_graph) {

@@ -672,6 +672,88 @@ __global__ void __launch_bounds__(ASV_JFA_THREADS, 3) k_jfa(AsvDev d, int pass,
     }
 }
 
+// ---------------------------------------------------------------------------
+// The first pass of a Lloyd iteration as a scatter from the seeds.  Its input
+// is the drawn seed volume: -1 everywhere but at the seed voxels, each
+// holding the seed that won its voxel.  At step 1 a voxel's candidates are
+// the seeds within its 3x3x3 neighbourhood (clamped to the edges), so instead
+// of every voxel gathering 27 mostly empty labels, each drawn seed visits the
+// up to 27 voxels around it.  The winner rule of the gather (least distance,
+// the first of equal ones in the shader's candidate order) becomes a 64-bit
+// minimum per voxel over keys (distance bits, candidate rank, label):
+// distances are >= +0, so their bits order like their values, and the rank is
+// the seed's first position in the voxel's candidate order (slices z, z-1,
+// z+1; rows y-1..y+1; columns x-1..x+1), which with edge clamping can be an
+// earlier offset than the plain one.  A distance that is not below 1e8 (or
+// NaN) never wins (flood.gs:63, :95-99).  The output volume is filled with
+// -1 first; k_jfa_first_take then hands each touched voxel's key to exactly
+// one thread (atomicExch leaves the key empty for the next iteration), which
+// writes the label.
+// ---------------------------------------------------------------------------
+#define ASV_KEY_EMPTY 0xffffffffffffffffull
+
+// first rank, in the order `order` of offsets, of an offset o with
+// clamp(v + o) == s along one axis of length n
+__device__ __forceinline__ int asv_first_rank(int v, int s, int n, const int order[3])
+{
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+        const int q = min(max(v + order[r], 0), n - 1);
+        if (q == s) return r;
+    }
+    return 3;    // not reached: s lies within one step of v
+}
+
+// thread -> (drawn seed, offset); false when the seed lost its voxel or the
+// voxel lies outside the segment
+__device__ __forceinline__ bool asv_first_target(const AsvDev &d, long long t, int &si, int &i, int &x, int &y,
+                                                 int &z, int &sx, int &sy, int &sz)
+{
+    const int g = (int)(t / 27), o = (int)(t - (long long)g * 27);
+    if (g >= d.total_seeds) return false;
+    si = asv_seed_seg(d, g, i);
+    const SegDesc &S = d.segs[si];
+    if (i >= S.Kp) return false;
+    const float4 p = d.pos[g];
+    if (!(p.x >= 0.0f && p.y >= 0.0f && p.z >= 0.0f)) return false;     // as k_draw
+    sx = (int)p.x; sy = (int)p.y; sz = (int)p.z;
+    if (sx >= S.W || sy >= S.H || sz >= S.D) return false;
+    if (d.labA[S.vox_off + ((long long)sz * S.H + sy) * S.W + sx] != i) return false;   // lost the draw
+    x = sx + (o % 3 - 1); y = sy + ((o / 3) % 3 - 1); z = sz + (o / 9 - 1);
+    return x >= 0 && x < S.W && y >= 0 && y < S.H && z >= 0 && z < S.D;
+}
+
+__global__ void __launch_bounds__(256) k_jfa_first_scatter(AsvDev d)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int si, i, x, y, z, sx, sy, sz;
+    if (!asv_first_target(d, t, si, i, x, y, z, sx, sy, sz)) return;
+    const SegDesc &S = d.segs[si];
+    const int xy_order[3] = { -1, 0, 1 }, z_order[3] = { 0, -1, 1 };
+    const int rank = asv_first_rank(z, sz, S.D, z_order) * 9 + asv_first_rank(y, sy, S.H, xy_order) * 3 +
+                     asv_first_rank(x, sx, S.W, xy_order);
+    const long long v = ((long long)z * S.H + y) * S.W + x;
+    const uchar4 c = __ldg(d.lab + S.vox_off + v);
+    const float dist = asv_jfa_dist(d.jtab + 3 * S.seed_off, i, make_float2((float)x + 0.5f, (float)y + 0.5f),
+                                    make_float2((float)z + 0.5f, (float)c.x), make_float2((float)c.y, (float)c.z),
+                                    S.ratio[0]);
+    if (!(dist < 100000000.0f)) return;
+    const unsigned long long key = ((unsigned long long)__float_as_uint(dist) << 32) |
+                                   ((unsigned long long)rank << 16) | (unsigned long long)i;
+    atomicMin(d.jkeys + S.vox_off + v, key);
+}
+
+__global__ void __launch_bounds__(256) k_jfa_first_take(AsvDev d)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int si, i, x, y, z, sx, sy, sz;
+    if (!asv_first_target(d, t, si, i, x, y, z, sx, sy, sz)) return;
+    const SegDesc &S = d.segs[si];
+    const long long v = S.vox_off + ((long long)z * S.H + y) * S.W + x;
+    const unsigned long long key = atomicExch(d.jkeys + v, ASV_KEY_EMPTY);
+    if (key != ASV_KEY_EMPTY) d.labB[v] = (int32_t)(key & 0x7fffu);
+}
+
 // single-segment pass with explicit step and ratio (test entry point)
 __global__ void __launch_bounds__(ASV_JFA_THREADS) k_jfa_single(AsvDev d, const int32_t *__restrict__ in,
                                                                 int32_t *__restrict__ out, int step,
@@ -1105,6 +1187,15 @@ void asv_launch_jfa(const AsvDev &d, int pass, int grid_blocks, cudaStream_t st)
     const int32_t *in = (pass & 1) ? d.labB : d.labA;
     int32_t *out = (pass & 1) ? d.labA : d.labB;
     k_jfa<<<grid_blocks, 256, 0, st>>>(d, pass, in, out);
+}
+
+void asv_launch_jfa_first_scatter(const AsvDev &d, cudaStream_t st)
+{
+    cudaMemsetAsync(d.labB, 0xff, sizeof(int32_t) * (size_t)d.total_chunks * ASV_CHUNK, st);
+    const long long threads = 27LL * d.total_seeds;
+    const int blocks = (int)((threads + 255) / 256);
+    k_jfa_first_scatter<<<blocks, 256, 0, st>>>(d);
+    k_jfa_first_take<<<blocks, 256, 0, st>>>(d);
 }
 
 void asv_launch_jfa_single(const AsvDev &d, const int32_t *in, int32_t *out, int step, float ratio,

@@ -85,7 +85,8 @@ typedef struct asv_info {
 } asv_info;
 
 typedef struct asv_stats {
-    double jfa_ms;      /* summed device time of the JFA passes of the last run */
+    double jfa_ms;      /* summed device time of the k_jfa gather passes of the last run
+                           (every pass but each iteration's first, a seed scatter) */
     int jfa_launches;
     double centroid_ms;
     double metric_ms;
