@@ -298,7 +298,7 @@ size_t asv_layout_bytes(const std::vector<SegHost> &seg)
     size_t per_vox = 3 + 4 + 8 + 8 + 4 + 4 + 8;
     // float4 pos0/pos/slab/grid, 8-float M0/M/Mself/Mmemo, jtab 3 float4, 8 u64
     // sums, int neg/mkey/rank, u64 dacc, the metric ring
-    size_t per_seed = 4 * 16 + 4 * 32 + 3 * 16 + 8 * 8 + 3 * 4 + 8 + ASV_RING * (32 + 4);
+    size_t per_seed = 4 * 16 + 4 * 32 + 3 * 16 + 8 * 8 + 3 * 4 + 8 + ASV_RING * (32 + 4) + 27 * 8;
     // each of the ~30 allocations rounds up to 256 bytes
     size_t fixed = 32 * 256 + 256 * 4 + 16;
     size_t per_seg = sizeof(SegDesc) + 3 * 4 + ASV_POST_WORDS * 4;
@@ -373,6 +373,8 @@ asv_status asv_build_layout(asv_ctx *ctx)
     AL(d.labA, (size_t)vox);
     AL(d.labB, (size_t)vox);
     AL(d.jkeys, (size_t)vox);
+    AL(d.tlist, (size_t)seeds * 27);
+    AL(d.tcount, 1);
     CK(cudaMemsetAsync(d.jkeys, 0xff, sizeof(unsigned long long) * (size_t)vox, ctx->st));
     AL(d.pos0, seeds); AL(d.M0, (size_t)seeds * 8);
     AL(d.pos, seeds); AL(d.slab, seeds); AL(d.M, (size_t)seeds * 8);
@@ -452,6 +454,9 @@ static void do_flood(asv_ctx *ctx, int evbase)
         if (evbase >= 0) rec_begin(ctx, evbase + 2 * p);
         if (p == 0 && ctx->drawn) {
             asv_launch_jfa_first_scatter(ctx->d, ctx->st);   // step 1 from the drawn seeds
+            ctx->launches += 2;
+        } else if (p == 1 && ctx->drawn) {
+            asv_launch_jfa_second_scatter(ctx->d, ctx->st);  // from the first pass's sparse labels
             ctx->launches += 2;
         } else {
             asv_launch_jfa(ctx->d, p, ctx->jfa_blocks, ctx->st);
@@ -835,12 +840,12 @@ asv_status asv_run_lloyd(asv_ctx *ctx)
         CK(cudaEventRecord(ctx->ev[tot + 1], ctx->st));
         CK(cudaGetLastError());
         CK(cudaEventSynchronize(ctx->ev[tot + 1]));
-        // every iteration draws its seeds, so its first pass is the seed
-        // scatter; jfa_ms / jfa_launches cover the k_jfa gather passes
+        // every iteration draws its seeds, so its first two passes are the
+        // scatters; jfa_ms / jfa_launches cover the k_jfa gather passes
         double jfa = 0.0;
         int gathers = 0;
         for (size_t k = 0; k < tot; k += 2) {
-            if ((k / 2) % (size_t)ctx->maxpass == 0) continue;
+            if ((k / 2) % (size_t)ctx->maxpass < 2) continue;
             float ms = 0.f;
             CK(cudaEventElapsedTime(&ms, ctx->ev[k], ctx->ev[k + 1]));
             jfa += ms;

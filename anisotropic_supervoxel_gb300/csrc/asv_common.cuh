@@ -79,6 +79,8 @@ struct AsvDev {
     float2 *fwd, *bwd;
     int32_t *labA, *labB;
     unsigned long long *jkeys;   // first-pass scatter keys, one per voxel, all ~0 between passes
+    unsigned long long *tlist;   // voxels labelled by the first pass: (segment << 32) | voxel, 27 per seed
+    int *tcount;                 // entries of tlist
     float4 *pos0;                // initial seeds (density placement)
     float *M0;                   // initial metric, 8 floats / seed
     float4 *pos, *slab;          // working seeds
@@ -109,6 +111,7 @@ void asv_launch_first_init(const AsvDev &d, cudaStream_t st);
 void asv_launch_draw(const AsvDev &d, cudaStream_t st);
 void asv_launch_jfa(const AsvDev &d, int pass, int grid_blocks, cudaStream_t st);
 void asv_launch_jfa_first_scatter(const AsvDev &d, cudaStream_t st);
+void asv_launch_jfa_second_scatter(const AsvDev &d, cudaStream_t st);
 void asv_launch_jfa_single(const AsvDev &d, const int32_t *in, int32_t *out, int step, float ratio,
                            cudaStream_t st);
 void asv_launch_centroids(const AsvDev &d, cudaStream_t st);

@@ -749,9 +749,85 @@ __global__ void __launch_bounds__(256) k_jfa_first_take(AsvDev d)
     int si, i, x, y, z, sx, sy, sz;
     if (!asv_first_target(d, t, si, i, x, y, z, sx, sy, sz)) return;
     const SegDesc &S = d.segs[si];
-    const long long v = S.vox_off + ((long long)z * S.H + y) * S.W + x;
+    const long long vl = ((long long)z * S.H + y) * S.W + x, v = S.vox_off + vl;
     const unsigned long long key = atomicExch(d.jkeys + v, ASV_KEY_EMPTY);
-    if (key != ASV_KEY_EMPTY) d.labB[v] = (int32_t)(key & 0x7fffu);
+    if (key != ASV_KEY_EMPTY) {
+        d.labB[v] = (int32_t)(key & 0x7fffu);
+        d.tlist[atomicAdd(d.tcount, 1)] = ((unsigned long long)si << 32) | (unsigned long long)vl;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// The second pass (step s = steps[1]) as a scatter too: its input, the first
+// pass's output, is labelled only at the voxels listed in tlist.  A voxel v
+// sees the label at u through offset o when clamp(v + o*s) == u along every
+// axis; per axis those v form a range (one voxel inside the volume, up to
+// s + 1 next to an edge, where several offsets clamp onto u).  Each (u, o)
+// thread visits that box; ranks and keys as in the first pass.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void asv_axis_sources(int u, int o, int s, int n, int &lo, int &hi)
+{
+    if (o == 0) { lo = hi = u; return; }
+    if (o < 0) {                              // clamp(v - s) == u
+        if (u > 0) lo = hi = u + s; else { lo = 0; hi = s; }
+    } else {                                  // clamp(v + s) == u
+        if (u < n - 1) lo = hi = u - s; else { lo = n - 1 - s; hi = n - 1; }
+    }
+    lo = max(lo, 0);
+    hi = min(hi, n - 1);                      // empty when lo > hi
+}
+
+// first rank, in the order `order`, of an offset o with clamp(v + o*s) == u
+__device__ __forceinline__ int asv_first_rank_step(int v, int u, int s, int n, const int order[3])
+{
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+        if (min(max(v + order[r] * s, 0), n - 1) == u) return r;
+    return 3;    // not reached: v is one of u's sources
+}
+
+template <bool TAKE>
+__global__ void __launch_bounds__(256) k_jfa_second(AsvDev d)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long e = t / 27;
+    if (e >= *d.tcount) return;
+    const int o = (int)(t - e * 27);
+    const unsigned long long ent = d.tlist[e];
+    const int si = (int)(ent >> 32);
+    const long long ul = (long long)(ent & 0xffffffffull);
+    const SegDesc &S = d.segs[si];
+    const int s = S.steps[1];
+    const int ux = (int)(ul % S.W), uy = (int)((ul / S.W) % S.H), uz = (int)(ul / ((long long)S.W * S.H));
+    int x0, x1, y0, y1, z0, z1;
+    asv_axis_sources(ux, o % 3 - 1, s, S.W, x0, x1);
+    asv_axis_sources(uy, (o / 3) % 3 - 1, s, S.H, y0, y1);
+    asv_axis_sources(uz, o / 9 - 1, s, S.D, z0, z1);
+    if (x0 > x1 || y0 > y1 || z0 > z1) return;
+    const int label = d.labB[S.vox_off + ul];
+    const int xy_order[3] = { -1, 0, 1 }, z_order[3] = { 0, -1, 1 };
+    for (int z = z0; z <= z1; z++)
+        for (int y = y0; y <= y1; y++)
+            for (int x = x0; x <= x1; x++) {
+                const long long v = S.vox_off + ((long long)z * S.H + y) * S.W + x;
+                if (TAKE) {
+                    const unsigned long long key = atomicExch(d.jkeys + v, ASV_KEY_EMPTY);
+                    if (key != ASV_KEY_EMPTY) d.labA[v] = (int32_t)(key & 0x7fffu);
+                    continue;
+                }
+                const int rank = asv_first_rank_step(z, uz, s, S.D, z_order) * 9 +
+                                 asv_first_rank_step(y, uy, s, S.H, xy_order) * 3 +
+                                 asv_first_rank_step(x, ux, s, S.W, xy_order);
+                const uchar4 c = __ldg(d.lab + v);
+                const float dist = asv_jfa_dist(d.jtab + 3 * S.seed_off, label,
+                                                make_float2((float)x + 0.5f, (float)y + 0.5f),
+                                                make_float2((float)z + 0.5f, (float)c.x),
+                                                make_float2((float)c.y, (float)c.z), S.ratio[1]);
+                if (!(dist < 100000000.0f)) continue;
+                const unsigned long long key = ((unsigned long long)__float_as_uint(dist) << 32) |
+                                               ((unsigned long long)rank << 16) | (unsigned long long)label;
+                atomicMin(d.jkeys + v, key);
+            }
 }
 
 // single-segment pass with explicit step and ratio (test entry point)
@@ -1192,10 +1268,20 @@ void asv_launch_jfa(const AsvDev &d, int pass, int grid_blocks, cudaStream_t st)
 void asv_launch_jfa_first_scatter(const AsvDev &d, cudaStream_t st)
 {
     cudaMemsetAsync(d.labB, 0xff, sizeof(int32_t) * (size_t)d.total_chunks * ASV_CHUNK, st);
+    cudaMemsetAsync(d.tcount, 0, sizeof(int), st);
     const long long threads = 27LL * d.total_seeds;
     const int blocks = (int)((threads + 255) / 256);
     k_jfa_first_scatter<<<blocks, 256, 0, st>>>(d);
     k_jfa_first_take<<<blocks, 256, 0, st>>>(d);
+}
+
+void asv_launch_jfa_second_scatter(const AsvDev &d, cudaStream_t st)
+{
+    cudaMemsetAsync(d.labA, 0xff, sizeof(int32_t) * (size_t)d.total_chunks * ASV_CHUNK, st);
+    const long long threads = 27LL * 27LL * d.total_seeds;   // tlist holds <= 27 entries per seed
+    const int blocks = (int)((threads + 255) / 256);
+    k_jfa_second<false><<<blocks, 256, 0, st>>>(d);
+    k_jfa_second<true><<<blocks, 256, 0, st>>>(d);
 }
 
 void asv_launch_jfa_single(const AsvDev &d, const int32_t *in, int32_t *out, int step, float ratio,

@@ -86,7 +86,7 @@ typedef struct asv_info {
 
 typedef struct asv_stats {
     double jfa_ms;      /* summed device time of the k_jfa gather passes of the last run
-                           (every pass but each iteration's first, a seed scatter) */
+                           (every pass but each iteration's first two, seed scatters) */
     int jfa_launches;
     double centroid_ms;
     double metric_ms;
