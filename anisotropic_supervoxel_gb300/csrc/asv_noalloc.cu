@@ -19,7 +19,8 @@
 // The semantics are those of asv_check_dead_seeds (GPU-AS/Image.cpp:
 // 1579-1778): count the voxels of each label, then relabel dead seeds
 // (<= 3 dead: label_replace.gs in order; > 3: sequence_label's raster remap)
-// and forward-fill label -1.
+// and forward-fill label -1.  A label outside [-1, Kp) (which the JFA never
+// writes) is read as -1 by every stage: counted in the -1 slot and filled.
 #include "asv.h"
 
 #include <cuda_runtime.h>
@@ -49,6 +50,13 @@ struct NaScratch {
     int *rec;
     int *scan;
 };
+
+// a raw label as every stage reads it: outside [-1, Kp) -> -1
+static __device__ __forceinline__ int na_label(const int32_t *__restrict__ raw, long long v, int Kp)
+{
+    const int l = raw[v];
+    return (l >= 0 && l < Kp) ? l : -1;
+}
 
 static __device__ __forceinline__ int na_relabel(const int *rec, int Kp, int l)
 {
@@ -83,8 +91,8 @@ __global__ void __launch_bounds__(256) k_na_count(NaScratch s, const int32_t *__
         long long v = (long long)blockIdx.x * NA_CHUNK + i * 256 + threadIdx.x;
         int key = -1;
         if (v < n) {
-            int l = raw[v];
-            key = (l < 0 || l >= Kp) ? Kp : l;
+            const int l = na_label(raw, v, Kp);
+            key = l < 0 ? Kp : l;
         }
         unsigned grp = __match_any_sync(NA_FULL, key);
         if (key >= 0 && (threadIdx.x & 31) == __ffs(grp) - 1) atomicAdd(s.counts + key, __popc(grp));
@@ -130,9 +138,9 @@ __global__ void __launch_bounds__(1024) k_na_stats(NaScratch s, const int32_t *_
         s.rec[R_DEAD] = dead;
         s.rec[R_MODE] = dead == 0 ? 0 : (dead <= 3 ? 1 : 2);
         s.rec[R_INVALID] = s.counts[Kp] > 0 ? 1 : 0;
-        int l0 = raw[0];
+        const int l0 = na_label(raw, 0, Kp);
         s.rec[R_L0] = l0;
-        s.rec[R_M0] = (l0 >= 0 && l0 < Kp && s.rank[l0] >= 0) ? s.rank[l0] : 0;
+        s.rec[R_M0] = (l0 >= 0 && s.rank[l0] >= 0) ? s.rank[l0] : 0;
     }
 }
 
@@ -143,7 +151,7 @@ __global__ void __launch_bounds__(256) k_na_chunk_max(NaScratch s, const int32_t
     long long m = -1;
     for (int i = 0; i < NA_CHUNK / 256; i++) {
         long long v = (long long)blockIdx.x * NA_CHUNK + i * 256 + threadIdx.x;
-        if (v < n) { long long q = na_src(s.rec, Kp, v, raw[v]); if (q > m) m = q; }
+        if (v < n) { long long q = na_src(s.rec, Kp, v, na_label(raw, v, Kp)); if (q > m) m = q; }
     }
     for (int o = 16; o; o >>= 1) { long long q = __shfl_xor_sync(NA_FULL, m, o); if (q > m) m = q; }
     __shared__ long long wm[8];
@@ -189,21 +197,34 @@ __global__ void __launch_bounds__(1024) k_na_prefix(NaScratch s, int nchunks)
     }
 }
 
+// The chunk's raw labels are staged through shared memory with coalesced
+// loads (voxel base + i * 256 + thread), then every thread scans its 8
+// consecutive voxels from there; the results go back through shared memory
+// and out with coalesced stores.
 __global__ void __launch_bounds__(256) k_na_apply(NaScratch s, const int32_t *__restrict__ raw,
                                                   int32_t *__restrict__ out, long long n, int Kp)
 {
+    __shared__ int32_t tile[NA_CHUNK + NA_CHUNK / 32];      // one pad word per 32: no bank conflicts
     const int *rec = s.rec;
     const bool scan = na_scan_needed(rec);
     const int mode = rec[R_MODE];
     const int per = NA_CHUNK / 256;
-    long long v0 = (long long)blockIdx.x * NA_CHUNK + (long long)threadIdx.x * per;
+    const long long base = (long long)blockIdx.x * NA_CHUNK;
+#define NA_PAD(i) ((i) + ((i) >> 5))
+    for (int i = 0; i < per; i++) {
+        const int k = i * 256 + threadIdx.x;
+        tile[NA_PAD(k)] = base + k < n ? na_label(raw, base + k, Kp) : -1;
+    }
+    __syncthreads();
+    const int k0 = threadIdx.x * per;
+    const long long v0 = base + k0;
     long long excl = -1;
     if (scan) {
         long long carry = (long long)s.scan[blockIdx.x] - 1;
         long long m = -1;
         for (int k = 0; k < per; k++) {
             long long v = v0 + k;
-            if (v < n) { long long q = na_src(rec, Kp, v, raw[v]); if (q > m) m = q; }
+            if (v < n) { long long q = na_src(rec, Kp, v, tile[NA_PAD(k0 + k)]); if (q > m) m = q; }
         }
         long long incl = m;
         int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -217,11 +238,13 @@ __global__ void __launch_bounds__(256) k_na_apply(NaScratch s, const int32_t *__
         if (lane == 0) ew = -1;
         excl = max(max(before, ew), carry);
     }
+    int res[NA_CHUNK / 256];
     long long src = excl;
     for (int k = 0; k < per; k++) {
         long long v = v0 + k;
-        if (v >= n) break;
-        int l = raw[v];
+        res[k] = -1;
+        if (v >= n) continue;
+        int l = tile[NA_PAD(k0 + k)];
         int r;
         if (!scan) {
             r = na_relabel(rec, Kp, l);
@@ -231,21 +254,32 @@ __global__ void __launch_bounds__(256) k_na_apply(NaScratch s, const int32_t *__
             if (mode == 2) {
                 if (src <= 0) r = rec[R_M0];
                 else {
-                    int ls = raw[src];
-                    r = (ls >= 0 && ls < Kp && s.rank[ls] >= 0) ? s.rank[ls] : 0;
+                    // the source voxel can lie in an earlier chunk: read it from global memory
+                    int ls = src >= base ? tile[NA_PAD((int)(src - base))] : na_label(raw, src, Kp);
+                    r = (ls >= 0 && s.rank[ls] >= 0) ? s.rank[ls] : 0;
                 }
             } else {
                 int rl = na_relabel(rec, Kp, l);
                 if (v == 0 || rl != -1) r = rl;
-                else if (src >= 1) r = na_relabel(rec, Kp, raw[src]);
-                else {
-                    int r0 = na_relabel(rec, Kp, raw[0]);
+                else if (src >= 1) {
+                    int ls = src >= base ? tile[NA_PAD((int)(src - base))] : na_label(raw, src, Kp);
+                    r = na_relabel(rec, Kp, ls);
+                } else {
+                    int r0 = na_relabel(rec, Kp, na_label(raw, 0, Kp));
                     r = r0 >= 0 ? r0 : 0;
                 }
             }
         }
-        out[v] = r;
+        res[k] = r;
     }
+    __syncthreads();                                        // every read of the staged labels is done
+    for (int k = 0; k < per; k++) tile[NA_PAD(k0 + k)] = res[k];
+    __syncthreads();
+    for (int i = 0; i < per; i++) {
+        const int k = i * 256 + threadIdx.x;
+        if (base + k < n) out[base + k] = tile[NA_PAD(k)];
+    }
+#undef NA_PAD
 }
 
 // Device address of the scratch array, resolved once per device (the first
@@ -272,8 +306,17 @@ extern "C" asv_status asv_check_dead_seeds_noalloc(const int32_t *d_raw, int32_t
                                                    int D, int Kp, void *stream)
 {
     if (!d_raw || !d_out || W < 1 || H < 1 || D < 1 || Kp < 1) return ASV_ERR_BAD_ARG;
+    if ((long long)W * H > NA_MAX_VOXELS || (long long)W * H * D > NA_MAX_VOXELS || Kp > NA_MAX_SEEDS)
+        return ASV_ERR_BAD_ARG;
     long long n = (long long)W * H * D;
-    if (n > NA_MAX_VOXELS || Kp > NA_MAX_SEEDS) return ASV_ERR_BAD_ARG;
+    // in and out must not overlap: blocks read labels of other chunks (the
+    // fill source) while others write theirs
+    const uintptr_t r0 = (uintptr_t)d_raw, o0 = (uintptr_t)d_out, nb = 4 * (uintptr_t)n;
+    if (r0 < o0 + nb && o0 < r0 + nb) return ASV_ERR_BAD_ARG;
+    // an error left pending by earlier work of the caller is returned as
+    // ASV_ERR_CUDA and left pending for its owner (not cleared, not mixed
+    // with this call's launches)
+    if (cudaPeekAtLastError() != cudaSuccess) return ASV_ERR_CUDA;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) { cudaGetLastError(); return ASV_ERR_NO_DEVICE; }
     void *base = nullptr;

@@ -571,24 +571,23 @@ __device__ __forceinline__ int32_t asv_jfa_eval(const asv_list_t *__restrict__ A
 }
 
 // Centroid sums of one voxel, fused into the last JFA pass of a Lloyd
-// iteration (centroids.vs:19-54): the lanes that run together are grouped by
+// iteration (centroids.vs:19-54): the lanes of the warp are grouped by
 // destination slot, reduced in the warp, and one u64 atomic per group and
-// component is issued.  Lanes of one warp can be in different tiles at this
-// point (a lane that left its tile early runs ahead into the next one, which
-// may belong to another segment), so the group key is the global sum slot
-// `slot0 + label`, never the segment-local label; grouping over whichever
-// lanes are active keeps the sums exact.
+// component is issued.  Every lane of the warp makes this call for every
+// voxel of the tile (a lane whose column lies outside the segment passes
+// valid = false and joins with key -1, which issues nothing), so the full
+// warp mask is exact here whatever path the lanes took through the
+// candidate evaluation before it.
 __device__ __forceinline__ void asv_accumulate(unsigned long long *__restrict__ sums, int slot0, uchar4 c,
-                                               int Kp, int x, int y, int z, int best)
+                                               int Kp, int x, int y, int z, int best, bool valid)
 {
-    const int key = slot0 + (best < 0 ? Kp : best);
-    const unsigned act = __activemask();
-    const unsigned grp = __match_any_sync(act, key);
+    const int key = valid ? slot0 + (best < 0 ? Kp : best) : -1;
+    const unsigned grp = __match_any_sync(0xffffffffu, key);
     const unsigned q[7] = { 2u * x + 1u, 2u * y + 1u, 2u * z + 1u, 1u, c.x, c.y, c.z };
     unsigned s[7];
 #pragma unroll
     for (int k = 0; k < 7; k++) s[k] = __reduce_add_sync(grp, q[k]);
-    if ((int)(threadIdx.x & 31) == __ffs(grp) - 1) {
+    if (valid && (int)(threadIdx.x & 31) == __ffs(grp) - 1) {
         unsigned long long *dst = sums + 8ull * key;
 #pragma unroll
         for (int k = 0; k < 7; k++) atomicAdd(dst + k, (unsigned long long)s[k]);
@@ -599,13 +598,15 @@ __device__ __forceinline__ void asv_accumulate(unsigned long long *__restrict__ 
 // `lists` is this thread's first entry of 3 slice-list rows of ASV_SLICE_MAX
 // entries and one merge row of 2 x ASV_SLICE_MAX.  A
 // chain continues while z + step < D; the next chain starts at the next
-// residue, whose minus slice is slice 0.
+// residue, whose minus slice is slice 0.  A lane whose column lies outside
+// the segment runs the same loop on the clamped column (valid = false) and
+// stores nothing, so the lanes of a warp stay in the same tile.
 template <bool SUMS>
 __device__ __forceinline__ void asv_jfa_run(const int32_t *__restrict__ in, int32_t *__restrict__ out,
                                             const uchar4 *__restrict__ lab, const float4 *__restrict__ tab,
                                             unsigned long long *__restrict__ sums, int slot0, int W, int H, int D,
                                             int Kp, int x, int y, int p0, int zrun, int step,
-                                            float ratio, asv_list_t *__restrict__ lists)
+                                            float ratio, asv_list_t *__restrict__ lists, bool valid)
 {
     const int sl = W * H;                       // segments hold < 2^31 voxels
     const int xs[3] = { max(x - step, 0), x, min(x + step, W - 1) };
@@ -629,8 +630,8 @@ __device__ __forceinline__ void asv_jfa_run(const int32_t *__restrict__ in, int3
                                        lists + 3 * row);
         const int32_t best = asv_jfa_eval(lists + sc * row, nc, lists + 3 * row, nx, tab, c, vx, vy,
                                           (float)z + 0.5f, ratio);
-        out[z * sl + col] = best;
-        if (SUMS) asv_accumulate(sums, slot0, c, Kp, x, y, z, best);
+        if (valid) out[z * sl + col] = best;
+        if (SUMS) asv_accumulate(sums, slot0, c, Kp, x, y, z, best, valid);
         if (--n == 0) break;
         if (more) {                             // next voxel of the chain: rotate the rows
             z = zp;
@@ -659,16 +660,17 @@ __global__ void __launch_bounds__(ASV_JFA_THREADS, 3) k_jfa(AsvDev d, int pass,
         const int lt = t - d.tile_prefix[si];
         const int tx = lt % S.tiles_x, rest = lt / S.tiles_x;
         const int ty = rest % S.tiles_y, p0 = (rest / S.tiles_y) * S.zrun;
-        const int x = tx * ASV_TILE_X + lx, y = ty * ASV_TILE_Y + ly;
-        if (x >= S.W || y >= S.H) continue;
+        const int gx = tx * ASV_TILE_X + lx, gy = ty * ASV_TILE_Y + ly;
+        const bool valid = gx < S.W && gy < S.H;   // block-uniform loop: every lane runs the tile
+        const int x = min(gx, S.W - 1), y = min(gy, S.H - 1);
         if (pass == S.npass - 1)                   // the iteration's labels: sum them
             asv_jfa_run<true>(in + S.vox_off, out + S.vox_off, d.lab + S.vox_off, d.jtab + 3 * S.seed_off,
                               d.sums, S.seed_off, S.W, S.H, S.D, S.Kp, x, y, p0, S.zrun,
-                              S.steps[pass], S.ratio[pass], lists + threadIdx.x);
+                              S.steps[pass], S.ratio[pass], lists + threadIdx.x, valid);
         else
             asv_jfa_run<false>(in + S.vox_off, out + S.vox_off, d.lab + S.vox_off, d.jtab + 3 * S.seed_off,
                                nullptr, 0, S.W, S.H, S.D, S.Kp, x, y, p0, S.zrun, S.steps[pass],
-                               S.ratio[pass], lists + threadIdx.x);
+                               S.ratio[pass], lists + threadIdx.x, valid);
     }
 }
 
@@ -843,10 +845,11 @@ __global__ void __launch_bounds__(ASV_JFA_THREADS) k_jfa_single(AsvDev d, const 
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int tx = t % S.tiles_x, rest = t / S.tiles_x;
         const int ty = rest % S.tiles_y, p0 = (rest / S.tiles_y) * S.zrun;
-        const int x = tx * ASV_TILE_X + lx, y = ty * ASV_TILE_Y + ly;
-        if (x >= S.W || y >= S.H) continue;
+        const int gx = tx * ASV_TILE_X + lx, gy = ty * ASV_TILE_Y + ly;
+        const bool valid = gx < S.W && gy < S.H;
         asv_jfa_run<false>(in, out, d.lab + S.vox_off, d.jtab + 3 * S.seed_off, nullptr, 0, S.W, S.H,
-                           S.D, S.Kp, x, y, p0, S.zrun, step, ratio, lists + threadIdx.x);
+                           S.D, S.Kp, min(gx, S.W - 1), min(gy, S.H - 1), p0, S.zrun, step, ratio,
+                           lists + threadIdx.x, valid);
     }
 }
 

@@ -386,14 +386,17 @@ asv_status asv_server_get_stats(asv_server *srv, asv_server_stats *st);
  * or latency-bound stages where cudaMalloc/cudaFree would synchronize the
  * device mid-pipeline.  The caller passes device buffers (d_raw: W*H*D
  * int32 raw labels in [-1, Kp); d_out: W*H*D int32) and an optional stream;
- * no context is needed.  Scratch is a fixed array of about 320 KiB inside
+ * no context is needed.  d_raw and d_out must not overlap (an in-place call
+ * returns ASV_ERR_BAD_ARG).  A label outside [-1, Kp) is read as -1.
+ * Scratch is a fixed array of about 320 KiB inside
  * the library's device image, held by every device the library is loaded on
  * until the process exits.  Limits: W*H*D <= 2^25 voxels, Kp <= 32767
  * (ASV_ERR_BAD_ARG beyond).  The first call on a device resolves the
  * scratch address (make it before any stream capture).  All calls on a
  * device share the scratch and leave it holding their data; calls whose
  * work overlaps on the GPU race, so serialize them.  Run with the buffers'
- * device current. */
+ * device current.  A CUDA error already pending on the calling thread is
+ * returned as ASV_ERR_CUDA before any work and left pending. */
 #define ASV_NOALLOC_MAX_VOXELS (1LL << 25)
 #define ASV_NOALLOC_MAX_SEEDS 32767
 asv_status asv_check_dead_seeds_noalloc(const int32_t *d_raw, int32_t *d_out, int W, int H, int D,

@@ -21,7 +21,10 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 LIB = os.path.join(OUT, "libref_shaders.so")
-REF = os.environ.get("ASV_REFERENCE_ROOT", "/root/reference")
+# the reference checkout: ASV_REFERENCE_ROOT, else a directory `reference`
+# beside the repository's root directory; absent -> the builds return None
+REF = os.environ.get("ASV_REFERENCE_ROOT") or os.path.join(os.path.dirname(os.path.dirname(HERE)),
+                                                            "reference")
 SHADERS = os.path.join(REF, "GPU-AS", "shaders")
 
 PROGRAMS = {
@@ -350,6 +353,9 @@ HOST_FUNCS = [
     ("streamGPU-AS/Image.cpp", "void Image::initialization_grid(", "StreamGridShim",
      "int texel_num, seeds_num, width, height, depth, s, max_s, ac_seeds_num, dNum, wNum, hNum;\n"
      "    vector<float> seeds_lsc, seeds_lsc_adjust; ostringstream cout;", "glGenVertexArrays"),
+    # Image::print_sv_txt (GPU-AS/Image.cpp:1780-1806): the txt label file
+    ("GPU-AS/Image.cpp", "void Image::print_sv_txt(", "TxtShim",
+     "int depth, height, width, slice_num; ostringstream cout;", None),
     ("streamGPU-AS/Image.cpp", "void Image::initialization_adjust(", "StreamInitShim",
      "int texel_num, slice_num, width, height, depth, ac_seeds_num, dNum, hNum, wNum;\n"
      "    vector<float> seeds_lsc, seeds_lsc_adjust; float *grid_out; const float *res_in;\n"
@@ -358,6 +364,8 @@ HOST_FUNCS = [
 
 HOST_PRELUDE = """#include <cmath>
 #include <cstring>
+#include <fstream>
+#include <iomanip>
 #include <iostream>
 #include <map>
 #include <sstream>
@@ -498,6 +506,14 @@ extern "C" int ref_flood_ladder(int s_, float *steps, float *ratios, int cap, fl
         }
     *ratio_out = f.ratio;
     return n;
+}
+
+// Image::print_sv_txt with output_label = true: writes <path_stem>.txt
+extern "C" void ref_print_sv_txt(int *labels, int W, int H, int D, const char *path_stem)
+{
+    TxtShim s;
+    s.width = W; s.height = H; s.depth = D; s.slice_num = W * H;
+    s.print_sv_txt(labels, string(path_stem), true, false);
 }
 
 extern "C" void ref_sequence_label(int *labels, long n, const long long *counts, int Kp, int dead_seed)

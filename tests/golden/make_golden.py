@@ -165,7 +165,26 @@ def main():
         steps[i, :st.size], ratios[i, :st.size] = st, ra
     np.savez_compressed(os.path.join(HERE, "flood_ladder.npz"), s=np.int32(pin.LADDER_S), count=count,
                         ratio=ratio, steps=steps, ratios=ratios)
+    labels_txt(host)
     print("fixtures written to", HERE)
+
+
+def labels_txt(host):
+    """Image::print_sv_txt: label volumes and the bytes of the txt file the
+    reference writes for them (labels_txt.npz)."""
+    import tempfile
+    host.ref_print_sv_txt.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                      ctypes.c_char_p]
+    rng = np.random.default_rng(20240611)
+    arrays = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        for i, (D, H, W, hi) in enumerate([(3, 5, 7, 20), (2, 4, 6, 99999), (1, 1, 1, 5), (2, 1, 13, 1500)]):
+            lab = rng.integers(-1, hi, (D, H, W)).astype(np.int32)
+            stem = os.path.join(tmp, f"k{i}")
+            host.ref_print_sv_txt(lab.ctypes.data_as(ctypes.c_void_p), W, H, D, stem.encode())
+            arrays[f"labels_{i}"] = lab
+            arrays[f"txt_{i}"] = np.frombuffer(open(stem + ".txt", "rb").read(), np.uint8)
+    np.savez_compressed(os.path.join(HERE, "labels_txt.npz"), **arrays)
 
 
 # clips of the density-placement fixture (W, H, D, K, middlebury); the clip is

@@ -166,3 +166,15 @@ def test_oracle_flood_ladder(orc):
         assert len(steps) == n, s
         assert np.array_equal(np.float32(steps), f["steps"][i, :n]), s
         assert np.array_equal(np.float32(rmul) * r, f["ratios"][i, :n]), s
+
+
+def test_labels_txt(asv, tmp_path):
+    """asv_write_labels_txt against the bytes Image::print_sv_txt wrote"""
+    f = load("labels_txt.npz")
+    n = 0
+    while f"labels_{n}" in f:
+        p = str(tmp_path / f"k{n}.txt")
+        asv.write_labels_txt(p, f[f"labels_{n}"])
+        assert open(p, "rb").read() == f[f"txt_{n}"].tobytes()
+        n += 1
+    assert n == 4

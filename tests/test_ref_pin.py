@@ -423,3 +423,21 @@ def test_flood_ladder_matches_reference(ref_host, orc):
         got_steps, rmul = orc.ladder(s)
         assert np.array_equal(np.float32(got_steps), steps), (s, got_steps, steps)
         assert np.array_equal(np.float32(rmul) * np.float32(want_r), ratios), s
+
+
+def test_labels_txt_matches_reference(ref_host, asv, tmp_path):
+    """asv_write_labels_txt against Image::print_sv_txt compiled from the
+    reference tree (GPU-AS/Image.cpp:1780-1806): byte-identical files for
+    random volumes with -1, 1- to 5-digit labels and degenerate shapes."""
+    ref_host.ref_print_sv_txt.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_char_p]
+    rng = np.random.default_rng(31)
+    for k, (D, H, W, hi) in enumerate([(3, 5, 7, 20), (2, 4, 6, 99999), (1, 1, 1, 5), (4, 9, 3, 12000),
+                                       (2, 1, 13, 1500)]):
+        lab = rng.integers(-1, hi, (D, H, W)).astype(np.int32)
+        lab.ravel()[0] = -1
+        stem = str(tmp_path / f"ref{k}")
+        ref_host.ref_print_sv_txt(P(lab), W, H, D, stem.encode())
+        ours = str(tmp_path / f"ours{k}.txt")
+        asv.write_labels_txt(ours, lab)
+        assert open(ours, "rb").read() == open(stem + ".txt", "rb").read()
