@@ -522,10 +522,9 @@ __device__ __forceinline__ int asv_merge_lists(const asv_list_t *__restrict__ A,
 // product feeding a two-wide sum is fused into a two-wide FMA by the
 // assembler even when both are written with explicit .rn rounding, which
 // changes the result.
-__device__ __forceinline__ float asv_jfa_dist(const float4 *__restrict__ tab, int l, float2 vxy, float2 vzl,
-                                              float2 vab, float ratio)
+__device__ __forceinline__ float asv_jfa_dist_v(const float4 t0, const float4 t1, const float4 t2, float2 vxy,
+                                                float2 vzl, float2 vab, float ratio)
 {
-    const float4 t0 = __ldg(tab + 3 * l), t1 = __ldg(tab + 3 * l + 1), t2 = __ldg(tab + 3 * l + 2);
     const float2 dxy = __fadd2_rn(vxy, make_float2(t0.x, t0.y));              // (dx, dy)
     const float2 dzl = __fadd2_rn(vzl, make_float2(t0.z, t0.w));              // (dz, eL)
     const float2 eab = __fadd2_rn(vab, make_float2(t2.z, t2.w));              // (ea, eb)
@@ -539,6 +538,14 @@ __device__ __forceinline__ float asv_jfa_dist(const float4 *__restrict__ tab, in
     col = col + eab.y * eab.y;
     pos = (pos < 0.0f) ? 0.0f : pos;                                           // flood.gs:90-93
     return ratio * pos + col;                                                  // flood.gs:94
+}
+
+// the same with seed l's row of the table in global memory
+__device__ __forceinline__ float asv_jfa_dist(const float4 *__restrict__ tab, int l, float2 vxy, float2 vzl,
+                                              float2 vab, float ratio)
+{
+    return asv_jfa_dist_v(__ldg(tab + 3 * l), __ldg(tab + 3 * l + 1), __ldg(tab + 3 * l + 2), vxy, vzl, vab,
+                          ratio);
 }
 
 // distance loop over the concatenated lists A (na) and X (nx): the first
@@ -571,7 +578,8 @@ __device__ __forceinline__ int32_t asv_jfa_eval(const asv_list_t *__restrict__ A
 }
 
 // Centroid sums of one voxel, fused into the last JFA pass of a Lloyd
-// iteration (centroids.vs:19-54): the lanes of the warp are grouped by
+// iteration (centroids.vs:19-54; a label outside [0, Kp) counts in the -1
+// slot, so no slot beyond the segment's is written): the lanes of the warp are grouped by
 // destination slot, reduced in the warp, and one u64 atomic per group and
 // component is issued.  Every lane of the warp makes this call for every
 // voxel of the tile (a lane whose column lies outside the segment passes
@@ -581,7 +589,7 @@ __device__ __forceinline__ int32_t asv_jfa_eval(const asv_list_t *__restrict__ A
 __device__ __forceinline__ void asv_accumulate(unsigned long long *__restrict__ sums, int slot0, uchar4 c,
                                                int Kp, int x, int y, int z, int best, bool valid)
 {
-    const int key = valid ? slot0 + (best < 0 ? Kp : best) : -1;
+    const int key = valid ? slot0 + ((unsigned)best < (unsigned)Kp ? best : Kp) : -1;
     const unsigned grp = __match_any_sync(0xffffffffu, key);
     const unsigned q[7] = { 2u * x + 1u, 2u * y + 1u, 2u * z + 1u, 1u, c.x, c.y, c.z };
     unsigned s[7];
@@ -646,13 +654,317 @@ __device__ __forceinline__ void asv_jfa_run(const int32_t *__restrict__ in, int3
     }
 }
 
+// ---------------------------------------------------------------------------
+// Bit-set form of a JFA pass (steps 1..ASV_BITS_MAXS).
+//
+// The label a voxel takes depends only on the set of distinct valid labels
+// among its 27 candidates, except when two of them tie at the least
+// distance (then the first in the shader's candidate order wins): the
+// distance is a function of the voxel and the label's seed alone.  A
+// sub-tile (16 x 16 columns x up to 8 chain positions of the tile) holds few
+// distinct labels in its whole footprint (the sub-tile grown by `step` on
+// every side; on the benchmarked clips mostly under 32).  So the block
+// copies the footprint and the sub-tile's LAB values into shared memory
+// with asynchronous copies (one memory latency per sub-tile), numbers the
+// footprint's distinct labels 0..T-1 (T <= 32, else the sub-tile takes the
+// list form), and gives every footprint row, per tile column x, the 32-bit
+// mask of the labels at x - step, x, x + step (one bit per label).  A
+// voxel's candidate mask is the OR of three such row masks in each of its
+// three slices; the voxel evaluates the labels of its mask in any order and
+// keeps the least distance below 1e8.  An exact tie at the least distance
+// between two labels (about 30 per million voxel-passes on the benchmarked
+// clips) sends the voxel through the shader's ordered scan of its 27
+// candidates instead, so every label equals the shader's.
+//
+// Footprint slices ("slots") of a sub-tile of n chain positions: slot 0 the
+// minus slice of position 0, slots 1..n the centre slices, slot n+1 the plus
+// slice of position n-1, and where a chain ends inside the sub-tile slot
+// n+2 (slice 0, the minus slice of every chain start after the first) and
+// slot n+3 (slice D-1, the clamped plus slice of every chain end).  Along a
+// chain the minus slice of a position is the centre of the one before it
+// and its plus slice the centre of the one after it.
+// ---------------------------------------------------------------------------
+#define ASV_JFA_LIST_BYTES (5 * ASV_SLICE_MAX * ASV_JFA_THREADS * (int)sizeof(asv_list_t))
+#define ASV_BITS_MAXS 6          // largest step taken in bit-set form
+#define ASV_BITS_MAXT 32         // labels per sub-tile footprint (one 32-bit mask)
+#define ASV_BITS_MAXKP 8192      // segment seed counts up to this use the bit-set form
+#define ASV_BITS_TLCAP 256       // claimed labels remembered for the reset
+#define ASV_BITS_NONE 255        // table number of no label
+#define ASV_BITS_AREA 48320      // shared bytes of the largest sub-tile (step 3)
+#define ASV_JFA_AREA (ASV_BITS_AREA > ASV_JFA_LIST_BYTES ? ASV_BITS_AREA : ASV_JFA_LIST_BYTES)
+
+struct AsvBitsShared {
+    float4 tdat[3 * ASV_BITS_MAXT];             // the table's seed rows (as jtab)
+    unsigned claim[ASV_BITS_MAXKP / 32];        // labels numbered in this sub-tile (all zero between)
+    int tlab[ASV_BITS_TLCAP];                   // label of each number
+    int slotz[16];                              // slice of each footprint slot
+    int tcount;
+    unsigned char map8[ASV_BITS_MAXKP];         // number of each claimed label
+};
+#define ASV_JFA_SMEM (ASV_JFA_AREA + (int)sizeof(AsvBitsShared))
+
+template <int S> struct AsvBitsGeo {
+    static constexpr int FW = ASV_TILE_X + 2 * S;                     // footprint width and height
+    static constexpr int FP = FW * FW;                                // footprint entries per slot
+    static constexpr int SUB = S <= 3 ? 8 : 4;                        // chain positions per sub-tile
+    static constexpr int NSLOT = SUB + 4;
+    static constexpr int NCOL = (FP + ASV_JFA_THREADS - 1) / ASV_JFA_THREADS;
+    static constexpr int HXN = FW * ASV_TILE_X;                       // row masks per slot
+    static constexpr int NHX = (HXN + ASV_JFA_THREADS - 1) / ASV_JFA_THREADS;
+    static constexpr int FLAB_BYTES = NSLOT * FP * 4;
+    static constexpr int HX_BYTES = NSLOT * HXN * 4;
+    static_assert(FLAB_BYTES + HX_BYTES + SUB * ASV_JFA_THREADS * 4 <= ASV_BITS_AREA,
+                  "bit-set sub-tile exceeds the shared area");
+};
+
+// 4-byte asynchronous copy global -> shared (cp.async, completed by
+// asv_cp_async_wait)
+__device__ __forceinline__ void asv_cp_async4(void *dst, const void *src)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void asv_cp_async_wait()
+{
+    asm volatile("cp.async.commit_group;\ncp.async.wait_all;\n" ::: "memory");
+}
+
+// table number of a footprint label (labels outside [0, Kp) are none)
+__device__ __forceinline__ int asv_bits_num(const AsvBitsShared &b, int l, int Kp)
+{
+    return (unsigned)l < (unsigned)Kp ? b.map8[l] : ASV_BITS_NONE;
+}
+
+// The shader's ordered scan of the 27 candidates (slices centre, minus,
+// plus; rows y-S, y, y+S; columns x-S, x, x+S) over the footprint labels,
+// strict '<' from 1e8 (flood.gs:63, :95-99): the tie-break path.
+template <int S>
+__device__ __noinline__ int asv_bits_ordered(const int *__restrict__ fc, const int *__restrict__ fm,
+                                             const int *__restrict__ fp, const AsvBitsShared &b, int Kp,
+                                             float2 vxy, float2 vzl, float2 vab, float ratio)
+{
+    constexpr int FW = AsvBitsGeo<S>::FW;
+    float mind = 100000000.0f;
+    int best = -1;
+    for (int k = 0; k < 3; k++) {
+        const int *f = k == 0 ? fc : (k == 1 ? fm : fp);
+        for (int a = 0; a < 3; a++)
+            for (int c = 0; c < 3; c++) {
+                const int e = asv_bits_num(b, f[a * S * FW + c * S], Kp);
+                if (e >= ASV_BITS_MAXT) continue;
+                const float dist = asv_jfa_dist_v(b.tdat[3 * e], b.tdat[3 * e + 1], b.tdat[3 * e + 2], vxy, vzl,
+                                                  vab, ratio);
+                if (dist < mind) { mind = dist; best = b.tlab[e]; }
+            }
+    }
+    return best;
+}
+
+// One sub-tile of n <= SUB chain positions from p0 in bit-set form; false
+// (nothing written) when its footprint holds more than 32 labels.  Called
+// by the whole block.
+template <int S, bool SUMS>
+__device__ bool asv_jfa_bits_sub(const int32_t *__restrict__ in, int32_t *__restrict__ out,
+                                 const uchar4 *__restrict__ lab, const float4 *__restrict__ tab,
+                                 unsigned long long *__restrict__ sums, int slot0, int W, int H, int D, int Kp,
+                                 int tx0, int ty0, int p0, int n, float ratio, unsigned char *smem)
+{
+    using G = AsvBitsGeo<S>;
+    constexpr int FW = G::FW, FP = G::FP;
+    int *flab = (int *)smem;
+    unsigned *hx = (unsigned *)(smem + G::FLAB_BYTES);
+    uchar4 *labsh = (uchar4 *)(smem + G::FLAB_BYTES + G::HX_BYTES);
+    AsvBitsShared &b = *(AsvBitsShared *)(smem + ASV_JFA_AREA);
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int sl = W * H;
+    const int lx = tid % ASV_TILE_X, ly = tid / ASV_TILE_X;
+    const int gx = tx0 + lx, gy = ty0 + ly;
+    const bool valid = gx < W && gy < H;                       // other lanes run along, store nothing
+    const int x = min(gx, W - 1), y = min(gy, H - 1);
+    const int col = y * W + x;
+
+    // slices of the footprint slots
+    bool brk = false;
+    if (tid < n) {
+        int r, j, len;
+        asv_chain_pos(p0 + tid, D, S, r, j, len);
+        const int z = r + j * S;
+        b.slotz[1 + tid] = z;
+        if (tid == 0) b.slotz[0] = max(z - S, 0);
+        if (tid == n - 1) b.slotz[n + 1] = z + S < D ? z + S : D - 1;
+        brk = tid < n - 1 && z + S >= D;
+    }
+    if (tid == 0) { b.slotz[n + 2] = 0; b.slotz[n + 3] = D - 1; }
+    const bool any_brk = __syncthreads_or(brk);
+    const int nf = any_brk ? n + 4 : n + 2;
+
+    // footprint labels (clamp-to-edge) and the voxels' LAB, copied
+    // asynchronously; each thread copies the same footprint columns of every slot
+    int coff[G::NCOL];
+#pragma unroll
+    for (int i = 0; i < G::NCOL; i++) {
+        const int e = tid + i * ASV_JFA_THREADS, fy = e / FW, fx = e - fy * FW;
+        coff[i] = min(max(ty0 - S + fy, 0), H - 1) * W + min(max(tx0 - S + fx, 0), W - 1);
+    }
+    for (int k = 0; k < nf; k++) {
+        const int32_t *src = in + b.slotz[k] * sl;
+#pragma unroll
+        for (int i = 0; i < G::NCOL; i++) {
+            const int e = tid + i * ASV_JFA_THREADS;
+            if (e < FP) asv_cp_async4(flab + k * FP + e, src + coff[i]);
+        }
+    }
+    for (int j = 0; j < n; j++) asv_cp_async4(labsh + j * ASV_JFA_THREADS + tid, lab + b.slotz[j + 1] * sl + col);
+    asv_cp_async_wait();
+    __syncthreads();
+
+    // number the distinct labels (each thread its own entries)
+    for (int k = 0; k < nf; k++) {
+#pragma unroll
+        for (int i = 0; i < G::NCOL; i++) {
+            const int e = tid + i * ASV_JFA_THREADS;
+            int v = e < FP ? flab[k * FP + e] : -1;
+            if ((unsigned)v >= (unsigned)Kp) v = -1;
+            const int vp = __shfl_up_sync(0xffffffffu, v, 1);
+            if (v >= 0 && !(lane > 0 && vp == v)) {
+                const unsigned w = (unsigned)v >> 5, bit = 1u << (v & 31);
+                if (!(*(volatile unsigned *)&b.claim[w] & bit) && !(atomicOr(&b.claim[w], bit) & bit)) {
+                    const int idx = atomicAdd(&b.tcount, 1);
+                    if (idx < ASV_BITS_TLCAP) b.tlab[idx] = v;
+                    b.map8[v] = (unsigned char)(idx < ASV_BITS_MAXT ? idx : ASV_BITS_NONE);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    const int T = b.tcount;
+    // the claim bits go back to zero for the next sub-tile
+    if (T <= ASV_BITS_TLCAP) {
+        for (int i = tid; i < T; i += ASV_JFA_THREADS) b.claim[b.tlab[i] >> 5] = 0u;
+    } else {
+        for (int i = tid; i < ASV_BITS_MAXKP / 32; i += ASV_JFA_THREADS) b.claim[i] = 0u;
+    }
+    if (T > ASV_BITS_MAXT) {
+        __syncthreads();
+        if (tid == 0) b.tcount = 0;
+        __syncthreads();
+        return false;
+    }
+    for (int i = tid; i < 3 * T; i += ASV_JFA_THREADS) b.tdat[i] = __ldg(tab + 3 * b.tlab[i / 3] + i % 3);
+    // row masks: labels at columns x - S, x, x + S of every footprint row
+    for (int k = 0; k < nf; k++) {
+#pragma unroll
+        for (int i = 0; i < G::NHX; i++) {
+            const int q = tid + i * ASV_JFA_THREADS;
+            if (q < G::HXN) {
+                const int *r = flab + k * FP + (q >> 4) * FW + (q & 15);
+                unsigned m = 0;
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    const int l = r[c * S];
+                    m |= (unsigned)l < (unsigned)Kp ? 1u << b.map8[l] : 0u;
+                }
+                hx[k * G::HXN + q] = m;
+            }
+        }
+    }
+    __syncthreads();
+
+    // the chain walk of this thread's column
+    const unsigned *h0 = hx + ly * ASV_TILE_X + lx;              // row y - S of slot 0
+    const int *f0 = flab + ly * FW + lx;                         // candidate (x - S, y - S) of slot 0
+    auto smask = [&](int k) -> unsigned {
+        const unsigned *h = h0 + k * G::HXN;
+        return h[0] | h[S * ASV_TILE_X] | h[2 * S * ASV_TILE_X];
+    };
+    const float2 vxy = make_float2((float)x + 0.5f, (float)y + 0.5f);
+    const unsigned m_zero = any_brk ? smask(n + 2) : 0u, m_last = any_brk ? smask(n + 3) : 0u;
+    unsigned mm = smask(0), mc = smask(1);
+    int im = 0;
+    for (int j = 0; j < n; j++) {
+        const int z = b.slotz[j + 1];
+        const bool chain = z + S < D;                         // the plus slice is the next centre
+        const int ip = j == n - 1 ? n + 1 : (chain ? j + 2 : n + 3);
+        const unsigned mp = (j < n - 1 && !chain) ? m_last : smask(ip);
+        const uchar4 c = labsh[j * ASV_JFA_THREADS + tid];
+        const float2 vzl = make_float2((float)z + 0.5f, (float)c.x), vab = make_float2((float)c.y, (float)c.z);
+        unsigned m = mm | mc | mp;
+        float best = 100000000.0f;
+        int bt = -1;
+        bool tie = false;
+        while (m) {
+            const int ta = __ffs(m) - 1;
+            m &= m - 1;
+            const float da = asv_jfa_dist_v(b.tdat[3 * ta], b.tdat[3 * ta + 1], b.tdat[3 * ta + 2], vxy, vzl, vab,
+                                            ratio);
+            if (da < best) { best = da; bt = ta; tie = false; } else if (da == best) tie = true;
+        }
+        int label = bt >= 0 ? b.tlab[bt] : -1;
+        if (tie)
+            label = asv_bits_ordered<S>(f0 + (j + 1) * FP, f0 + im * FP, f0 + ip * FP, b, Kp, vxy, vzl, vab, ratio);
+        if (valid) out[z * sl + col] = label;
+        if (SUMS) asv_accumulate(sums, slot0, c, Kp, x, y, z, label, valid);
+        if (j + 1 < n) {
+            if (chain) { mm = mc; mc = mp; im = j + 1; }
+            else { mm = m_zero; mc = smask(j + 2); im = n + 2; }
+        }
+    }
+    __syncthreads();                                          // the footprint and table are reused
+    if (tid == 0) b.tcount = 0;
+    return true;
+}
+
+// one tile of a pass: bit-set form by sub-tiles where it applies, else (or
+// for a sub-tile whose footprint holds too many labels) the list form
+template <bool SUMS>
+__device__ __forceinline__ void asv_jfa_tile(const int32_t *__restrict__ in, int32_t *__restrict__ out,
+                                             const uchar4 *__restrict__ lab, const float4 *__restrict__ tab,
+                                             unsigned long long *__restrict__ sums, int slot0, int W, int H, int D,
+                                             int Kp, int tx0, int ty0, int p0, int zrun, int step, float ratio,
+                                             unsigned char *smem)
+{
+    const int n = min(zrun, D - p0);
+    const int lx = threadIdx.x % ASV_TILE_X, ly = threadIdx.x / ASV_TILE_X;
+    const int gx = tx0 + lx, gy = ty0 + ly;
+    const bool valid = gx < W && gy < H;                       // block-uniform loop: every lane runs the tile
+    auto list_run = [&](int q0, int nq) {
+        asv_jfa_run<SUMS>(in, out, lab, tab, sums, slot0, W, H, D, Kp, min(gx, W - 1), min(gy, H - 1), q0, nq,
+                          step, ratio, (asv_list_t *)smem + threadIdx.x, valid);
+        __syncthreads();                                       // the list rows alias the footprint
+    };
+    if (step <= ASV_BITS_MAXS && Kp <= ASV_BITS_MAXKP) {
+#define ASV_BITS_CASE(S_)                                                                                    \
+    case S_:                                                                                                 \
+        for (int q0 = 0; q0 < n; q0 += AsvBitsGeo<S_>::SUB) {                                                \
+            const int nq = min(AsvBitsGeo<S_>::SUB, n - q0);                                                 \
+            if (!asv_jfa_bits_sub<S_, SUMS>(in, out, lab, tab, sums, slot0, W, H, D, Kp, tx0, ty0, p0 + q0,  \
+                                            nq, ratio, smem))                                                \
+                list_run(p0 + q0, nq);                                                                       \
+        }                                                                                                    \
+        return;
+        switch (step) {
+            ASV_BITS_CASE(1) ASV_BITS_CASE(2) ASV_BITS_CASE(3) ASV_BITS_CASE(4) ASV_BITS_CASE(5) ASV_BITS_CASE(6)
+        }
+#undef ASV_BITS_CASE
+    }
+    list_run(p0, n);
+}
+
+__device__ __forceinline__ void asv_jfa_smem_init(unsigned char *smem)
+{
+    AsvBitsShared &b = *(AsvBitsShared *)(smem + ASV_JFA_AREA);
+    for (int i = threadIdx.x; i < ASV_BITS_MAXKP / 32; i += blockDim.x) b.claim[i] = 0u;
+    if (threadIdx.x == 0) b.tcount = 0;
+    __syncthreads();
+}
+
 // tile = ASV_TILE_X x ASV_TILE_Y columns x S.zrun chain positions
 __global__ void __launch_bounds__(ASV_JFA_THREADS, 3) k_jfa(AsvDev d, int pass,
                                                          const int32_t *__restrict__ in,
                                                          int32_t *__restrict__ out)
 {
-    __shared__ asv_list_t lists[5 * ASV_SLICE_MAX * ASV_JFA_THREADS];
-    const int lx = threadIdx.x % ASV_TILE_X, ly = threadIdx.x / ASV_TILE_X;
+    extern __shared__ __align__(16) unsigned char asv_jfa_smem[];
+    asv_jfa_smem_init(asv_jfa_smem);
     for (int t = blockIdx.x; t < d.total_tiles; t += gridDim.x) {
         const int si = asv_find_seg(d.tile_prefix, d.nseg, t);
         const SegDesc &S = d.segs[si];
@@ -660,17 +972,14 @@ __global__ void __launch_bounds__(ASV_JFA_THREADS, 3) k_jfa(AsvDev d, int pass,
         const int lt = t - d.tile_prefix[si];
         const int tx = lt % S.tiles_x, rest = lt / S.tiles_x;
         const int ty = rest % S.tiles_y, p0 = (rest / S.tiles_y) * S.zrun;
-        const int gx = tx * ASV_TILE_X + lx, gy = ty * ASV_TILE_Y + ly;
-        const bool valid = gx < S.W && gy < S.H;   // block-uniform loop: every lane runs the tile
-        const int x = min(gx, S.W - 1), y = min(gy, S.H - 1);
         if (pass == S.npass - 1)                   // the iteration's labels: sum them
-            asv_jfa_run<true>(in + S.vox_off, out + S.vox_off, d.lab + S.vox_off, d.jtab + 3 * S.seed_off,
-                              d.sums, S.seed_off, S.W, S.H, S.D, S.Kp, x, y, p0, S.zrun,
-                              S.steps[pass], S.ratio[pass], lists + threadIdx.x, valid);
+            asv_jfa_tile<true>(in + S.vox_off, out + S.vox_off, d.lab + S.vox_off, d.jtab + 3 * S.seed_off,
+                               d.sums, S.seed_off, S.W, S.H, S.D, S.Kp, tx * ASV_TILE_X, ty * ASV_TILE_Y, p0,
+                               S.zrun, S.steps[pass], S.ratio[pass], asv_jfa_smem);
         else
-            asv_jfa_run<false>(in + S.vox_off, out + S.vox_off, d.lab + S.vox_off, d.jtab + 3 * S.seed_off,
-                               nullptr, 0, S.W, S.H, S.D, S.Kp, x, y, p0, S.zrun, S.steps[pass],
-                               S.ratio[pass], lists + threadIdx.x, valid);
+            asv_jfa_tile<false>(in + S.vox_off, out + S.vox_off, d.lab + S.vox_off, d.jtab + 3 * S.seed_off,
+                                nullptr, 0, S.W, S.H, S.D, S.Kp, tx * ASV_TILE_X, ty * ASV_TILE_Y, p0,
+                                S.zrun, S.steps[pass], S.ratio[pass], asv_jfa_smem);
     }
 }
 
@@ -837,19 +1146,16 @@ __global__ void __launch_bounds__(ASV_JFA_THREADS) k_jfa_single(AsvDev d, const 
                                                                 int32_t *__restrict__ out, int step,
                                                                 float ratio)
 {
-    __shared__ asv_list_t lists[5 * ASV_SLICE_MAX * ASV_JFA_THREADS];
+    extern __shared__ __align__(16) unsigned char asv_jfa_smem[];
+    asv_jfa_smem_init(asv_jfa_smem);
     const SegDesc &S = d.segs[0];
-    const int lx = threadIdx.x % ASV_TILE_X, ly = threadIdx.x / ASV_TILE_X;
     const int tiles_z = (S.D + S.zrun - 1) / S.zrun;
     const int ntiles = S.tiles_x * S.tiles_y * tiles_z;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int tx = t % S.tiles_x, rest = t / S.tiles_x;
         const int ty = rest % S.tiles_y, p0 = (rest / S.tiles_y) * S.zrun;
-        const int gx = tx * ASV_TILE_X + lx, gy = ty * ASV_TILE_Y + ly;
-        const bool valid = gx < S.W && gy < S.H;
-        asv_jfa_run<false>(in, out, d.lab + S.vox_off, d.jtab + 3 * S.seed_off, nullptr, 0, S.W, S.H,
-                           S.D, S.Kp, min(gx, S.W - 1), min(gy, S.H - 1), p0, S.zrun, step, ratio,
-                           lists + threadIdx.x, valid);
+        asv_jfa_tile<false>(in, out, d.lab + S.vox_off, d.jtab + 3 * S.seed_off, nullptr, 0, S.W, S.H, S.D,
+                            S.Kp, tx * ASV_TILE_X, ty * ASV_TILE_Y, p0, S.zrun, step, ratio, asv_jfa_smem);
     }
 }
 
@@ -1240,6 +1546,21 @@ void asv_launch_density_adjust(const AsvDev &d, cudaStream_t st)
 void asv_launch_first_init(const AsvDev &d, cudaStream_t st) { k_first_init<<<seed_blocks(d), 128, 0, st>>>(d); }
 void asv_launch_draw(const AsvDev &d, cudaStream_t st) { k_draw<<<seed_blocks(d), 128, 0, st>>>(d); }
 
+// k_jfa's dynamic shared memory (list rows or bit-set footprint, and the
+// bit-set table) exceeds the 48 KiB default: raised once per device
+static void asv_jfa_attributes()
+{
+    static std::mutex mu;
+    static bool done[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mu);
+    if (dev >= 0 && dev < 64 && done[dev]) return;
+    cudaFuncSetAttribute(k_jfa, cudaFuncAttributeMaxDynamicSharedMemorySize, ASV_JFA_SMEM);
+    cudaFuncSetAttribute(k_jfa_single, cudaFuncAttributeMaxDynamicSharedMemorySize, ASV_JFA_SMEM);
+    if (dev >= 0 && dev < 64) done[dev] = true;
+}
+
 // resident k_jfa blocks on the device (persistent grid size); computed once
 // per process (thread-safe static initialisation)
 int asv_jfa_resident_blocks()
@@ -1248,7 +1569,8 @@ int asv_jfa_resident_blocks()
         int dev = 0, sms = 0, per = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_jfa, ASV_JFA_THREADS, 0);
+        asv_jfa_attributes();
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_jfa, ASV_JFA_THREADS, ASV_JFA_SMEM);
         const int b = sms * (per > 0 ? per : 1);
         return b > 0 ? b : 1024;
     }();
@@ -1265,7 +1587,8 @@ void asv_launch_jfa(const AsvDev &d, int pass, int grid_blocks, cudaStream_t st)
 {
     const int32_t *in = (pass & 1) ? d.labB : d.labA;
     int32_t *out = (pass & 1) ? d.labA : d.labB;
-    k_jfa<<<grid_blocks, 256, 0, st>>>(d, pass, in, out);
+    asv_jfa_attributes();
+    k_jfa<<<grid_blocks, 256, ASV_JFA_SMEM, st>>>(d, pass, in, out);
 }
 
 void asv_launch_jfa_first_scatter(const AsvDev &d, cudaStream_t st)
@@ -1290,7 +1613,8 @@ void asv_launch_jfa_second_scatter(const AsvDev &d, cudaStream_t st)
 void asv_launch_jfa_single(const AsvDev &d, const int32_t *in, int32_t *out, int step, float ratio,
                            cudaStream_t st)
 {
-    k_jfa_single<<<asv_jfa_grid_blocks(d.total_tiles), 256, 0, st>>>(d, in, out, step, ratio);
+    asv_jfa_attributes();
+    k_jfa_single<<<asv_jfa_grid_blocks(d.total_tiles), 256, ASV_JFA_SMEM, st>>>(d, in, out, step, ratio);
 }
 
 void asv_launch_centroids(const AsvDev &d, cudaStream_t st) { k_centroids<<<d.total_chunks, 256, 0, st>>>(d); }

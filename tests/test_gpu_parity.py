@@ -97,6 +97,53 @@ def test_jfa_single_pass(asv, orc, step):
     assert mismatch(got, want) == 0
 
 
+def _blocky_labels(rng, shape, kp, block, minus=0.02):
+    """labels constant on block^3 cubes (few labels per JFA tile footprint), some -1"""
+    D, H, W = shape
+    nb = [(n + block - 1) // block for n in shape]
+    ids = rng.integers(0, kp, nb).astype(np.int32)
+    lab = ids[np.arange(D)[:, None, None] // block, np.arange(H)[None, :, None] // block,
+              np.arange(W)[None, None, :] // block]
+    lab[rng.random(shape) < minus] = -1
+    return np.ascontiguousarray(lab)
+
+
+@pytest.mark.parametrize("zrun", [4, 16, 64])
+@pytest.mark.parametrize("step", [1, 2, 3, 4, 5, 6, 8])
+def test_jfa_single_pass_bitset_and_ties(asv, orc, step, zrun):
+    """Labels constant on small cubes keep a sub-tile's footprint under 32
+    labels, so the pass takes the bit-set form (steps <= 6); seeds come in
+    identical pairs (same position, colour and metric), so pairs of labels
+    tie at the least distance (thousands of voxels per case) and the
+    shader's candidate order decides.  A third of the volume holds random
+    labels (footprints over 32 labels: the list form)."""
+    W, H, D, K = 90, 70, 40, 300
+    rgb, fwd, bwd = small_clip(asv, W, H, D, seed=13)
+    img = _gpu_clip(asv, rgb, fwd, bwd, K, 2, jfa_zrun=zrun)
+    lab4 = img.lab()
+    rng = np.random.default_rng(100 + step)
+    kp = img.info().Kp
+    seeds = np.zeros((kp, 12), np.float32)
+    seeds[:, 0] = rng.integers(0, W, kp) + 0.5
+    seeds[:, 1] = rng.integers(0, H, kp) + 0.5
+    seeds[:, 2] = rng.integers(0, D, kp) + 0.5
+    seeds[:, 3:6] = rng.integers(0, 256, (kp, 3)).astype(np.float32)
+    A = rng.normal(0, 0.3, (kp, 3, 3)).astype(np.float32)
+    M = np.einsum("kij,kil->kjl", A, A)
+    seeds[:, 6:12] = M[:, [0, 0, 0, 1, 1, 2], [0, 1, 2, 1, 2, 2]]
+    seeds[: kp // 8, 6:12] *= -1.0
+    seeds[1::2] = seeds[0::2][: kp // 2]                  # identical pairs: exact ties
+    img.set_seeds(seeds)
+    labels = _blocky_labels(rng, (D, H, W), 24, 6)           # 12 tying pairs, often neighbours
+    labels[: D // 2, H // 2:] = _blocky_labels(rng, (D // 2, H - H // 2, W), kp, 5)
+    labels[:, :, : W // 3] = rng.integers(-1, kp, (D, H, W // 3))
+    ratio = 0.0123
+    got = img.jfa_pass(labels, step, ratio)
+    want = orc.jfa_pass(labels, lab4, seeds, step, ratio)
+    assert mismatch(got, want) == 0
+    img.close()
+
+
 CASES = [
     # W, H, D, K, iters, variant, full_ladder, density
     (64, 48, 12, 60, 4, 0, 0, 1),
