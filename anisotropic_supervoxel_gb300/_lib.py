@@ -42,7 +42,7 @@ class Info(ctypes.Structure):
 class Stats(ctypes.Structure):
     _fields_ = [("jfa_ms", ctypes.c_double), ("jfa_launches", c_int),
                 ("centroid_ms", ctypes.c_double), ("metric_ms", ctypes.c_double),
-                ("total_ms", ctypes.c_double), ("launches", c_int)]
+                ("total_ms", ctypes.c_double), ("launches", c_int), ("window_ms", ctypes.c_double)]
 
 
 class StreamInfo(ctypes.Structure):

@@ -1560,6 +1560,12 @@ asv_status asv_stream_push(asv_ctx *ctx, const uint8_t *rgb, const float *fwd, c
     ctx->maxpass = h.npass;
     ctx->jfa_blocks = jfa_blocks_for(ctx, tiles);
 
+    // device time of the window's compute: from here (its frames are on the
+    // device) to the labels mapped, before they are read back
+    asv_status es = ensure_events(ctx, 2);
+    if (es != ASV_OK) return es;
+    const size_t ev0 = ctx->ev.size() - 2;
+    CK(cudaEventRecord(ctx->ev[ev0], st));
     asv_launch_rgb2lab(d, st);                                   // new frames only (lab_from)
     CK(cudaMemsetAsync(d.dacc, 0, sizeof(unsigned long long) * d.total_seeds, st));
     asv_launch_density(d, st);
@@ -1581,17 +1587,24 @@ asv_status asv_stream_push(asv_ctx *ctx, const uint8_t *rgb, const float *fwd, c
     ctx->seg[0].seed_off = 0;
 
     // seed_matrix, RGB2LAB (above), Lloyd loop, check_dead_seeds (Render.cpp:470-512)
-    ctx->launches = 0;
+    ctx->launches = 4;                                           // LAB, density (2), seed composition
     asv_launch_metric(d, 0, st);
+    ctx->launches += 5;
     enqueue_lloyd(ctx, false);
     const int keep = b < m.nb - 1;
     asv_launch_stream_next(d, m.s, (float)(m.bs - one_third), (float)two_third, keep, st);
     const int done = keep ? Db - one_third : Db;
     asv_launch_stream_map(d, m.s, (long long)WH * done, st);
+    ctx->launches += 2;
     CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->ev[ev0 + 1], st));
     CK(cudaMemcpyAsync(labels_out, m.s.lab_out, sizeof(int32_t) * WH * done, cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(ctr, m.s.ctr, sizeof(ctr), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    float wms = 0.f;
+    CK(cudaEventElapsedTime(&wms, ctx->ev[ev0], ctx->ev[ev0 + 1]));
+    ctx->stats.window_ms = wms;
+    ctx->stats.launches = ctx->launches;
     std::swap(m.s.kept_pos, m.s.kept_next);
     std::swap(m.s.gmap_prev, m.s.gmap_cur);
     m.placed = ctr[STREAM_PLACED];

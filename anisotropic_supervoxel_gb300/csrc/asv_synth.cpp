@@ -244,6 +244,9 @@ extern "C" int asv_write_labels_txt(const char *path, const int32_t *labels, int
     return std::fclose(f) == 0 ? 0 : -3;
 }
 
+// the render writer needs the palette of asv_png.cpp; a build of the
+// generator alone (ASV_SYNTH_ONLY) leaves it out
+#ifndef ASV_SYNTH_ONLY
 extern "C" int asv_write_render_ppm(const char *prefix, const int32_t *labels, int W, int H, int D,
                                     int n_labels)
 {
@@ -262,3 +265,4 @@ extern "C" int asv_write_render_ppm(const char *prefix, const int32_t *labels, i
     }
     return 0;
 }
+#endif

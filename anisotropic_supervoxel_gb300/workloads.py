@@ -48,13 +48,31 @@ def serving_mix():
     ]
 
 
-def make_clip(w, scale=None):
-    """rgb, fwd, bwd of a workload dict (optionally spatially scaled for tests)."""
-    from .image import synth_clip
+def make_clip(w, scale=None, gen=None):
+    """rgb, fwd, bwd of a workload dict (optionally spatially scaled for
+    tests).  `gen` is the generator (a function with synth_clip's
+    arguments); default this package's."""
+    if gen is None:
+        from .image import synth_clip as gen
     W, H, D = w["W"], w["H"], w["D"]
     if scale:
         W, H, D = max(8, int(W * scale)), max(8, int(H * scale)), max(4, int(D * scale))
-    return synth_clip(W, H, D, n_ellipses=w["n_ellipses"], noise_sigma=w["noise_sigma"],
-                      vmax=w["vmax"], jitter=w.get("jitter", 0.0),
-                      drift_amp=w.get("drift_amp", 0.0), drift_period=w.get("drift_period", 60.0),
-                      seed=w["seed"])
+    return gen(W, H, D, n_ellipses=w["n_ellipses"], noise_sigma=w["noise_sigma"],
+               vmax=w["vmax"], jitter=w.get("jitter", 0.0),
+               drift_amp=w.get("drift_amp", 0.0), drift_period=w.get("drift_period", 60.0),
+               seed=w["seed"])
+
+
+def stream_frames(w, frame0, n, gen=None, crop=None):
+    """Frames [frame0, frame0 + n) of the streaming video `w` (rgb, fwd,
+    bwd); crop = (x0, y0, cw, ch) cuts that region out of every frame (the
+    rows counted in the frames' texture orientation, y up)."""
+    if gen is None:
+        from .image import synth_clip as gen
+    rgb, fwd, bwd = gen(w["W"], w["H"], n, n_ellipses=w["n_ellipses"], noise_sigma=w["noise_sigma"],
+                        vmax=w["vmax"], jitter=w.get("jitter", 0.0), drift_amp=w.get("drift_amp", 0.0),
+                        drift_period=w.get("drift_period", 60.0), seed=w["seed"], frame0=frame0)
+    if crop is not None:
+        x0, y0, cw, ch = crop
+        rgb, fwd, bwd = (np.ascontiguousarray(a[:, y0:y0 + ch, x0:x0 + cw]) for a in (rgb, fwd, bwd))
+    return rgb, fwd, bwd

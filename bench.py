@@ -1,17 +1,28 @@
 #!/usr/bin/env python3
-"""Throughput of the supervoxel JFA+Lloyd loop on GB300 (one JSON line).
+"""Throughput and window latency of the supervoxel JFA+Lloyd path on GB300
+(one JSON line).
 
-step      one full Lloyd loop (all iterations: metric solves, reseeding, every
-          JFA pass, centroid sums, post-processing) over one synthetic clip.
-value     Mvoxel-iterations/s = W*H*D*iters*steps / device time, inputs
-          resident in HBM; L2 flushed (512 MiB write) before every step.
-e2e       the same metric through the public C ABI with pinned host buffers:
-          RGB + flow upload, seed placement, metric, LAB, loop, labels back.
+Default workload (stream_720p): the 1280x720 streaming video, 900 frames in
+windows of 30 with 10 overlap, 2000 new seeds per window, 20 Lloyd
+iterations, on one resident streaming context.
+step      one window (asv_stream_push): its new frames up, seed placement,
+          metric, LAB, the Lloyd loop (every JFA pass, centroid sums,
+          reseeding), post-processing, video-wide labels down.
+value     Mvoxel-iterations/s = window voxels x 20 / device time of the
+          window's compute (CUDA events; its new frames already in HBM).
+e2e       the same metric over asv_stream_push's wall time with pinned host
+          buffers; latency_ms p50/p99 of the same calls.
 --impl reference
-          the CPU restatement of the reference's path (the reference's own
-          GLSL/OpenGL pipeline cannot run here) on all host cores.
-Multi-GPU: replicas only (independent clips per rank, no collective on the
-data path); value = all ranks' voxel-iterations / max rank time.
+          the CPU restatement of the reference's path (its own GLSL/OpenGL
+          pipeline cannot run here) on all host cores, over a 256x144 crop of
+          the same video with the same seed spacing, timed over the same
+          region (whole windows).  That process loads no library of the GPU
+          path (its inputs come from the generator compiled on its own).
+Other workloads (--workload): single clips, the 16-clip batch, serving,
+connectivity, the whole pipeline, evaluation.
+Multi-GPU: replicas only (each rank runs its own stream or clip, no
+collective on the data path); value = all ranks' voxel-iterations / max
+rank time.
 """
 import argparse
 import json
@@ -31,6 +42,7 @@ METRIC = ("Mvoxel-iterations/s (JFA+Lloyd) and p50/p99 window latency vs plain f
 UNIT = "Mvoxel-iterations/s"
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 TRAFFIC = os.path.join(ROOT, "profiles", "k_jfa_320x240x85.md")
+TRAFFIC_720P = os.path.join(ROOT, "profiles", "k_jfa_1280x720x30.md")
 # algorithmic bytes per voxel of one JFA pass: label in 4 + label out 4 + LAB 3
 JFA_BYTES_PER_VOXEL = 11
 # nominal FP32 work per voxel of one JFA pass: 27 candidates x 33 operations
@@ -43,13 +55,14 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="clip_320x240x85",
+    ap.add_argument("--workload", default="stream_720p",
                     choices=["clip_320x240x85", "clip_240x160x30", "batch16", "stream_720p",
                              "serve_mix", "connect_320x240x85", "pipeline_320x240x85",
                              "pipeline_png_320x240x85", "quality_320x240x85", "stream_720p_flow"])
     ap.add_argument("--requests", type=int, default=160, help="serve_mix: requests in the run")
     ap.add_argument("--rate", type=float, default=40.0, help="serve_mix: mean arrivals per second")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="stream_720p: skip the per-clip extra key")
     return ap.parse_args()
 
 
@@ -132,10 +145,10 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def profile_value(key):
-    """A `key: value` line of the committed k_jfa ncu summary."""
+def profile_value(key, path=None):
+    """A `key: value` line of a committed k_jfa ncu summary."""
     try:
-        with open(TRAFFIC) as f:
+        with open(path or TRAFFIC) as f:
             for line in f:
                 if line.startswith(key + ":"):
                     return float(line.split(":")[1])
@@ -175,14 +188,17 @@ def run_reference(args):
     ws, rank, _ = dist()
     if rank != 0:
         return
+    if args.workload == "stream_720p":
+        return run_stream_reference(args)
     if args.workload not in ("clip_320x240x85", "clip_240x160x30"):
         print(json.dumps({"impl": "reference", "unavailable": "the CPU arm covers the single-clip "
                           "workloads; " + args.workload + " has no CPU counterpart"}), flush=True)
         return
     w = workload(args.workload)
     from anisotropic_supervoxel_gb300 import workloads
-    rgb, fwd, bwd = workloads.make_clip(w)
-    iters = 3
+    from oracle import oracle
+    rgb, fwd, bwd = workloads.make_clip(w, gen=oracle.synth_clip)
+    iters = w["iters"]
     for _ in range(args.warmup):
         cpu_baseline(w, rgb, fwd, bwd, iters)
     vals = []
@@ -491,61 +507,274 @@ def run_batch16(args):
            "clocks": clk, "gpu_launches": int(launches * args.steps)})
 
 
+# crop of the 1280x720 stream timed by the CPU arms and used for the
+# agreement check: the 256x144 region at (512, 288) of every frame (1/25 of
+# the area) with 1/25 of the new seeds per window: the same voxels per seed,
+# so the same seed spacing s = 23 and JFA ladder as the full frame
+STREAM_CROP = (512, 288, 256, 144)
+STREAM_CROP_SEEDS100 = 10000 // 25
+
+
+def _stream_windows_frames(n_windows):
+    """frames of a video of n_windows stream windows (30 + 20 per further window)"""
+    return 30 + 20 * (n_windows - 1)
+
+
+def _oracle_stream(w, n_windows, nthreads, gen):
+    """the oracle's streaming run over the crop video of n_windows windows:
+    (labels, blocks, seconds, voxel-iterations)"""
+    from anisotropic_supervoxel_gb300 import workloads
+    from oracle import oracle
+    D_all = _stream_windows_frames(n_windows)
+    rgb, fwd, bwd = workloads.stream_frames(w, 0, D_all, gen=gen, crop=STREAM_CROP)
+    t = time.perf_counter()
+    labels, info = oracle.run_stream(rgb, fwd, bwd, seeds_num_100=STREAM_CROP_SEEDS100, iters=w["iters"],
+                                     block_size=w["block_size"], nthreads=nthreads)
+    dt = time.perf_counter() - t
+    cw, ch = STREAM_CROP[2], STREAM_CROP[3]
+    return labels, info["blocks"], dt, info["blocks"] * cw * ch * w["block_size"] * w["iters"], (rgb, fwd, bwd)
+
+
+def _stream_config(w, ws, device_flow=False):
+    return {"workload": "stream_1280x720x900_w30o10_K2000_I20" + ("_device_flow" if device_flow else ""),
+            "W": w["W"], "H": w["H"], "frames": w["D_all"], "window": w["block_size"], "overlap": 10,
+            "K_window": w["K_window"], "seeds_num_100": w["seeds_num_100"], "lloyd_iters": w["iters"],
+            "ellipses": w["n_ellipses"], "noise_sigma": w["noise_sigma"], "variant": "stream",
+            "step": "one window: its 20 new frames up, seeds, metric, LAB, 20 Lloyd iterations, "
+                    "post-processing, video-wide labels down",
+            "parallelism": f"replicas{ws}", "l2": "inputs larger than L2 (each window 27.6 M voxels, ~1.1 GB)"}
+
+
 def run_stream_720p(args, device_flow=False):
-    """1280x720 video, 900 frames, 30-frame windows with 10-frame overlap, on
-    one resident streaming context; per-window latency = asv_stream_push wall
-    time (new frames up from pinned memory, the window's Lloyd loop, finished
-    labels back)."""
+    """The headline: the 1280x720 streaming video (900 frames, windows of 30
+    with 10 overlap, 2000 new seeds per window, 20 Lloyd iterations) on one
+    resident streaming context.  A step is one window (asv_stream_push).
+    value: window voxel-iterations / device time of the window's compute
+    (CUDA events from its first kernel, its new frames already in HBM, to
+    its labels mapped); e2e and latency: wall time of asv_stream_push with
+    pinned host buffers (new frames up, compute, finished labels down)."""
     import numpy as np
     import torch
 
     import anisotropic_supervoxel_gb300 as asv
     from anisotropic_supervoxel_gb300 import workloads
-    torch.cuda.set_device(0)
+
+    ws, rank, local = dist()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+
     w = workloads.STREAM_720P
-    W, H, D_all, bs = w["W"], w["H"], w["D_all"], w["block_size"]
+    W, H, D_all, bs, I = w["W"], w["H"], w["D_all"], w["block_size"], w["iters"]
     s100 = w["seeds_num_100"]
-    st = asv.Stream(W, H, D_all, seeds_num_100=s100, block_size=bs, lloyd_iters=w["iters"])
-    nb = st.info().blocks
-    lat, vox_it, kps = [], 0, []
-    clocks = Clocks(0)
-    clocks.start()
-    t_all = 0.0
-    for b in range(nb):
+    pin = {k: _pinned(np.zeros((bs,) + sh, dt)) for k, sh, dt in
+           (("rgb", (H, W, 3), np.uint8), ("fwd", (H, W, 2), np.float32), ("bwd", (H, W, 2), np.float32))}
+
+    def new_stream():
+        return asv.Stream(W, H, D_all, seeds_num_100=s100, block_size=bs, lloyd_iters=I, device=local)
+
+    st = new_stream()
+    lat, dev_ms, vox_it, kps, launches, h2d, d2h = [], [], 0, [], 0, 0, 0
+    clocks = Clocks(local)
+    t_region = 0.0
+    for k in range(args.warmup + args.steps):
+        if st.info().next_block >= st.info().blocks:        # the video is done: start it again
+            st.close()
+            st = new_stream()
         inf = st.info()
-        a = inf.block_end - inf.frames_needed
-        rgb, fwd, bwd = asv.synth_clip(W, H, inf.frames_needed, n_ellipses=w["n_ellipses"],
-                                       noise_sigma=w["noise_sigma"], vmax=w["vmax"],
-                                       drift_amp=w["drift_amp"], drift_period=w["drift_period"],
-                                       seed=w["seed"], frame0=a)
-        rgb, fwd, bwd = _pinned(rgb), _pinned(fwd), _pinned(bwd)
+        n = inf.frames_needed
+        a = inf.block_end - n
+        frames = workloads.stream_frames(w, a, n)
+        for key, arr in zip(("rgb", "fwd", "bwd"), frames):
+            pin[key][:n] = arr
+        args_push = (pin["rgb"][:n],) if device_flow else (pin["rgb"][:n], pin["fwd"][:n], pin["bwd"][:n])
+        if k == args.warmup:
+            barrier()
+            torch.cuda.synchronize()
+            clocks.start()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        if device_flow:
-            st.push(rgb)                       # the block's flow computed on the device
-        else:
-            st.push(rgb, fwd, bwd)
+        f0, lab = st.push(*args_push)
         dt = time.perf_counter() - t0
-        if b >= args.warmup:
+        if k >= args.warmup:
+            s = st.stats()
             lat.append(dt * 1e3)
-            vox_it += W * H * (inf.block_end - inf.block_start) * w["iters"]
-            t_all += dt
+            dev_ms.append(s.window_ms)
+            launches += s.launches
+            vox_it += W * H * (inf.block_end - inf.block_start) * I
             kps.append(st.info().block_Kp)
+            h2d += n * W * H * (3 if device_flow else 19)
+            d2h += lab.nbytes
+            t_region += dt
+    torch.cuda.synchronize()
+    barrier()
     clk = clocks.stop()
     st.close()
-    value = vox_it / t_all / 1e6
-    _line(args, value, statistics.mean(lat),
-          {"workload": "stream_1280x720x900_w30o10" + ("_device_flow" if device_flow else ""),
-           "K_window": w["K_window"],
-           "seeds_num_100": s100, "lloyd_iters": w["iters"], "variant": "stream",
-           "parallelism": "replicas1", "l2": "inputs larger than L2 (each window 27.6 M voxels)"},
-          {"latency_ms": {"p50": _pct(lat, 50), "p99": _pct(lat, 99), "max": max(lat),
-                          "windows": len(lat), "target_p99": 33.0},
-           "block_Kp_mean": statistics.mean(kps),
-           "e2e": {"value": value, "unit": UNIT,
-                   "h2d_bytes_per_step": int(W * H * 20 * (3 if device_flow else 19)),
-                   "d2h_bytes_per_step": int(W * H * 20 * 4)},
-           "clocks": clk})
+    value, dev_s = replicas_value(vox_it / 1e6, sum(dev_ms) / 1e3, f"cuda:{local}")
+    e2e_val, e2e_s = replicas_value(vox_it / 1e6, t_region, f"cuda:{local}")
+
+    # k_jfa per launch at this size: the Lloyd loop of the video's first 30
+    # frames (2000 seeds, stream variant) with a CUDA event around every pass
+    rgb, fwd, bwd = workloads.stream_frames(w, 0, bs)
+    prof = asv.Image(lloyd_iters=I, device=local, instrument=1, use_graph=0, variant=1)
+    prof.init_gpu(rgb, w["K_window"])
+    prof.upload_flow(fwd, bwd)
+    prof.initialization()
+    prof.seed_matrix()
+    prof.RGB2LAB()
+    prof.run_lloyd()
+    jfa_ms, jfa_n, loop_ms = 0.0, 0, 0.0
+    for _ in range(3):
+        prof.run_lloyd()
+        s = prof.stats()
+        jfa_ms += s.jfa_ms
+        jfa_n += s.jfa_launches
+        loop_ms += s.total_ms
+    prof.close()
+    nvox = W * H * bs
+    jfa_launch_s = jfa_ms / jfa_n / 1e3
+    peak, peak_kind = peaks()
+    achieved = JFA_BYTES_PER_VOXEL * nvox / jfa_launch_s / 1e9
+    tpv = profile_value("dram_bytes_per_voxel", TRAFFIC_720P)
+
+    # agreement with the oracle on the crop sample (the same windows the CPU
+    # arm times), and the CPU baseline itself
+    cb = agree = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        n_win = 2
+        want, nb, cpu_s, cpu_vox, (crgb, cfwd, cbwd) = _oracle_stream(w, n_win, os.cpu_count() or 1, None)
+        cw, ch = STREAM_CROP[2], STREAM_CROP[3]
+        cst = asv.Stream(cw, ch, crgb.shape[0], seeds_num_100=STREAM_CROP_SEEDS100, block_size=bs, lloyd_iters=I,
+                         device=local)
+        got = np.full(want.shape, -7, np.int32)
+        for _ in range(cst.info().blocks):
+            ci = cst.info()
+            a0 = ci.block_end - ci.frames_needed
+            f0, lab = cst.push(crgb[a0:ci.block_end], cfwd[a0:ci.block_end], cbwd[a0:ci.block_end])
+            got[f0:f0 + lab.shape[0]] = lab
+        cst.close()
+        agree = {"voxels": int(want.size), "equal": float((got == want).mean()), "bit_exact": bool((got == want).all()),
+                 "sample": f"{cw}x{ch} crop at ({STREAM_CROP[0]}, {STREAM_CROP[1]}) of frames 0-{want.shape[0] - 1}, "
+                           f"{nb} windows, {I} iterations, seeds_num_100 {STREAM_CROP_SEEDS100} (same seed spacing)",
+                 "against": "the oracle (CPU restatement of the reference's shaders and Render/Image host logic)"}
+        cb = {"value": cpu_vox / cpu_s / 1e6, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+              "sample": f"the oracle's streaming run over a {cw}x{ch} crop of the same video (frames 0-"
+                        f"{want.shape[0] - 1}, {nb} windows of 30, 20 iterations, 1/25 of the seeds: the same seed "
+                        f"spacing and JFA ladder), OpenMP over {os.cpu_count()} threads, {cpu_s:.1f} s"}
+
+    extra = {}
+    if rank == 0 and ws == 1 and not getattr(args, "no_extras", False):
+        extra["clip_320x240x85"] = _clip_rate(args, workloads.CLIP_320x240x85, local)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_s * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded ellipse video with background drift, exact generating flow"
+                    + ("; flow computed on the device" if device_flow else "") + ")",
+            "config": _stream_config(w, ws, device_flow),
+            "latency_ms": {"p50": _pct(lat, 50), "p99": _pct(lat, 99), "max": max(lat), "windows": len(lat),
+                           "device_p50": _pct(dev_ms, 50), "device_p99": _pct(dev_ms, 99),
+                           "what": "asv_stream_push wall time per window (frames up, compute, labels down); "
+                                   "device_*: its compute alone", "target_p99": 33.0},
+            "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(h2d / args.steps),
+                    "d2h_bytes_per_step": int(d2h / args.steps)},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind, "kernel": "k_jfa",
+                         "bytes_per_launch": JFA_BYTES_PER_VOXEL * nvox, "launch_ms": jfa_launch_s * 1e3,
+                         "launch_of": "a k_jfa gather pass over one 1280x720x30 window (27.6 M voxels)",
+                         "traffic": tpv * nvox if tpv is not None else None,
+                         "issue_active_ncu": profile_value("issue_active", TRAFFIC_720P),
+                         "jfa_share_of_loop": jfa_ms / loop_ms if loop_ms else None},
+            "block_Kp_mean": statistics.mean(kps),
+            "clocks": clk, "gpu_launches": int(launches),
+        }
+        if agree is not None:
+            line["agreement"] = agree
+        if cb is not None:
+            line["cpu_baseline"] = cb
+        line.update(extra)
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def _clip_rate(args, w, local, steps=5):
+    """the per-clip form on one clip (extra key of the headline line):
+    device-timed Lloyd loop with inputs resident, and end to end"""
+    import torch
+
+    import anisotropic_supervoxel_gb300 as asv
+    from anisotropic_supervoxel_gb300 import workloads
+    rgb, fwd, bwd = workloads.make_clip(w)
+    D, H, W, _ = rgb.shape
+    img = asv.Image(lloyd_iters=w["iters"], device=local)
+    img.init_gpu(rgb, w["K"])
+    img.upload_flow(fwd, bwd)
+    img.initialization()
+    img.seed_matrix()
+    img.RGB2LAB()
+    for _ in range(3):
+        img.run_lloyd()
+    img.synchronize()
+    st = torch.cuda.ExternalStream(img.stream(), device=torch.device("cuda", local))
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    ms = []
+    for k in range(steps):
+        with torch.cuda.stream(st):
+            flush.fill_(k & 255)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        img.run_lloyd()
+        e1.record(st)
+        st.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    img.close()
+    vox_it = W * H * D * w["iters"]
+    return {"value": vox_it / (sum(ms) / len(ms) / 1e3) / 1e6, "unit": UNIT, "ms_per_loop": sum(ms) / len(ms),
+            "workload": f"clip_{W}x{H}x{D}_K{w['K']}_I{w['iters']}, Lloyd loop on the device, inputs resident"}
+
+
+def run_stream_reference(args):
+    """The CPU arm of the headline: the oracle's streaming run (the
+    reference's path restated on the host cores) over the 256x144 crop of the
+    same video, which keeps the per-voxel work (seed spacing, JFA ladder).
+    W untimed warm-up windows, then a video of exactly K windows timed.  Its
+    inputs come from the generator compiled on its own (oracle.synth_clip):
+    this process loads no library of the GPU path."""
+    ws, rank, _ = dist()
+    if rank != 0:
+        return
+    from anisotropic_supervoxel_gb300 import workloads
+    from oracle import oracle
+    w = workloads.STREAM_720P
+    n = os.cpu_count() or 1
+    if args.warmup > 0:
+        _oracle_stream(w, args.warmup, n, oracle.synth_clip)
+    labels, nb, dt, vox, _ = _oracle_stream(w, args.steps, n, oracle.synth_clip)
+    v = vox / dt / 1e6
+    cw, ch = STREAM_CROP[2], STREAM_CROP[3]
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded ellipse video with background drift, exact generating flow)",
+        "config": _stream_config(w, 1),
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": n, "kind": "port",
+                         "sample": f"{cw}x{ch} crop at ({STREAM_CROP[0]}, {STREAM_CROP[1]}) of the video, {nb} windows "
+                                   f"of 30 frames (the first {nb}), 20 iterations, 1/25 of the seeds (the same seed "
+                                   f"spacing and JFA ladder as the full frame); OpenMP over {n} threads; {dt:.1f} s"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "windows_timed": nb,
+        "note": "the reference's own pipeline is GLSL over OpenGL (no graphics stack here); this arm runs the "
+                "C restatement of its shader maths and Render/Image host logic, timed over the same region "
+                "as the GPU arm (a whole window: seeds, metric, LAB, the Lloyd loop, post-processing)",
+    }), flush=True)
 
 
 def run_serve_mix(args):

@@ -91,7 +91,10 @@ typedef struct asv_stats {
     double centroid_ms;
     double metric_ms;
     double total_ms;    /* device time of the last asv_run_lloyd */
-    int launches;       /* kernels launched by the last asv_run_lloyd */
+    int launches;       /* kernels launched by the last asv_run_lloyd or asv_stream_push */
+    double window_ms;   /* device time of the last asv_stream_push's compute: from its
+                           first kernel (the window's new frames already uploaded) to the
+                           window's labels mapped, before they are read back */
 } asv_stats;
 
 typedef struct asv_ctx asv_ctx;

@@ -31,8 +31,61 @@ class GridInfo(ctypes.Structure):
     _fields_ = [(n, c_int) for n in ("s", "dNum", "hNum", "wNum", "Kp")]
 
 
+# The seeded synthetic-clip generator (asv_synth_clip) compiled on its own,
+# so that CPU-only runs (the timed CPU restatement) generate their inputs
+# without loading libasv.so; same source and host flags as in libasv.so.
+SYNTH_SRC = os.path.join(os.path.dirname(HERE), "anisotropic_supervoxel_gb300", "csrc", "asv_synth.cpp")
+SYNTH_INC = [os.path.join(os.path.dirname(HERE), "include"),
+             os.path.join(os.path.dirname(HERE), "anisotropic_supervoxel_gb300", "csrc")]
+SYNTH_LIB = os.path.join(HERE, "libsynth.so")
+
+
+def build_synth(force=False):
+    if not force and os.path.exists(SYNTH_LIB) and os.path.getmtime(SYNTH_LIB) >= max(
+            os.path.getmtime(SYNTH_SRC), os.path.getmtime(__file__)):
+        return SYNTH_LIB
+    tmp = SYNTH_LIB + ".tmp"
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-shared", "-DASV_SYNTH_ONLY",
+           *[f"-I{d}" for d in SYNTH_INC], "-o", tmp, SYNTH_SRC]
+    p = subprocess.run(cmd, capture_output=True, text=True)
+    if p.returncode != 0:
+        raise RuntimeError("synthetic generator build failed:\n" + p.stdout + p.stderr)
+    os.replace(tmp, SYNTH_LIB)
+    return SYNTH_LIB
+
+
+class SynthParams(ctypes.Structure):
+    _fields_ = [("W", c_int), ("H", c_int), ("frame0", c_int), ("nframes", c_int), ("n_ellipses", c_int),
+                ("noise_sigma", c_float), ("vmax", c_float), ("jitter", c_float), ("drift_amp", c_float),
+                ("drift_period", c_float), ("seed", ctypes.c_uint64)]
+
+
+_SYNTH = None
+
+
+def synth_clip(W, H, D, n_ellipses=12, noise_sigma=5.0, vmax=3.0, jitter=0.0, drift_amp=0.0,
+               drift_period=60.0, seed=1, frame0=0):
+    """The seeded synthetic clip (rgb uint8 [D,H,W,3], fwd/bwd float32
+    [D,H,W,2]), identical to anisotropic_supervoxel_gb300.synth_clip."""
+    global _SYNTH
+    if _SYNTH is None:
+        build_synth()
+        _SYNTH = ctypes.CDLL(SYNTH_LIB)
+        _SYNTH.asv_synth_clip.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p]
+        _SYNTH.asv_synth_clip.restype = c_int
+    rgb = np.empty((D, H, W, 3), np.uint8)
+    fwd = np.empty((D, H, W, 2), np.float32)
+    bwd = np.empty((D, H, W, 2), np.float32)
+    p = SynthParams(W, H, frame0, D, n_ellipses, noise_sigma, vmax, jitter, drift_amp, drift_period, seed)
+    if _SYNTH.asv_synth_clip(ctypes.byref(p), _p(rgb), _p(fwd), _p(bwd)) != 0:
+        raise ValueError("bad synthetic clip parameters")
+    return rgb, fwd, bwd
+
+
 def build(force=False):
-    """Compiles liboracle.so with -ffp-contract=off (no FMA contraction)."""
+    """Compiles liboracle.so with -ffp-contract=off (no FMA contraction), and
+    the generator library."""
+    build_synth(force)
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(
             os.path.getmtime(SRC), os.path.getmtime(HDR), os.path.getmtime(__file__)):
         return LIB

@@ -53,3 +53,24 @@ def test_reference_arm_prints_on_rank0_only():
     assert p.returncode == 0
     line = json.loads(p.stdout.strip().splitlines()[-1])
     assert line["impl"] == "reference" and "unavailable" in line
+
+
+def test_reference_arm_loads_no_gpu_library():
+    """The headline's CPU arm (stream_720p) times the oracle on one window of
+    the crop sample, with inputs from the generator compiled on its own: the
+    process maps the oracle's libraries and not libasv.so."""
+    code = ("import runpy, sys; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '0'];"
+            "runpy.run_path('bench.py', run_name='__main__');"
+            "m = open('/proc/self/maps').read();"
+            "print('MAPPED', sorted({l.split()[-1].rsplit('/', 1)[-1] for l in m.splitlines() if '.so' in l}))")
+    env = dict(os.environ, RANK="0", WORLD_SIZE="1", LOCAL_RANK="0")
+    p = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, env=env,
+                       timeout=600)
+    assert p.returncode == 0, p.stderr[-2000:]
+    lines = p.stdout.strip().splitlines()
+    line = json.loads(lines[-2])
+    assert line["impl"] == "reference" and line["steps"] == 1 and line["windows_timed"] == 1
+    assert line["config"]["workload"].startswith("stream_1280x720")
+    mapped = lines[-1]
+    assert "liboracle.so" in mapped and "libsynth.so" in mapped
+    assert "libasv.so" not in mapped

@@ -386,3 +386,19 @@ def test_middlebury_step_known_answers(orc):
         assert g.s == int(math.floor(math.pow(1.0 * W * H / K, 0.5))), (W, H, D, K)
         _, g0 = orc.grid_seeds(W, H, D, K, middlebury=0)
         assert g0.s == int(math.floor(math.pow((W * H * D) // K, 1.0 / 3))), (W, H, D, K)
+
+
+def test_oracle_generator_equals_library(asv, orc):
+    """The generator library of the CPU-only runs (oracle.synth_clip)
+    produces the very clips of asv.synth_clip, so both timed arms segment
+    the same inputs."""
+    for args in [dict(W=64, H=48, D=5, n_ellipses=6, noise_sigma=5.0, seed=3),
+                 dict(W=160, H=90, D=4, n_ellipses=60, noise_sigma=5.0, vmax=3.0, drift_amp=6.0,
+                      drift_period=90.0, seed=20240604, frame0=37),
+                 dict(W=33, H=17, D=3, n_ellipses=2, noise_sigma=8.0, jitter=0.5, seed=9)]:
+        a = asv.synth_clip(**{k: v for k, v in args.items() if k not in ("W", "H", "D")},
+                           W=args["W"], H=args["H"], D=args["D"])
+        b = orc.synth_clip(**{k: v for k, v in args.items() if k not in ("W", "H", "D")},
+                           W=args["W"], H=args["H"], D=args["D"])
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y)
