@@ -304,8 +304,14 @@ int orc_density_adjust(const uint8_t *rgb, int W, int H, int D, const float *gri
 /* Sum of v[0..m-1] in the CUDA solver's warp butterfly order: 32 slots
  * (the values, then +0); for off = 16, 8, 4, 2, 1 slot i < off takes
  * t[i] + t[i + off]; the sum is slot 0. */
+static int g_solver;
 static float lane_sum(const float *v, int m)
 {
+    if (g_solver & 8) {                      /* the control: the same sums in sequential order */
+        float acc = 0.0f;
+        for (int i = 0; i < m; i++) acc = acc + v[i];
+        return acc;
+    }
     float t[32];
     for (int i = 0; i < 32; i++) t[i] = i < m ? v[i] : 0.0f;
     for (int off = 16; off > 0; off >>= 1)
@@ -482,6 +488,391 @@ static void m6_nearest_psd(const float M[6], float out[6])
     }
 }
 
+/* ======================================================================
+ * Second restatement of the metric solve, for measuring how much the
+ * labels depend on the solver (orc_set_solver(1)): the algorithms of the
+ * reference's Eigen calls, all in FP32 as the reference's MatrixXf is.
+ *   - BDCSVD(A).solve(b) (Image.cpp:961): for a matrix of 6 columns BDCSVD
+ *     hands the work to a two-sided Jacobi SVD; a non-square matrix is first
+ *     reduced by a Householder QR with column pivoting (of A when it has
+ *     more rows than columns, of A^T otherwise), the square factor is
+ *     diagonalised by 2x2 rotation pairs (the left rotation makes the 2x2
+ *     block symmetric, a symmetric Jacobi rotation then diagonalises it)
+ *     until every off-diagonal entry is within 2 eps of its diagonal pair;
+ *     singular values below sigma_max * min(m, 6) * eps count as zero and
+ *     the solve is the minimum-norm one.
+ *   - eigenvalues() (Image.cpp:997-1006): the matrix as a general 3x3 one,
+ *     Householder reduction to Hessenberg form, then Francis double-shift QR
+ *     steps with deflation on negligible subdiagonal entries; "negative"
+ *     when an eigenvalue's real part is below 0.
+ *   - the nearest PSD matrix (Image.cpp:786-835, :1460-1534): eigenvectors
+ *     of the symmetric matrix (cyclic Jacobi in FP32), negative eigenvalues
+ *     set to 0, V diag V^T.
+ * These are this project's implementations of the published methods, not
+ * Eigen itself (which is not vendored); they differ from the primary solver
+ * (and from Eigen) in rounding only.
+ * ==================================================================== */
+/* g_solver bit 0: least squares, bit 1: PSD test, bit 2: nearest PSD by
+ * the second restatement; bit 3: the primary solver's column sums in
+ * sequential order (a control: the same algorithm, other rounding) */
+void orc_set_solver(int mode) { g_solver = mode == 1 ? 7 : mode; }
+
+/* two-sided Jacobi SVD of the square n x n matrix a (row-major, n <= 6):
+ * a = U diag(s) V^T, s >= 0 sorted descending */
+static void jacobi2_svd(int n, float a[6][6], float U[6][6], float V[6][6], float s[6])
+{
+    for (int r = 0; r < n; r++)
+        for (int c = 0; c < n; c++) { U[r][c] = r == c ? 1.0f : 0.0f; V[r][c] = U[r][c]; }
+    for (int sweep = 0; sweep < 64; sweep++) {
+        int done = 1;
+        for (int p = 1; p < n; p++)
+            for (int q = 0; q < p; q++) {
+                float thr = 2.0f * FLT_EPSILON * fmaxf(fabsf(a[p][p]), fabsf(a[q][q]));
+                if (thr < FLT_MIN) thr = FLT_MIN;
+                if (!(fabsf(a[p][q]) > thr || fabsf(a[q][p]) > thr)) continue;
+                done = 0;
+                /* block [[w, x], [y, z]] on rows/cols (q, p) */
+                float w = a[q][q], x = a[q][p], y = a[p][q], z = a[p][p];
+                /* left rotation making it symmetric: tan(t) = (y - x) / (w + z) */
+                float c1 = 1.0f, s1 = 0.0f;
+                float num = y - x, den = w + z;
+                if (fabsf(num) > FLT_MIN) {
+                    if (fabsf(den) < FLT_MIN) { c1 = 0.0f; s1 = num > 0.0f ? 1.0f : -1.0f; }
+                    else {
+                        float u = num / den, r = sqrtf(1.0f + u * u);
+                        c1 = 1.0f / r; s1 = u / r;
+                        if (den < 0.0f) { c1 = -c1; s1 = -s1; }
+                    }
+                }
+                /* the symmetric block [[sa, sb], [sb, sd]] = R1 B */
+                float sa = c1 * w + s1 * y, sb = c1 * x + s1 * z, sd = -s1 * x + c1 * z;
+                float c2 = 1.0f, s2 = 0.0f;
+                if (fabsf(sb) > FLT_MIN) {
+                    float zeta = (sd - sa) / (2.0f * sb);
+                    float t = 1.0f / (fabsf(zeta) + sqrtf(1.0f + zeta * zeta));
+                    if (zeta < 0.0f) t = -t;
+                    c2 = 1.0f / sqrtf(1.0f + t * t);
+                    s2 = t * c2;
+                }
+                /* left: L = J^T R1, right: J = [[c2, s2], [-s2, c2]] */
+                float lc = c2 * c1 + s2 * s1, ls = c2 * s1 - s2 * c1;
+                for (int k = 0; k < n; k++) {           /* rows q, p of a <- L */
+                    float aq = a[q][k], ap = a[p][k];
+                    a[q][k] = lc * aq + ls * ap;
+                    a[p][k] = -ls * aq + lc * ap;
+                }
+                for (int k = 0; k < n; k++) {           /* U <- U L^T */
+                    float uq = U[k][q], up = U[k][p];
+                    U[k][q] = lc * uq + ls * up;
+                    U[k][p] = -ls * uq + lc * up;
+                }
+                for (int k = 0; k < n; k++) {           /* cols q, p of a <- a J; V <- V J */
+                    float aq = a[k][q], ap = a[k][p];
+                    a[k][q] = c2 * aq - s2 * ap;
+                    a[k][p] = s2 * aq + c2 * ap;
+                    float vq = V[k][q], vp = V[k][p];
+                    V[k][q] = c2 * vq - s2 * vp;
+                    V[k][p] = s2 * vq + c2 * vp;
+                }
+            }
+        if (done) break;
+    }
+    for (int i = 0; i < n; i++) {
+        s[i] = fabsf(a[i][i]);
+        if (a[i][i] < 0.0f) for (int k = 0; k < n; k++) U[k][i] = -U[k][i];
+    }
+    for (int i = 0; i < n; i++) {                      /* sort descending */
+        int best = i;
+        for (int j = i + 1; j < n; j++) if (s[j] > s[best]) best = j;
+        if (best != i) {
+            float t = s[i]; s[i] = s[best]; s[best] = t;
+            for (int k = 0; k < n; k++) {
+                t = U[k][i]; U[k][i] = U[k][best]; U[k][best] = t;
+                t = V[k][i]; V[k][i] = V[k][best]; V[k][best] = t;
+            }
+        }
+    }
+}
+
+/* Householder QR with column pivoting of the r x c matrix M (r >= c, c <= 18
+ * rows of at most 18): M P = Q R.  Q is r x c (thin), R c x c, perm[j] the
+ * column of M in position j. */
+static void qr_colpiv(int r, int c, float M[18][18], float Q[18][18], float R[6][6], int perm[18])
+{
+    float A[18][18];
+    float vs[18][18];
+    float beta[18];
+    for (int i = 0; i < r; i++) for (int j = 0; j < c; j++) A[i][j] = M[i][j];
+    for (int j = 0; j < c; j++) perm[j] = j;
+    for (int k = 0; k < c; k++) {
+        int best = k;
+        float bn = -1.0f;
+        for (int j = k; j < c; j++) {
+            float s = 0.0f;
+            for (int i = k; i < r; i++) s = s + A[i][j] * A[i][j];
+            if (s > bn) { bn = s; best = j; }
+        }
+        if (best != k) {
+            for (int i = 0; i < r; i++) { float t = A[i][k]; A[i][k] = A[i][best]; A[i][best] = t; }
+            int t = perm[k]; perm[k] = perm[best]; perm[best] = t;
+        }
+        float norm = 0.0f;
+        for (int i = k; i < r; i++) norm = norm + A[i][k] * A[i][k];
+        norm = sqrtf(norm);
+        for (int i = 0; i < r; i++) vs[k][i] = 0.0f;
+        beta[k] = 0.0f;
+        if (norm > 0.0f) {
+            float alpha = A[k][k] > 0.0f ? -norm : norm;
+            float v0 = A[k][k] - alpha;
+            vs[k][k] = 1.0f;
+            for (int i = k + 1; i < r; i++) vs[k][i] = A[i][k] / v0;
+            float vv = 0.0f;
+            for (int i = k; i < r; i++) vv = vv + vs[k][i] * vs[k][i];
+            beta[k] = 2.0f / vv;
+            for (int j = k; j < c; j++) {
+                float d = 0.0f;
+                for (int i = k; i < r; i++) d = d + vs[k][i] * A[i][j];
+                d = d * beta[k];
+                for (int i = k; i < r; i++) A[i][j] = A[i][j] - d * vs[k][i];
+            }
+        }
+    }
+    for (int i = 0; i < c; i++) for (int j = 0; j < c; j++) R[i][j] = j >= i ? A[i][j] : 0.0f;
+    /* Q = H_0 ... H_{c-1} applied to the first c columns of the identity */
+    for (int i = 0; i < r; i++) for (int j = 0; j < c; j++) Q[i][j] = i == j ? 1.0f : 0.0f;
+    for (int k = c - 1; k >= 0; k--) {
+        if (beta[k] == 0.0f) continue;
+        for (int j = 0; j < c; j++) {
+            float d = 0.0f;
+            for (int i = k; i < r; i++) d = d + vs[k][i] * Q[i][j];
+            d = d * beta[k];
+            for (int i = k; i < r; i++) Q[i][j] = Q[i][j] - d * vs[k][i];
+        }
+    }
+}
+
+/* min-norm solution of the m x 6 system A x = b in the Eigen-style solver */
+static void lsq_minnorm_qrsvd(int m, float A[18][6], const float *b, float x[6])
+{
+    float Ua[18][6], Va[6][6], s[6];
+    int n = m < 6 ? m : 6;                             /* the diagonal size */
+    float sq[6][6], Us[6][6], Vs[6][6];
+    if (m == 6) {
+        for (int i = 0; i < 6; i++) for (int j = 0; j < 6; j++) sq[i][j] = A[i][j];
+        jacobi2_svd(6, sq, Us, Vs, s);
+        for (int i = 0; i < 6; i++) for (int j = 0; j < 6; j++) { Ua[i][j] = Us[i][j]; Va[i][j] = Vs[i][j]; }
+    } else if (m > 6) {                                /* A P = Q R, R = Us S Vs^T */
+        float M[18][18], Q[18][18], R[6][6];
+        int perm[18];
+        for (int i = 0; i < m; i++) for (int j = 0; j < 6; j++) M[i][j] = A[i][j];
+        qr_colpiv(m, 6, M, Q, R, perm);
+        jacobi2_svd(6, R, Us, Vs, s);
+        for (int i = 0; i < m; i++)
+            for (int j = 0; j < 6; j++) {
+                float acc = 0.0f;
+                for (int k = 0; k < 6; k++) acc = acc + Q[i][k] * Us[k][j];
+                Ua[i][j] = acc;
+            }
+        for (int j = 0; j < 6; j++) for (int k = 0; k < 6; k++) Va[perm[j]][k] = Vs[j][k];
+    } else {                                           /* A^T P = Q R: A = P R^T Q^T */
+        float M[18][18], Q[18][18], R[6][6], Rt[6][6];
+        int perm[18];
+        for (int i = 0; i < 6; i++) for (int j = 0; j < m; j++) M[i][j] = A[j][i];
+        qr_colpiv(6, m, M, Q, R, perm);
+        for (int i = 0; i < m; i++) for (int j = 0; j < m; j++) Rt[i][j] = R[j][i];
+        jacobi2_svd(m, Rt, Us, Vs, s);                 /* R^T = Us S Vs^T */
+        for (int i = 0; i < m; i++) for (int k = 0; k < m; k++) Ua[perm[i]][k] = Us[i][k];
+        for (int i = 0; i < 6; i++)
+            for (int j = 0; j < m; j++) {
+                float acc = 0.0f;
+                for (int k = 0; k < m; k++) acc = acc + Q[i][k] * Vs[k][j];
+                Va[i][j] = acc;
+            }
+    }
+    float thr = s[0] * ((float)n * FLT_EPSILON);
+    if (thr < FLT_MIN) thr = FLT_MIN;
+    for (int r = 0; r < 6; r++) x[r] = 0.0f;
+    for (int j = 0; j < n; j++) {
+        if (s[j] < thr) break;
+        float ub = 0.0f;
+        for (int i = 0; i < m; i++) ub = ub + Ua[i][j] * b[i];
+        float coef = ub / s[j];
+        for (int r = 0; r < 6; r++) x[r] = x[r] + Va[r][j] * coef;
+    }
+}
+
+/* real parts of the eigenvalues of a general 3x3 matrix: Householder
+ * Hessenberg reduction, then Francis double-shift QR with deflation (the
+ * published real-Schur method), in FP32 */
+static void eig3_general_real(const float Min[3][3], float wr[3])
+{
+    float a[3][3];
+    memcpy(a, Min, sizeof(a));
+    {   /* Hessenberg: zero a[2][0] with a reflection on rows/cols 1, 2 */
+        float x1 = a[1][0], x2 = a[2][0];
+        float nrm = sqrtf(x1 * x1 + x2 * x2);
+        if (x2 != 0.0f && nrm > 0.0f) {
+            float alpha = x1 > 0.0f ? -nrm : nrm;
+            float v1 = x1 - alpha, v2 = x2;
+            float vv = v1 * v1 + v2 * v2, beta = 2.0f / vv;
+            for (int j = 0; j < 3; j++) {               /* H a */
+                float d = beta * (v1 * a[1][j] + v2 * a[2][j]);
+                a[1][j] = a[1][j] - d * v1;
+                a[2][j] = a[2][j] - d * v2;
+            }
+            for (int i = 0; i < 3; i++) {               /* (H a) H */
+                float d = beta * (a[i][1] * v1 + a[i][2] * v2);
+                a[i][1] = a[i][1] - d * v1;
+                a[i][2] = a[i][2] - d * v2;
+            }
+            a[2][0] = 0.0f;
+        }
+    }
+    int hi = 2, iter = 0;
+    float exshift = 0.0f;
+    while (hi >= 0) {
+        /* negligible subdiagonal entry below hi */
+        int lo = hi;
+        while (lo > 0) {
+            float sc = fabsf(a[lo - 1][lo - 1]) + fabsf(a[lo][lo]);
+            if (sc == 0.0f) sc = 1.0f;
+            if (fabsf(a[lo][lo - 1]) <= FLT_EPSILON * sc) { a[lo][lo - 1] = 0.0f; break; }
+            lo--;
+        }
+        if (lo == hi) {                                 /* a 1x1 block */
+            wr[hi] = a[hi][hi] + exshift;
+            hi--;
+            iter = 0;
+        } else if (lo == hi - 1) {                      /* a 2x2 block */
+            float p = 0.5f * (a[hi - 1][hi - 1] - a[hi][hi]);
+            float q = p * p + a[hi][hi - 1] * a[hi - 1][hi];
+            float base = a[hi][hi] + exshift;
+            if (q >= 0.0f) {
+                float z = sqrtf(q);
+                z = p >= 0.0f ? p + z : p - z;
+                wr[hi - 1] = base + z;
+                wr[hi] = z != 0.0f ? base - a[hi][hi - 1] * a[hi - 1][hi] / z : base + z;
+            } else {
+                wr[hi - 1] = wr[hi] = base + p;         /* a complex pair: the common real part */
+            }
+            hi -= 2;
+            iter = 0;
+        } else {                                        /* a 3x3 block: a double-shift step */
+            if (++iter > 60) {                          /* no convergence: take the diagonal */
+                for (int k = lo; k <= hi; k++) wr[k] = a[k][k] + exshift;
+                break;
+            }
+            float x = a[hi][hi], y = a[hi - 1][hi - 1], w = a[hi][hi - 1] * a[hi - 1][hi];
+            if (iter == 10 || iter == 20) {             /* exceptional shift */
+                exshift += x;
+                for (int k = lo; k <= hi; k++) a[k][k] -= x;
+                float sft = fabsf(a[hi][hi - 1]) + fabsf(a[hi - 1][hi - 2 >= 0 ? hi - 2 : 0]);
+                x = y = 0.75f * sft;
+                w = -0.4375f * sft * sft;
+            }
+            /* first column of (H - s1)(H - s2), then bulge chase (n = 3) */
+            float z0 = a[lo][lo];
+            float r = x - z0, s = y - z0;
+            float p = (r * s - w) / a[lo + 1][lo] + a[lo][lo + 1];
+            float q = a[lo + 1][lo + 1] - z0 - r - s;
+            float rr = a[lo + 2][lo + 1];
+            {
+                float xx = fabsf(p) + fabsf(q) + fabsf(rr);
+                if (xx > 0.0f) { p /= xx; q /= xx; rr /= xx; }
+            }
+            /* the bulge of the previous step (left in place below the
+             * subdiagonal, zero by construction) */
+            for (int i = lo + 2; i <= hi; i++) { a[i][i - 2] = 0.0f; if (i != lo + 2) a[i][i - 3] = 0.0f; }
+            for (int k = lo; k <= hi - 1; k++) {
+                float xx = 1.0f;
+                if (k != lo) {
+                    p = a[k][k - 1];
+                    q = a[k + 1][k - 1];
+                    rr = k != hi - 1 ? a[k + 2][k - 1] : 0.0f;
+                    xx = fabsf(p) + fabsf(q) + fabsf(rr);
+                    if (xx == 0.0f) continue;
+                    p /= xx; q /= xx; rr /= xx;
+                }
+                float sgn = sqrtf(p * p + q * q + rr * rr);
+                if (p < 0.0f) sgn = -sgn;
+                if (sgn == 0.0f) continue;
+                if (k != lo) a[k][k - 1] = -sgn * xx;
+                p = p + sgn;
+                float xk = p / sgn, yk = q / sgn, zk = rr / sgn;
+                q = q / p; rr = rr / p;
+                for (int j = k; j <= hi; j++) {         /* rows k, k+1, k+2 */
+                    float t = a[k][j] + q * a[k + 1][j];
+                    if (k != hi - 1) { t = t + rr * a[k + 2][j]; a[k + 2][j] = a[k + 2][j] - t * zk; }
+                    a[k + 1][j] = a[k + 1][j] - t * yk;
+                    a[k][j] = a[k][j] - t * xk;
+                }
+                int mm = k + 3 < hi ? k + 3 : hi;
+                for (int i = lo; i <= mm; i++) {        /* columns k, k+1, k+2 */
+                    float t = xk * a[i][k] + yk * a[i][k + 1];
+                    if (k != hi - 1) { t = t + zk * a[i][k + 2]; a[i][k + 2] = a[i][k + 2] - t * rr; }
+                    a[i][k + 1] = a[i][k + 1] - t * q;
+                    a[i][k] = a[i][k] - t;
+                }
+            }
+        }
+    }
+}
+
+/* test hooks of the second restatement */
+void orc_eig3_real(const float M9[9], float wr[3])
+{
+    float A[3][3];
+    for (int i = 0; i < 9; i++) A[i / 3][i % 3] = M9[i];
+    eig3_general_real(A, wr);
+}
+
+void orc_lsq_qrsvd(int m, const float *A6, const float *b, float x[6])
+{
+    float A[18][6];
+    for (int i = 0; i < m; i++) for (int j = 0; j < 6; j++) A[i][j] = A6[6 * i + j];
+    lsq_minnorm_qrsvd(m, A, b, x);
+}
+
+static int m6_negative_eig(const float M[6])
+{
+    const float A[3][3] = { { M[0], M[1], M[2] }, { M[1], M[3], M[4] }, { M[2], M[4], M[5] } };
+    float wr[3] = { 0.0f, 0.0f, 0.0f };
+    eig3_general_real(A, wr);
+    return (wr[0] < 0.0f || wr[1] < 0.0f || wr[2] < 0.0f) ? 1 : 0;
+}
+
+/* nearest PSD in FP32: cyclic Jacobi eigenvectors, clip, V diag V^T */
+static void m6_nearest_psd_f32(const float M[6], float out[6])
+{
+    float a[3][3] = { { M[0], M[1], M[2] }, { M[1], M[3], M[4] }, { M[2], M[4], M[5] } };
+    float V[3][3] = { { 1, 0, 0 }, { 0, 1, 0 }, { 0, 0, 1 } };
+    static const int P[3] = { 0, 0, 1 }, Q[3] = { 1, 2, 2 };
+    for (int sw = 0; sw < 50; sw++) {
+        int rot = 0;
+        for (int k = 0; k < 3; k++) {
+            int p = P[k], q = Q[k];
+            float apq = a[p][q];
+            if (fabsf(apq) <= FLT_EPSILON * (fabsf(a[p][p]) + fabsf(a[q][q])) || apq == 0.0f) continue;
+            float th = (a[q][q] - a[p][p]) / (2.0f * apq);
+            float t = 1.0f / (fabsf(th) + sqrtf(th * th + 1.0f));
+            if (th < 0.0f) t = -t;
+            float c = 1.0f / sqrtf(t * t + 1.0f), s = t * c;
+            for (int r = 0; r < 3; r++) { float ap = a[r][p], aq = a[r][q]; a[r][p] = c * ap - s * aq; a[r][q] = s * ap + c * aq; }
+            for (int r = 0; r < 3; r++) { float ap = a[p][r], aq = a[q][r]; a[p][r] = c * ap - s * aq; a[q][r] = s * ap + c * aq; }
+            for (int r = 0; r < 3; r++) { float vp = V[r][p], vq = V[r][q]; V[r][p] = c * vp - s * vq; V[r][q] = s * vp + c * vq; }
+            rot++;
+        }
+        if (!rot) break;
+    }
+    float w[3];
+    for (int k = 0; k < 3; k++) w[k] = a[k][k] < 0.0f ? 0.0f : a[k][k];
+    static const int R[6] = { 0, 0, 0, 1, 1, 2 }, C[6] = { 0, 1, 2, 1, 2, 2 };
+    for (int e = 0; e < 6; e++) {
+        int i = R[e], j = C[e];
+        out[e] = (V[i][0] * w[0]) * V[j][0] + (V[i][1] * w[1]) * V[j][1] + (V[i][2] * w[2]) * V[j][2];
+    }
+}
+
 static float round_half_up(float f) { return (float)floor((double)f + 0.5); } /* :901 */
 
 int orc_metric_solve(const float *fwd, const float *bwd, int W, int H, int D, float sx, float sy,
@@ -514,9 +905,10 @@ int orc_metric_solve(const float *fwd, const float *bwd, int W, int H, int D, fl
         }
     float x[6];
     if (m == 0) { for (int k = 0; k < 6; k++) x[k] = 0.0f; }
+    else if (g_solver & 1) lsq_minnorm_qrsvd(m, A, b, x);
     else lsq_minnorm(m, A, b, x);
     for (int k = 0; k < 6; k++) M[k] = x[k];
-    return m6_negative(M);
+    return (g_solver & 2) ? m6_negative_eig(M) : m6_negative(M);
 }
 
 /* flow-angle filter of the plain reseed (Image.cpp:1406-1409); flow of the
@@ -572,7 +964,8 @@ void orc_seed_metrics(const float *fwd, const float *bwd, int W, int H, int D, i
             if (n > 0) {
                 for (int e = 0; e < 6; e++) M6[6 * i + e] = sum[e] / (float)n;
             } else {
-                m6_nearest_psd(self, M6 + 6 * i);
+                if (g_solver & 4) m6_nearest_psd_f32(self, M6 + 6 * i);
+                else m6_nearest_psd(self, M6 + 6 * i);
                 k = 3;
             }
         }

@@ -60,6 +60,13 @@ void orc_grid_cell_tables(int W, int H, int D, const float *grid4, const orc_gri
                           int *xcell, int *ycell, int *zcell);
 int  orc_density_adjust(const uint8_t *rgb, int W, int H, int D, const float *grid4,
                         const orc_grid_info *g, float *seeds4_out, float *density_out);
+/* 0: the primary solver (the CUDA path's twin); 1: the FP32 restatement of
+ * the algorithms of the reference's Eigen calls (QR-preconditioned two-sided
+ * Jacobi SVD, Hessenberg + Francis QR eigenvalues), for measuring how much
+ * the labels depend on the solver.  Process-wide. */
+void orc_set_solver(int mode);
+void orc_eig3_real(const float M9[9], float wr[3]);                       /* test hooks of mode 1 */
+void orc_lsq_qrsvd(int m, const float *A6, const float *b, float x[6]);
 int  orc_m6_negative(const float M[6]);   /* exact "an eigenvalue < 0" of (M00,M01,M02,M11,M12,M22) */
 int  orc_metric_solve(const float *fwd, const float *bwd, int W, int H, int D,
                       float sx, float sy, int frame, float M[6]);

@@ -123,6 +123,12 @@ def _p(a):
     return a.ctypes.data_as(c_void_p) if a is not None else None
 
 
+def set_solver(mode):
+    """0: the primary metric solver (the CUDA path's twin); 1: the FP32
+    restatement of the algorithms of the reference's Eigen calls."""
+    load().orc_set_solver(int(mode))
+
+
 def grid_seeds(W, H, D, K, middlebury=0):
     lib = load()
     g = GridInfo()
