@@ -92,6 +92,51 @@ int asv_render_rgb(const int32_t *labels, int W, int H, int D, int n_labels, uin
 int asv_write_render_png(const char *prefix, const int32_t *labels, int W, int H, int D,
                          int n_labels, int start_index);
 
+/* ---- the reference's host programs ------------------------------------ */
+
+/* Options of asv_render_run / asv_render_stream_run. */
+typedef struct asv_render_options {
+    int lloyd_iters;    /* 0: 20, the reference's Lloyd_max_iter (GPU-AS/Render.cpp:11) */
+    int write_txt;      /* the label txt file (the reference's output_label) */
+    int write_render;   /* the pseudo-colour frames as PNG files */
+    int connectivity;   /* plain form: post-processing 6.2, 3D connectivity enforcement
+                           (GPU-AS/Render.cpp:323-341), instead of 6.1 */
+    int device;         /* CUDA device ordinal */
+    int verbose;        /* progress lines on stdout, as the reference's cout */
+} asv_render_options;
+
+/* defaults: 20 iterations, txt and renders written, 6.1 post-processing,
+ * device 0, quiet */
+void asv_render_options_default(asv_render_options *opt);
+
+#define ASV_RENDER_ERR_ARG (-1)     /* NULL argument or seeds_num < 1 */
+#define ASV_RENDER_ERR_IO (-2)      /* no frames, unreadable folder, unwritable output */
+#define ASV_RENDER_ERR_DECODE (-3)  /* a frame is not a readable PNG file */
+#define ASV_RENDER_ERR_SIZE (-4)    /* frames of different sizes */
+#define ASV_RENDER_ERR_GPU (-5)     /* a C ABI call failed (message on stderr) */
+
+/* Render::run of the plain program (GPU-AS/Render.cpp:100-350, called by
+ * GPU-AS/main.cpp:49-86 with the same arguments): the sorted frames of
+ * <dataset_path>/<vdname> (PNG), preprocessing and optical flow on the
+ * device, seeds (K = seeds_num), metric, LAB, the Lloyd loop and
+ * check_dead_seeds; writes <save_path><dbname>/AS/<vdname>/<seeds_num>.txt
+ * (print_sv_txt) and <seeds_num>_NNNNN.png pseudo-colour frames
+ * (print_render, numbered from 1).  compactness is accepted and, as in the
+ * reference (Image::init_variables, GPU-AS/Image.cpp:1050), 8 is used.
+ * opt NULL: asv_render_options_default.  Returns 0 or ASV_RENDER_ERR_*. */
+int asv_render_run(const char *dataset_path, const char *save_path, const char *dbname, const char *vdname,
+                   int seeds_num, float compactness, const asv_render_options *opt);
+
+/* Render::run of the streaming program (streamGPU-AS/Render.cpp:100-303):
+ * seeds_num over the whole video (seeds_num_100 = seeds_num * 100 / frames),
+ * blocks of 30 frames overlapping by 10, each block's flow computed on the
+ * device; writes the video-wide labels as <seeds_num>.txt
+ * (output_label_all, :741-764) and <seeds_num>_NNNNN.png
+ * (output_render_all, :766-826) in the same folder layout.  Compactness 6
+ * (streamGPU-AS/Image.cpp:968). */
+int asv_render_stream_run(const char *dataset_path, const char *save_path, const char *dbname,
+                          const char *vdname, int seeds_num, float compactness, const asv_render_options *opt);
+
 #ifdef __cplusplus
 }
 #endif
