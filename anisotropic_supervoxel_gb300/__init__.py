@@ -6,5 +6,5 @@ in the CUDA kernels of csrc/.
 """
 from ._lib import AsvError, load  # noqa: F401
 from .image import (Batch, Image, Server, Stream, config, list_frames, png_info, preprocess_frame,  # noqa: F401
-                    read_frames, read_png, render_rgb, synth_clip, synth_truth, write_labels_txt, write_png,
+                    read_frames, read_png, render_rgb, render_run, synth_clip, synth_truth, write_labels_txt, write_png,
                     write_render_png, write_render_ppm)

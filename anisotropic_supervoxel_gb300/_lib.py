@@ -78,6 +78,11 @@ class SynthParams(ctypes.Structure):
 
 
 # name -> (restype, argtypes); every function declared in include/asv*.h
+class RenderOptions(ctypes.Structure):
+    _fields_ = [(n, c_int) for n in ("lloyd_iters", "write_txt", "write_render", "connectivity", "device",
+                                     "verbose")]
+
+
 SIGNATURES = {
     "asv_config_default": (None, [P(Config)]),
     "asv_create": (c_int, [P(Config), P(c_void_p)]),
@@ -149,6 +154,9 @@ SIGNATURES = {
     "asv_png_write_rgb": (c_int, [c_char_p, c_void_p, c_int, c_int]),
     "asv_render_rgb": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_void_p]),
     "asv_write_render_png": (c_int, [c_char_p, c_void_p, c_int, c_int, c_int, c_int, c_int]),
+    "asv_render_options_default": (None, [P(RenderOptions)]),
+    "asv_render_run": (c_int, [c_char_p, c_char_p, c_char_p, c_char_p, c_int, c_float, P(RenderOptions)]),
+    "asv_render_stream_run": (c_int, [c_char_p, c_char_p, c_char_p, c_char_p, c_int, c_float, P(RenderOptions)]),
 }
 
 _LIB = None

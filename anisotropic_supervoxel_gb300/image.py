@@ -536,3 +536,19 @@ def preprocess_frame(bgr):
     if _lib.load().asv_preprocess_frame(_ptr(bgr), W, H, _ptr(out)) != 0:
         raise ValueError("bad frame")
     return out
+
+
+def render_run(dataset_path, save_path, dbname, vdname, seeds_num, compactness=8.0, stream=False, **opts):
+    """Render::run of the plain (or, stream=True, the streaming) program:
+    <dataset_path>/<vdname> PNG frames in, <save_path><dbname>/AS/<vdname>/
+    <seeds_num>.txt and <seeds_num>_NNNNN.png out (asv_render_run /
+    asv_render_stream_run).  opts: lloyd_iters, write_txt, write_render,
+    connectivity, device, verbose.  Returns the library's code (0 = done)."""
+    lib = _lib.load()
+    o = _lib.RenderOptions()
+    lib.asv_render_options_default(ctypes.byref(o))
+    for k, v in opts.items():
+        setattr(o, k, int(v))
+    fn = lib.asv_render_stream_run if stream else lib.asv_render_run
+    return fn(os.fsencode(dataset_path), os.fsencode(save_path), dbname.encode(), vdname.encode(), int(seeds_num),
+              float(compactness), ctypes.byref(o))
