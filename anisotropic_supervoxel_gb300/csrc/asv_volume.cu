@@ -927,27 +927,31 @@ __device__ __forceinline__ void asv_jfa_tile(const int32_t *__restrict__ in, int
     const int lx = threadIdx.x % ASV_TILE_X, ly = threadIdx.x / ASV_TILE_X;
     const int gx = tx0 + lx, gy = ty0 + ly;
     const bool valid = gx < W && gy < H;                       // block-uniform loop: every lane runs the tile
-    auto list_run = [&](int q0, int nq) {
-        asv_jfa_run<SUMS>(in, out, lab, tab, sums, slot0, W, H, D, Kp, min(gx, W - 1), min(gy, H - 1), q0, nq,
-                          step, ratio, (asv_list_t *)smem + threadIdx.x, valid);
-        __syncthreads();                                       // the list rows alias the footprint
-    };
-    if (step <= ASV_BITS_MAXS && Kp <= ASV_BITS_MAXKP) {
+    // sub-tiles the bit-set form leaves (a bit per sub-tile of `sub` positions)
+    // go through one inlined copy of the list form
+    unsigned fail = 1u;
+    int sub = n;
+    if (step <= ASV_BITS_MAXS && Kp <= ASV_BITS_MAXKP && n <= 32 * 4) {   // <= 32 sub-tiles of >= 4
+        fail = 0u;
 #define ASV_BITS_CASE(S_)                                                                                    \
     case S_:                                                                                                 \
-        for (int q0 = 0; q0 < n; q0 += AsvBitsGeo<S_>::SUB) {                                                \
-            const int nq = min(AsvBitsGeo<S_>::SUB, n - q0);                                                 \
-            if (!asv_jfa_bits_sub<S_, SUMS>(in, out, lab, tab, sums, slot0, W, H, D, Kp, tx0, ty0, p0 + q0,  \
-                                            nq, ratio, smem))                                                \
-                list_run(p0 + q0, nq);                                                                       \
-        }                                                                                                    \
-        return;
+        sub = AsvBitsGeo<S_>::SUB;                                                                           \
+        for (int q0 = 0; q0 < n; q0 += AsvBitsGeo<S_>::SUB)                                                  \
+            if (!asv_jfa_bits_sub<S_, SUMS>(in, out, lab, tab, sums, slot0, W, H, D, Kp, tx0, ty0, p0 + q0, \
+                                            min(AsvBitsGeo<S_>::SUB, n - q0), ratio, smem))                  \
+                fail |= 1u << (q0 / AsvBitsGeo<S_>::SUB);                                                  \
+        break;
         switch (step) {
             ASV_BITS_CASE(1) ASV_BITS_CASE(2) ASV_BITS_CASE(3) ASV_BITS_CASE(4) ASV_BITS_CASE(5) ASV_BITS_CASE(6)
         }
 #undef ASV_BITS_CASE
     }
-    list_run(p0, n);
+    for (int i = 0; fail; i++, fail >>= 1) {
+        if (!(fail & 1u)) continue;
+        asv_jfa_run<SUMS>(in, out, lab, tab, sums, slot0, W, H, D, Kp, min(gx, W - 1), min(gy, H - 1), p0 + i * sub,
+                          min(sub, n - i * sub), step, ratio, (asv_list_t *)smem + threadIdx.x, valid);
+        __syncthreads();                                       // the list rows alias the footprint
+    }
 }
 
 __device__ __forceinline__ void asv_jfa_smem_init(unsigned char *smem)
