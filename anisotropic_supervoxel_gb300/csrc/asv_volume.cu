@@ -418,8 +418,8 @@ __global__ void k_draw(AsvDev d)
     // IEEE arithmetic, and doubling is exact, so
     // (dx*dy)*(2*M01) == ((2*dx)*dy)*M01 (flood.gs:85).
     d.jtab[3 * g + 0] = make_float4(-p.x, -p.y, -p.z, -c.x);
-    d.jtab[3 * g + 1] = make_float4(m[0], m[3], 2.0f * m[1], 2.0f * m[4]);
-    d.jtab[3 * g + 2] = make_float4(2.0f * m[2], m[5], -c.y, -c.z);
+    d.jtab[3 * g + 1] = make_float4(m[0], m[3], 2.0f * m[2], 2.0f * m[4]);
+    d.jtab[3 * g + 2] = make_float4(2.0f * m[1], m[5], -c.y, -c.z);
     if (!(p.x >= 0.0f && p.y >= 0.0f && p.z >= 0.0f)) return;
     int x = (int)p.x, y = (int)p.y, z = (int)p.z;
     if (x >= S.W || y >= S.H || z >= S.D) return;
@@ -512,16 +512,19 @@ __device__ __forceinline__ int asv_merge_lists(const asv_list_t *__restrict__ A,
 }
 
 // flood.gs:72-94: anisotropic distance of the voxel centre to seed l of the
-// table, in the shader's operation order.  The voxel side comes packed as
-// vxy = (x, y), vzl = (z, L), vab = (a, b); the table holds the seed's
-// negated position and colour, so the six differences are three two-wide
-// FP32 additions (__fadd2_rn: each half rounds like the scalar addition, and
-// v + (-s) is v - s).  Only these additions are paired: their operands are
-// loads, never products, so nothing can be fused into them.  Products and
-// the sums they feed stay scalar (kept apart by -fmad=false): a two-wide
-// product feeding a two-wide sum is fused into a two-wide FMA by the
-// assembler even when both are written with explicit .rn rounding, which
-// changes the result.
+// table, in the shader's operation order: every product and sum of the
+// shader on the same operands, each rounded once.  The voxel side comes
+// packed as vxy = (x, y), vzl = (z, L), vab = (a, b); the table rows are
+// (-x, -y, -z, -L), (M00, M11, 2 M02, 2 M12), (2 M01, M22, -a, -b), so the
+// six differences are three two-wide additions (__fadd2_rn: each half
+// rounds like the scalar addition, and v + (-s) is v - s) and the products
+// pair up two-wide where both operands lie side by side: (dx dx, dy dy),
+// (dz dz, eL eL), (ea ea, eb eb), (dx dz, dy dz), then those times
+// (M00, M11) and (2 M02, 2 M12).  Every sum stays a scalar addition with
+// explicit round-to-nearest (-fmad=false), which the PTX ISA keeps apart
+// from the products; a two-wide product feeding a two-wide sum was seen
+// fused into a two-wide FMA, so no sum is two-wide.  The bit-exact tests
+// against the oracle (millions of distances per run) guard both.
 __device__ __forceinline__ float asv_jfa_dist_v(const float4 t0, const float4 t1, const float4 t2, float2 vxy,
                                                 float2 vzl, float2 vab, float ratio)
 {
@@ -529,13 +532,19 @@ __device__ __forceinline__ float asv_jfa_dist_v(const float4 t0, const float4 t1
     const float2 dzl = __fadd2_rn(vzl, make_float2(t0.z, t0.w));              // (dz, eL)
     const float2 eab = __fadd2_rn(vab, make_float2(t2.z, t2.w));              // (ea, eb)
     const float dx = dxy.x, dy = dxy.y, dz = dzl.x;
-    float p1 = (dx * dx) * t1.x + (dx * dy) * t1.z;                            // flood.gs:85
-    p1 = p1 + (dx * dz) * t2.x;
-    float p2 = (dy * dy) * t1.y + (dy * dz) * t1.w;
-    p2 = p2 + (dz * dz) * t2.y;
+    const float2 sq = __fmul2_rn(dxy, dxy);
+    const float2 zl = __fmul2_rn(dzl, dzl);
+    const float2 ab = __fmul2_rn(eab, eab);
+    const float2 cz = __fmul2_rn(dxy, make_float2(dz, dz));
+    const float2 wa = __fmul2_rn(sq, make_float2(t1.x, t1.y));
+    const float2 wc = __fmul2_rn(cz, make_float2(t1.z, t1.w));
+    float p1 = wa.x + (dx * dy) * t2.x;
+    p1 = p1 + wc.x;
+    float p2 = wa.y + wc.y;
+    p2 = p2 + zl.x * t2.y;
     float pos = p1 + p2;
-    float col = dzl.y * dzl.y + eab.x * eab.x;                                 // flood.gs:89
-    col = col + eab.y * eab.y;
+    float col = zl.y + ab.x;
+    col = col + ab.y;
     pos = (pos < 0.0f) ? 0.0f : pos;                                           // flood.gs:90-93
     return ratio * pos + col;                                                  // flood.gs:94
 }
