@@ -45,8 +45,6 @@ TRAFFIC = os.path.join(ROOT, "profiles", "k_jfa_320x240x85.md")
 TRAFFIC_720P = os.path.join(ROOT, "profiles", "k_jfa_1280x720x30.md")
 # algorithmic bytes per voxel of one JFA pass: label in 4 + label out 4 + LAB 3
 JFA_BYTES_PER_VOXEL = 11
-# nominal FP32 work per voxel of one JFA pass: 27 candidates x 33 operations
-JFA_FLOP_PER_VOXEL = 27 * 33
 
 
 def parse():
@@ -366,7 +364,6 @@ def run_ours(args):
                          "launch_ms": jfa_launch_s * 1e3,
                          "traffic": tpv * nvox if tpv is not None else None,
                          "issue_active_ncu": profile_value("issue_active"),
-                         "fp32_nominal_tflops": JFA_FLOP_PER_VOXEL * nvox / jfa_launch_s / 1e12,
                          "jfa_share_of_loop": jfa_ms / loop_ms if loop_ms else None},
             "clocks": clk,
             "gpu_launches": int(launches * args.steps),
