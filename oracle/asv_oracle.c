@@ -1392,6 +1392,29 @@ int orc_run_clip(const orc_params *p, const uint8_t *rgb, const float *fwd, cons
  * Streaming form: streamGPU-AS/Render.cpp:156-569.
  * info_out = {blocks, seeds_num_placed}.
  * ==================================================================== */
+/* post_and_next's kept seeds (streamGPU-AS/Render.cpp:519-540): the final
+ * centroids (x, y, z, id) of a block with z > block_size - block_size/3, z
+ * shifted back by the block's new frames (1.5 when it would fall below 1);
+ * returns how many, written to kept (4 floats each). */
+int orc_stream_keep(const float *info, int n, int bs, float *kept)
+{
+    const int one_third = bs / 3, two_third = bs - one_third;
+    int k = 0;
+    for (int i = 0; i < n; i++) {
+        float z = info[4 * i + 2];
+        if (z > (float)(bs - one_third)) {
+            float nz = z - (float)two_third;
+            if (nz < 1) nz = 1.5f;
+            kept[4 * k + 0] = info[4 * i + 0];
+            kept[4 * k + 1] = info[4 * i + 1];
+            kept[4 * k + 2] = nz;
+            kept[4 * k + 3] = info[4 * i + 3];
+            k++;
+        }
+    }
+    return k;
+}
+
 int orc_stream_blocks(int D_all, int block_size, int *intervals, int cap)
 {
     int one_third = block_size / 3, two_third = 2 * block_size / 3;     /* :200-201 */
@@ -1471,18 +1494,7 @@ int orc_run_stream(const orc_stream_params *p, const uint8_t *rgb, const float *
         free(kept); kept = NULL; kept_num = 0;
         if (b < nb - 1) {                                                 /* :519-557 */
             kept = malloc(sizeof(float) * 4 * (nal > 0 ? nal : 1));
-            for (int i = 0; i < nal; i++) {
-                float z = info[4 * i + 2];
-                if (z > (float)(bs - one_third)) {
-                    float nz = z - (float)two_third;
-                    if (nz < 1) nz = 1.5f;
-                    kept[4 * kept_num + 0] = info[4 * i + 0];
-                    kept[4 * kept_num + 1] = info[4 * i + 1];
-                    kept[4 * kept_num + 2] = nz;
-                    kept[4 * kept_num + 3] = info[4 * i + 3];
-                    kept_num++;
-                }
-            }
+            kept_num = orc_stream_keep(info, nal, bs, kept);
             done_frames = Db - one_third;
         }
         long done = slice * done_frames;                                  /* :559-563 */

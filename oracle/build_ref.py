@@ -529,6 +529,38 @@ extern "C" void ref_sequence_label(int *labels, long n, const long long *counts,
 """
 
 
+# Host code that lies inside a longer function of the reference: the text
+# between two markers is cut out and placed in a wrapper of this project's
+# (the shim supplies the surrounding function's locals and members).
+SNIPPETS = [
+    # the block partition of the streaming Render::run (streamGPU-AS/Render.cpp:199-241)
+    ("streamGPU-AS/Render.cpp", "int Render::run(", "block_size = 30;", "block_num = block_interval.size() / 2;",
+     "struct StreamBlocksShim {\n    int block_size, block_num, depth_all; ostringstream cout;\n"
+     "    int run(int D, int *out, int cap) {\n        depth_all = D;\n@SNIPPET@\n"
+     "        for (int i = 0; i < (int)block_interval.size() && i < cap; i++) out[i] = block_interval[i];\n"
+     "        return block_num;\n    }\n};\n"
+     "extern \"C\" int ref_stream_blocks(int D, int *out, int cap) { StreamBlocksShim s; return s.run(D, out, cap); }\n"),
+    # the kept seeds of post_and_next (streamGPU-AS/Render.cpp:519-540)
+    ("streamGPU-AS/Render.cpp", "void Render::post_and_next(", "int sind = 0;", "sind += 4;",
+     "struct KeepShim {\n    int block_size, kept_seeds_num; vector<float> kept_seeds; ostringstream cout;\n"
+     "    int run(const float *info, int n, int bs, float *out) {\n        block_size = bs;\n"
+     "        vector<float> seeds_info(info, info + 4 * n);\n        int final_seeds_num = n;\n"
+     "        int one_third = int(block_size / 3);\n        int two_third = block_size - one_third;\n"
+     "@SNIPPET@\n        }\n"
+     "        for (int i = 0; i < (int)kept_seeds.size(); i++) out[i] = kept_seeds[i];\n"
+     "        return kept_seeds_num;\n    }\n};\n"
+     "extern \"C\" int ref_stream_keep(const float *info, int n, int bs, float *out)"
+     " { KeepShim s; return s.run(info, n, bs, out); }\n"),
+]
+
+
+def _snippet(text, fn_start, start, stop):
+    fn = _cut_function(text, fn_start)
+    i = fn.index(start)
+    j = fn.index(stop, i) + len(stop)
+    return fn[i:j]
+
+
 def _strip_comments(src):
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
     return re.sub(r"//[^\n]*", "", src)
@@ -577,6 +609,9 @@ def build_host(force=False):
             fn = text[i:text.index(stop, i)] + "}"
         fn = re.sub(r"\b\w+::(\w+\s*\()", r"\1", fn, count=1)
         parts.append(f"struct {shim} {{\n    {members}\n{fn}\n}};\n")
+    for path, fn_start, start, stop, wrapper in SNIPPETS:
+        text = _strip_comments(open(os.path.join(REF, path), encoding="latin-1").read())
+        parts.append(wrapper.replace("@SNIPPET@", _snippet(text, fn_start, start, stop)))
     parts.append(HOST_WRAPPERS)
     cpp = os.path.join(OUT, "ref_host.cpp")
     with open(cpp, "w", encoding="latin-1") as fh:

@@ -166,7 +166,32 @@ def main():
     np.savez_compressed(os.path.join(HERE, "flood_ladder.npz"), s=np.int32(pin.LADDER_S), count=count,
                         ratio=ratio, steps=steps, ratios=ratios)
     labels_txt(host)
+    stream_scheduler(host)
     print("fixtures written to", HERE)
+
+
+def stream_scheduler(host):
+    """the streaming program's block partition and kept seeds
+    (streamGPU-AS/Render.cpp:199-241, :519-540): stream_scheduler.npz"""
+    V = ctypes.c_void_p
+    host.ref_stream_blocks.argtypes = [ctypes.c_int, V, ctypes.c_int]
+    host.ref_stream_keep.argtypes = [V, ctypes.c_int, ctypes.c_int, V]
+    Ds = np.array(list(range(2, 200)) + [899, 900, 901], np.int32)
+    iv = np.zeros((Ds.size, 512), np.int32)
+    nb = np.zeros(Ds.size, np.int32)
+    for i, D in enumerate(Ds):
+        nb[i] = host.ref_stream_blocks(int(D), iv[i].ctypes.data_as(V), 512)
+    rng = np.random.default_rng(20240612)
+    info = np.zeros((2000, 4), np.float32)
+    info[:, 0] = rng.integers(0, 1280, 2000) + 0.5
+    info[:, 1] = rng.integers(0, 720, 2000) + 0.5
+    info[:, 2] = rng.integers(0, 30, 2000) + 0.5
+    info[::5, 2] = 20.0
+    info[:, 3] = np.arange(2000)
+    kept = np.zeros((2000, 4), np.float32)
+    nk = host.ref_stream_keep(info.ctypes.data_as(V), 2000, 30, kept.ctypes.data_as(V))
+    np.savez_compressed(os.path.join(HERE, "stream_scheduler.npz"), D=Ds, blocks=nb, intervals=iv, info=info,
+                        kept=kept[:nk])
 
 
 def labels_txt(host):

@@ -178,3 +178,22 @@ def test_labels_txt(asv, tmp_path):
         assert open(p, "rb").read() == f[f"txt_{n}"].tobytes()
         n += 1
     assert n == 4
+
+
+def test_oracle_stream_scheduler(orc):
+    """the oracle's block partition and kept seeds against the reference's
+    compiled streaming Render.cpp"""
+    import ctypes
+    f = load("stream_scheduler.npz")
+    lib = orc.load()
+    V = ctypes.c_void_p
+    lib.orc_stream_blocks.argtypes = [ctypes.c_int, ctypes.c_int, V, ctypes.c_int]
+    lib.orc_stream_keep.argtypes = [V, ctypes.c_int, ctypes.c_int, V]
+    for i, D in enumerate(f["D"]):
+        iv = np.zeros(512, np.int32)
+        n = lib.orc_stream_blocks(int(D), 30, iv.ctypes.data_as(V), 512)
+        assert n == f["blocks"][i] and np.array_equal(iv[:2 * n], f["intervals"][i, :2 * n]), D
+    info = np.ascontiguousarray(f["info"])
+    kept = np.zeros_like(info)
+    k = lib.orc_stream_keep(info.ctypes.data_as(V), info.shape[0], 30, kept.ctypes.data_as(V))
+    assert k == f["kept"].shape[0] and np.array_equal(kept[:k], f["kept"])

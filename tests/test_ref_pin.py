@@ -441,3 +441,33 @@ def test_labels_txt_matches_reference(ref_host, asv, tmp_path):
         ours = str(tmp_path / f"ours{k}.txt")
         asv.write_labels_txt(ours, lab)
         assert open(ours, "rb").read() == open(stem + ".txt", "rb").read()
+
+
+def test_stream_scheduler_matches_reference(ref_host, orc):
+    """The streaming program's block partition (streamGPU-AS/Render.cpp:
+    199-241) and post_and_next's kept seeds (:519-540), both compiled from the
+    reference tree, against the restatement the streaming oracle runs."""
+    lib = orc.load()
+    V = ctypes.c_void_p
+    ref_host.ref_stream_blocks.argtypes = [ctypes.c_int, V, ctypes.c_int]
+    ref_host.ref_stream_keep.argtypes = [V, ctypes.c_int, ctypes.c_int, V]
+    lib.orc_stream_blocks.argtypes = [ctypes.c_int, ctypes.c_int, V, ctypes.c_int]
+    lib.orc_stream_keep.argtypes = [V, ctypes.c_int, ctypes.c_int, V]
+    for D in list(range(2, 400)) + [899, 900, 901, 1777]:
+        a, b = np.zeros(512, np.int32), np.zeros(512, np.int32)
+        na = ref_host.ref_stream_blocks(D, P(a), 512)
+        nb = lib.orc_stream_blocks(D, 30, P(b), 512)
+        assert na == nb and np.array_equal(a[:2 * na], b[:2 * nb]), D
+    rng = np.random.default_rng(37)
+    for bs in (30, 42, 12):
+        for n in (0, 1, 7, 500, 3000):
+            info = np.zeros((max(n, 1), 4), np.float32)
+            info[:, 0] = rng.integers(0, 1280, info.shape[0]) + 0.5
+            info[:, 1] = rng.integers(0, 720, info.shape[0]) + 0.5
+            info[:, 2] = rng.integers(0, bs, info.shape[0]) + 0.5
+            info[::5, 2] = bs - bs // 3 + np.float32(0.0)             # exactly on the threshold
+            info[:, 3] = np.arange(info.shape[0])
+            ka, kb = np.zeros((max(n, 1), 4), np.float32), np.zeros((max(n, 1), 4), np.float32)
+            ma = ref_host.ref_stream_keep(P(info), n, bs, P(ka))
+            mb = lib.orc_stream_keep(P(info), n, bs, P(kb))
+            assert ma == mb and np.array_equal(ka[:ma], kb[:mb]), (bs, n)
