@@ -670,20 +670,20 @@ __device__ __forceinline__ void asv_jfa_run(const int32_t *__restrict__ in, int3
 // among its 27 candidates, except when two of them tie at the least
 // distance (then the first in the shader's candidate order wins): the
 // distance is a function of the voxel and the label's seed alone.  A
-// sub-tile (16 x 16 columns x up to 8 chain positions of the tile) holds few
-// distinct labels in its whole footprint (the sub-tile grown by `step` on
-// every side; on the benchmarked clips mostly under 32).  So the block
+// sub-tile (16 x 16 columns x up to 16 chain positions of the tile) holds
+// few distinct labels in its whole footprint (the sub-tile grown by `step`
+// on every side; on the benchmarked clips mostly under 32).  So the block
 // copies the footprint and the sub-tile's LAB values into shared memory
 // with asynchronous copies (one memory latency per sub-tile), numbers the
 // footprint's distinct labels 0..T-1 (T <= 32, else the sub-tile takes the
-// list form), and gives every footprint row, per tile column x, the 32-bit
-// mask of the labels at x - step, x, x + step (one bit per label).  A
-// voxel's candidate mask is the OR of three such row masks in each of its
-// three slices; the voxel evaluates the labels of its mask in any order and
-// keeps the least distance below 1e8.  An exact tie at the least distance
-// between two labels (about 30 per million voxel-passes on the benchmarked
-// clips) sends the voxel through the shader's ordered scan of its 27
-// candidates instead, so every label equals the shader's.
+// list form) and turns every footprint entry into its label's bit.  A
+// voxel's candidate mask is the OR of the 9 bits of each of its three
+// slices (the plus slice's mask becomes the next position's centre mask);
+// the voxel evaluates the labels of its mask in any order and keeps the
+// least distance below 1e8.  An exact tie at the least distance between two
+// labels (about 30 per million voxel-passes on the benchmarked clips) sends
+// the voxel through the shader's ordered scan of its 27 candidates instead,
+// so every label equals the shader's.
 //
 // Footprint slices ("slots") of a sub-tile of n chain positions: slot 0 the
 // minus slice of position 0, slots 1..n the centre slices, slot n+1 the plus
@@ -699,14 +699,14 @@ __device__ __forceinline__ void asv_jfa_run(const int32_t *__restrict__ in, int3
 #define ASV_BITS_MAXKP 8192      // segment seed counts up to this use the bit-set form
 #define ASV_BITS_TLCAP 256       // claimed labels remembered for the reset
 #define ASV_BITS_NONE 255        // table number of no label
-#define ASV_BITS_AREA 48320      // shared bytes of the largest sub-tile (step 3)
+#define ASV_BITS_AREA 48384      // shared bytes of the largest sub-tile (step 2, 16 positions)
 #define ASV_JFA_AREA (ASV_BITS_AREA > ASV_JFA_LIST_BYTES ? ASV_BITS_AREA : ASV_JFA_LIST_BYTES)
 
 struct AsvBitsShared {
     float4 tdat[3 * ASV_BITS_MAXT];             // the table's seed rows (as jtab)
     unsigned claim[ASV_BITS_MAXKP / 32];        // labels numbered in this sub-tile (all zero between)
     int tlab[ASV_BITS_TLCAP];                   // label of each number
-    int slotz[16];                              // slice of each footprint slot
+    int slotz[20];                              // slice of each footprint slot
     int tcount;
     unsigned char map8[ASV_BITS_MAXKP];         // number of each claimed label
 };
@@ -715,15 +715,12 @@ struct AsvBitsShared {
 template <int S> struct AsvBitsGeo {
     static constexpr int FW = ASV_TILE_X + 2 * S;                     // footprint width and height
     static constexpr int FP = FW * FW;                                // footprint entries per slot
-    static constexpr int SUB = S <= 3 ? 8 : 4;                        // chain positions per sub-tile
+    // chain positions per sub-tile: deep where the footprint stays small
+    static constexpr int SUB = S <= 2 ? 16 : (S <= 4 ? 8 : 4);
     static constexpr int NSLOT = SUB + 4;
     static constexpr int NCOL = (FP + ASV_JFA_THREADS - 1) / ASV_JFA_THREADS;
-    static constexpr int HXN = FW * ASV_TILE_X;                       // row masks per slot
-    static constexpr int NHX = (HXN + ASV_JFA_THREADS - 1) / ASV_JFA_THREADS;
     static constexpr int FLAB_BYTES = NSLOT * FP * 4;
-    static constexpr int HX_BYTES = NSLOT * HXN * 4;
-    static_assert(FLAB_BYTES + HX_BYTES + SUB * ASV_JFA_THREADS * 4 <= ASV_BITS_AREA,
-                  "bit-set sub-tile exceeds the shared area");
+    static_assert(FLAB_BYTES + SUB * ASV_JFA_THREADS * 4 <= ASV_BITS_AREA, "bit-set sub-tile exceeds the shared area");
 };
 
 // 4-byte asynchronous copy global -> shared (cp.async, completed by
@@ -738,29 +735,24 @@ __device__ __forceinline__ void asv_cp_async_wait()
     asm volatile("cp.async.commit_group;\ncp.async.wait_all;\n" ::: "memory");
 }
 
-// table number of a footprint label (labels outside [0, Kp) are none)
-__device__ __forceinline__ int asv_bits_num(const AsvBitsShared &b, int l, int Kp)
-{
-    return (unsigned)l < (unsigned)Kp ? b.map8[l] : ASV_BITS_NONE;
-}
-
 // The shader's ordered scan of the 27 candidates (slices centre, minus,
-// plus; rows y-S, y, y+S; columns x-S, x, x+S) over the footprint labels,
-// strict '<' from 1e8 (flood.gs:63, :95-99): the tie-break path.
+// plus; rows y-S, y, y+S; columns x-S, x, x+S) over the footprint's label
+// bits, strict '<' from 1e8 (flood.gs:63, :95-99): the tie-break path.
 template <int S>
-__device__ __noinline__ int asv_bits_ordered(const int *__restrict__ fc, const int *__restrict__ fm,
-                                             const int *__restrict__ fp, const AsvBitsShared &b, int Kp,
+__device__ __noinline__ int asv_bits_ordered(const unsigned *__restrict__ fc, const unsigned *__restrict__ fm,
+                                             const unsigned *__restrict__ fp, const AsvBitsShared &b,
                                              float2 vxy, float2 vzl, float2 vab, float ratio)
 {
     constexpr int FW = AsvBitsGeo<S>::FW;
     float mind = 100000000.0f;
     int best = -1;
     for (int k = 0; k < 3; k++) {
-        const int *f = k == 0 ? fc : (k == 1 ? fm : fp);
+        const unsigned *f = k == 0 ? fc : (k == 1 ? fm : fp);
         for (int a = 0; a < 3; a++)
             for (int c = 0; c < 3; c++) {
-                const int e = asv_bits_num(b, f[a * S * FW + c * S], Kp);
-                if (e >= ASV_BITS_MAXT) continue;
+                const unsigned bit = f[a * S * FW + c * S];
+                if (!bit) continue;
+                const int e = __ffs(bit) - 1;
                 const float dist = asv_jfa_dist_v(b.tdat[3 * e], b.tdat[3 * e + 1], b.tdat[3 * e + 2], vxy, vzl,
                                                   vab, ratio);
                 if (dist < mind) { mind = dist; best = b.tlab[e]; }
@@ -780,9 +772,8 @@ __device__ bool asv_jfa_bits_sub(const int32_t *__restrict__ in, int32_t *__rest
 {
     using G = AsvBitsGeo<S>;
     constexpr int FW = G::FW, FP = G::FP;
-    int *flab = (int *)smem;
-    unsigned *hx = (unsigned *)(smem + G::FLAB_BYTES);
-    uchar4 *labsh = (uchar4 *)(smem + G::FLAB_BYTES + G::HX_BYTES);
+    int *flab = (int *)smem;                                   // labels, then their bits
+    uchar4 *labsh = (uchar4 *)(smem + G::FLAB_BYTES);
     AsvBitsShared &b = *(AsvBitsShared *)(smem + ASV_JFA_AREA);
     const int tid = threadIdx.x, lane = tid & 31;
     const int sl = W * H;
@@ -860,31 +851,31 @@ __device__ bool asv_jfa_bits_sub(const int32_t *__restrict__ in, int32_t *__rest
         return false;
     }
     for (int i = tid; i < 3 * T; i += ASV_JFA_THREADS) b.tdat[i] = __ldg(tab + 3 * b.tlab[i / 3] + i % 3);
-    // row masks: labels at columns x - S, x, x + S of every footprint row
+    // every footprint entry becomes its label's bit (0: no label), in place:
+    // each thread converts the entries it copied
     for (int k = 0; k < nf; k++) {
 #pragma unroll
-        for (int i = 0; i < G::NHX; i++) {
-            const int q = tid + i * ASV_JFA_THREADS;
-            if (q < G::HXN) {
-                const int *r = flab + k * FP + (q >> 4) * FW + (q & 15);
-                unsigned m = 0;
-#pragma unroll
-                for (int c = 0; c < 3; c++) {
-                    const int l = r[c * S];
-                    m |= (unsigned)l < (unsigned)Kp ? 1u << b.map8[l] : 0u;
-                }
-                hx[k * G::HXN + q] = m;
+        for (int i = 0; i < G::NCOL; i++) {
+            const int e = tid + i * ASV_JFA_THREADS;
+            if (e < FP) {
+                int *q = flab + k * FP + e;
+                const int l = *q;
+                *q = (int)((unsigned)l < (unsigned)Kp ? 1u << b.map8[l] : 0u);
             }
         }
     }
     __syncthreads();
 
     // the chain walk of this thread's column
-    const unsigned *h0 = hx + ly * ASV_TILE_X + lx;              // row y - S of slot 0
-    const int *f0 = flab + ly * FW + lx;                         // candidate (x - S, y - S) of slot 0
-    auto smask = [&](int k) -> unsigned {
-        const unsigned *h = h0 + k * G::HXN;
-        return h[0] | h[S * ASV_TILE_X] | h[2 * S * ASV_TILE_X];
+    const unsigned *f0 = (const unsigned *)flab + ly * FW + lx;  // candidate (x - S, y - S) of slot 0
+    auto smask = [&](int k) -> unsigned {                         // a slice's 9 candidates
+        const unsigned *f = f0 + k * FP;
+        unsigned m = 0;
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) m |= f[a * S * FW + c * S];
+        return m;
     };
     const float2 vxy = make_float2((float)x + 0.5f, (float)y + 0.5f);
     const unsigned m_zero = any_brk ? smask(n + 2) : 0u, m_last = any_brk ? smask(n + 3) : 0u;
@@ -910,7 +901,7 @@ __device__ bool asv_jfa_bits_sub(const int32_t *__restrict__ in, int32_t *__rest
         }
         int label = bt >= 0 ? b.tlab[bt] : -1;
         if (tie)
-            label = asv_bits_ordered<S>(f0 + (j + 1) * FP, f0 + im * FP, f0 + ip * FP, b, Kp, vxy, vzl, vab, ratio);
+            label = asv_bits_ordered<S>(f0 + (j + 1) * FP, f0 + im * FP, f0 + ip * FP, b, vxy, vzl, vab, ratio);
         if (valid) out[z * sl + col] = label;
         if (SUMS) asv_accumulate(sums, slot0, c, Kp, x, y, z, label, valid);
         if (j + 1 < n) {
