@@ -306,12 +306,12 @@ size_t asv_layout_bytes(const std::vector<SegHost> &seg)
 }
 
 // JFA tile depth for a set of segments: the configured one, else the
-// deepest of 32/16/8 that still gives every resident block two tiles (deeper
-// runs share more slice lists; shallower ones fill the GPU), else 4.
+// deepest of 32/16/8 that still gives every resident block four tiles
+// (deeper runs share more slices; shallower ones balance the GPU), else 4.
 static int pick_zrun(const asv_ctx *ctx, const std::vector<SegHost> &seg)
 {
     if (ctx->cfg.jfa_zrun > 0) return std::min(ctx->cfg.jfa_zrun, 256);
-    const long long want = 2LL * asv_jfa_resident_blocks();
+    const long long want = 4LL * asv_jfa_resident_blocks();
     for (int z : { 32, 16, 8 }) {
         long long tiles = 0;
         for (const SegHost &h : seg)
