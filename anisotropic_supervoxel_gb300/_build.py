@@ -1,8 +1,11 @@
 """In-tree build of libasv.so (CUDA kernels for sm_103a + host C++).
 
-The kernels are compiled with -fmad=false: every float operation is one IEEE
-operation in the written order, which is what makes the labels bit-exact
-against the CPU restatement.
+The kernels with floating-point arithmetic are compiled with -fmad=false:
+every float operation is one IEEE operation in the written order, which is
+what makes the labels, metrics and flow bit-exact against the CPU
+restatement.  The integer-only kernels (connectivity, evaluation, the
+no-allocation post-processing) have no float multiply-add to contract, so
+they build without the flag.
 """
 import concurrent.futures
 import os
@@ -40,8 +43,13 @@ def _stale():
     return any(os.path.getmtime(s) > t for s in _sources() if os.path.exists(s))
 
 
+# translation units without floating-point arithmetic
+INTEGER_ONLY = {"asv_connect.cu", "asv_eval.cu", "asv_noalloc.cu"}
+
+
 def _nvcc_cmd(src, obj):
-    return [NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xptxas", "-v",
+    fmad = [] if os.path.basename(src) in INTEGER_ONLY else ["-fmad=false"]
+    return [NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", *fmad, "-Xptxas", "-v",
             "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC, "-c", src, "-o", obj]
 
 
