@@ -25,7 +25,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["asv_volume.cu", "asv_metric.cu", "asv_noalloc.cu", "asv_stream.cu", "asv_connect.cu",
               "asv_flow.cu", "asv_eval.cu"]
-CPP_SOURCES = ["asv_api.cpp", "asv_synth.cpp", "asv_server.cpp", "asv_png.cpp", "asv_render.cpp"]
+CPP_SOURCES = ["asv_api.cpp", "asv_synth.cpp", "asv_server.cpp", "asv_png.cpp", "asv_frames.cpp", "asv_render.cpp"]
 HEADERS = ["asv_common.cuh", "asv_internal.h", "asv_stream.cuh", "asv_connect.cuh", "asv_flow.cuh",
            "asv_eval.cuh"]
 PUBLIC_HEADERS = ["asv.h", "asv_host.h"]

@@ -154,6 +154,9 @@ SIGNATURES = {
     "asv_png_write_rgb": (c_int, [c_char_p, c_void_p, c_int, c_int]),
     "asv_render_rgb": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_void_p]),
     "asv_write_render_png": (c_int, [c_char_p, c_void_p, c_int, c_int, c_int, c_int, c_int]),
+    "asv_frame_info": (c_int, [c_char_p, P(c_int), P(c_int)]),
+    "asv_frame_read_bgr": (c_int, [c_char_p, c_void_p, c_int, c_int]),
+    "asv_frames_read_bgr": (c_int, [P(c_char_p), c_int, c_int, c_int, c_void_p]),
     "asv_render_options_default": (None, [P(RenderOptions)]),
     "asv_render_run": (c_int, [c_char_p, c_char_p, c_char_p, c_char_p, c_int, c_float, P(RenderOptions)]),
     "asv_render_stream_run": (c_int, [c_char_p, c_char_p, c_char_p, c_char_p, c_int, c_float, P(RenderOptions)]),

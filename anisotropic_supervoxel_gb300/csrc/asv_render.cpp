@@ -8,8 +8,8 @@
 // txt label file <seeds_num>.txt (print_sv_txt / output_label_all) and the
 // pseudo-colour frames <seeds_num>_NNNNN.png (print_render /
 // output_render_all, whose per-frame imwrite the reference leaves commented
-// out).  No GL context, window or OpenCV: frames are PNG files decoded by
-// this library.
+// out).  No GL context, window or OpenCV: frames are PNG, BMP or PNM files
+// decoded by this library.
 #include "asv.h"
 #include "asv_host.h"
 
@@ -74,7 +74,7 @@ int read_png_frames(const std::vector<std::string> &files, int f0, int n, int W,
     std::vector<const char *> paths;
     for (int i = f0; i < f0 + n; i++) paths.push_back(files[i].c_str());
     bgr.resize((size_t)n * W * H * 3);
-    const int e = asv_png_read_frames_bgr(paths.data(), n, W, H, bgr.data());
+    const int e = asv_frames_read_bgr(paths.data(), n, W, H, bgr.data());
     if (e == -5) return ASV_RENDER_ERR_SIZE;
     return e ? ASV_RENDER_ERR_DECODE : 0;
 }
@@ -112,7 +112,7 @@ extern "C" int asv_render_run(const char *dataset_path, const char *save_path, c
     if (out_stem(save_path, dbname, vdname, seeds_num, stem) != 0) return ASV_RENDER_ERR_IO;
     say(o, "%s,%lld:\n", vdname, seeds_num);
     int W = 0, H = 0;
-    if (asv_png_info(files[0].c_str(), &W, &H) != 0) return ASV_RENDER_ERR_DECODE;
+    if (asv_frame_info(files[0].c_str(), &W, &H) != 0) return ASV_RENDER_ERR_DECODE;
     const int D = (int)files.size();
     std::vector<uint8_t> bgr;
     int e = read_png_frames(files, 0, D, W, H, bgr);
@@ -164,7 +164,7 @@ extern "C" int asv_render_stream_run(const char *dataset_path, const char *save_
     if (out_stem(save_path, dbname, vdname, seeds_num, stem) != 0) return ASV_RENDER_ERR_IO;
     say(o, "%s,%lld:\n", vdname, seeds_num);
     int W = 0, H = 0;
-    if (asv_png_info(files[0].c_str(), &W, &H) != 0) return ASV_RENDER_ERR_DECODE;
+    if (asv_frame_info(files[0].c_str(), &W, &H) != 0) return ASV_RENDER_ERR_DECODE;
     const int D_all = (int)files.size();
 
     asv_config cfg;

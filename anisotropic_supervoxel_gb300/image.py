@@ -259,7 +259,7 @@ class Image:
         return self.labels()
 
     def segment_folder(self, folder, K):
-        """Render::run from a folder of PNG frames (GPU-AS/Render.cpp:151-243):
+        """Render::run from a folder of PNG, BMP or PNM frames (GPU-AS/Render.cpp:151-243):
         the sorted frames decoded on the host, preprocessing and optical flow
         on the device, then the plain sequence.  Returns post-processed labels."""
         self.init_gpu_bgr(read_frames(list_frames(folder)), K)
@@ -480,26 +480,44 @@ def read_png(path):
     return out
 
 
+FRAME_EXTENSIONS = (".png", ".bmp", ".ppm", ".pgm", ".pnm")
+
+
 def list_frames(folder):
-    """The PNG frames of a folder in sorted order (Render::run sorts the file
-    list, GPU-AS/Render.cpp:151-153)."""
-    names = sorted(f for f in os.listdir(folder) if f.lower().endswith(".png"))
+    """The frame files (PNG, BMP, PNM) of a folder in sorted order
+    (Render::run sorts the file list, GPU-AS/Render.cpp:151-153)."""
+    names = sorted(f for f in os.listdir(folder) if f.lower().endswith(FRAME_EXTENSIONS))
     if not names:
-        raise ValueError(f"no PNG frames in {folder}")
+        raise ValueError(f"no frames in {folder}")
     return [os.path.join(folder, f) for f in names]
 
 
+def frame_info(path):
+    """(W, H) of a PNG, BMP or PNM frame file"""
+    W, H = ctypes.c_int(), ctypes.c_int()
+    _png_ck(_lib.load().asv_frame_info(os.fsencode(path), ctypes.byref(W), ctypes.byref(H)), path)
+    return W.value, H.value
+
+
+def read_frame(path):
+    """cv::imread(path, 1) of a PNG, BMP or PNM frame: [H, W, 3] uint8 BGR, top row first."""
+    W, H = frame_info(path)
+    out = np.empty((H, W, 3), np.uint8)
+    _png_ck(_lib.load().asv_frame_read_bgr(os.fsencode(path), _ptr(out), W, H), path)
+    return out
+
+
 def read_frames(paths, out=None):
-    """Frames of one size decoded on all host threads: [D, H, W, 3] uint8 BGR
-    (into `out`, e.g. a pinned buffer, when given)."""
+    """Frames of one size (PNG, BMP or PNM) decoded on all host threads:
+    [D, H, W, 3] uint8 BGR (into `out`, e.g. a pinned buffer, when given)."""
     paths = list(paths)
-    W, H = png_info(paths[0])
+    W, H = frame_info(paths[0])
     if out is None:
         out = np.empty((len(paths), H, W, 3), np.uint8)
     elif out.shape != (len(paths), H, W, 3) or out.dtype != np.uint8 or not out.flags.c_contiguous:
         raise ValueError(f"out must be a contiguous uint8 array of shape {(len(paths), H, W, 3)}")
     arr = (ctypes.c_char_p * len(paths))(*[os.fsencode(p) for p in paths])
-    _png_ck(_lib.load().asv_png_read_frames_bgr(arr, len(paths), W, H, _ptr(out)), "frames")
+    _png_ck(_lib.load().asv_frames_read_bgr(arr, len(paths), W, H, _ptr(out)), "frames")
     return out
 
 

@@ -78,6 +78,15 @@ int asv_png_read_bgr(const char *path, uint8_t *bgr, int W, int H);
  * first frame that failed. */
 int asv_png_read_frames_bgr(const char *const *paths, int n, int W, int H, uint8_t *bgr);
 
+/* Any supported frame file, the format taken from its first bytes: PNG, BMP
+ * (1/4/8-bit palette, 16/24/32-bit, bit fields; RLE refused as -4) or
+ * binary PNM (P5 grey, P6 colour; maxval 255 or 65535).  Same pixels and
+ * return codes as the PNG calls above: imread(path, 1)'s BGR, top row first. */
+int asv_frame_info(const char *path, int *W, int *H);
+int asv_frame_read_bgr(const char *path, uint8_t *bgr, int W, int H);
+/* n frames of one size of any supported format, on all host threads */
+int asv_frames_read_bgr(const char *const *paths, int n, int W, int H, uint8_t *bgr);
+
 /* 8-bit RGB PNG (W*H*3 bytes, top row first). */
 int asv_png_write_rgb(const char *path, const uint8_t *rgb, int W, int H);
 
