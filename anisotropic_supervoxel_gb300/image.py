@@ -323,10 +323,13 @@ class Stream(Image):
         self._ck(self.lib.asv_stream_info_get(self.h, ctypes.byref(i)))
         return i
 
-    def push(self, rgb, fwd=None, bwd=None):
+    def push(self, rgb, fwd=None, bwd=None, out=None):
         """rgb [n,H,W,3] uint8, fwd/bwd [n,H,W,2] float32: the next block's new frames
         (fwd and bwd None: the block's flow is computed on the device).
-        Returns (first frame index, labels [done,H,W] int32)."""
+        `out`: where the labels go, an int32 C-contiguous array of at least
+        [block frames, H, W] (e.g. a pinned buffer reused for every block);
+        a new array when None.
+        Returns (first frame index, labels [done,H,W] int32, a view of `out`)."""
         inf = self.info()
         rgb = np.ascontiguousarray(rgb, np.uint8)
         if fwd is not None:
@@ -335,7 +338,11 @@ class Stream(Image):
         if rgb.shape[0] != inf.frames_needed:
             raise ValueError(f"block {inf.next_block} needs {inf.frames_needed} new frames")
         D = inf.block_end - inf.block_start
-        out = np.empty((D, self.H, self.W), np.int32)
+        if out is None:
+            out = np.empty((D, self.H, self.W), np.int32)
+        elif (out.dtype != np.int32 or not out.flags.c_contiguous or out.ndim != 3
+              or out.shape[0] < D or out.shape[1:] != (self.H, self.W)):
+            raise ValueError(f"out must be C-contiguous int32 of at least ({D}, {self.H}, {self.W})")
         done = ctypes.c_int()
         self._ck(self.lib.asv_stream_push(self.h, _ptr(rgb), _ptr(fwd), _ptr(bwd), _ptr(out),
                                           ctypes.byref(done)))
