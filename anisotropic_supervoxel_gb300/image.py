@@ -327,8 +327,9 @@ class Stream(Image):
         """rgb [n,H,W,3] uint8, fwd/bwd [n,H,W,2] float32: the next block's new frames
         (fwd and bwd None: the block's flow is computed on the device).
         `out`: where the labels go, an int32 C-contiguous array of at least
-        [block frames, H, W] (e.g. a pinned buffer reused for every block);
-        a new array when None.
+        [block frames, H, W]; a buffer reused for every block (e.g. pinned)
+        takes block_size + block_size // 3 frames, the longest block (the
+        last block absorbs the remainder of the video); a new array when None.
         Returns (first frame index, labels [done,H,W] int32, a view of `out`)."""
         inf = self.info()
         rgb = np.ascontiguousarray(rgb, np.uint8)

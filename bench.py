@@ -569,8 +569,8 @@ def run_stream_720p(args, device_flow=False):
     W, H, D_all, bs, I = w["W"], w["H"], w["D_all"], w["block_size"], w["iters"]
     s100 = w["seeds_num_100"]
     pin = {k: _pinned(np.zeros((bs,) + sh, dt)) for k, sh, dt in
-           (("rgb", (H, W, 3), np.uint8), ("fwd", (H, W, 2), np.float32), ("bwd", (H, W, 2), np.float32),
-            ("lab", (H, W), np.int32))}
+           (("rgb", (H, W, 3), np.uint8), ("fwd", (H, W, 2), np.float32), ("bwd", (H, W, 2), np.float32))}
+    pin["lab"] = _pinned(np.zeros((bs + bs // 3, H, W), np.int32))   # the longest block (the video's last)
 
     def new_stream():
         return asv.Stream(W, H, D_all, seeds_num_100=s100, block_size=bs, lloyd_iters=I, device=local)

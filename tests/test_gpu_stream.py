@@ -10,7 +10,7 @@ def _run_stream(asv, rgb, fwd, bwd, seeds100, iters, bs=30, reuse_out=False):
     D_all, H, W, _ = rgb.shape
     st = asv.Stream(W, H, D_all, seeds_num_100=seeds100, block_size=bs, lloyd_iters=iters)
     out = np.full((D_all, H, W), -7, np.int32)
-    buf = np.full((bs, H, W), -9, np.int32) if reuse_out else None   # one buffer for every block
+    buf = np.full((bs + bs // 3, H, W), -9, np.int32) if reuse_out else None   # the longest block
     info = st.info()
     nb = info.blocks
     for b in range(nb):
