@@ -142,6 +142,10 @@ SIGNATURES = {
     "asv_stream_begin": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_int, c_int]),
     "asv_stream_info_get": (c_int, [c_void_p, c_void_p]),
     "asv_stream_push": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, P(c_int)]),
+    "asv_stream_block": (c_int, [c_void_p, c_int, P(c_int), P(c_int), P(c_int)]),
+    "asv_stream_feed": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    "asv_stream_feed_bgr": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    "asv_stream_push_fed": (c_int, [c_void_p, c_void_p, P(c_int)]),
     # include/asv_host.h
     "asv_synth_clip": (c_int, [P(SynthParams), c_void_p, c_void_p, c_void_p]),
     "asv_synth_truth": (c_int, [P(SynthParams), c_void_p]),

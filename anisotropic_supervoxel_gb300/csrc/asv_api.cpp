@@ -170,7 +170,18 @@ struct asv_ctx {
         std::vector<int> iv;   // block intervals [start, end)
         StreamDev s{};
         int placed = 0, kept = 0, last_Kp = 0;
+        // blocks fed ahead (asv_stream_feed): two staging slots of new frames
+        int fed_next = 0;                          // the block the next feed takes
+        int fed_n[2] = { 0, 0 };                   // new frames held by each slot
+        bool fed_devflow[2] = { false, false };    // fed without flow: flow on the device
+        bool fed_bgr[2] = { false, false };        // fed as decoded BGR: preprocessed on the device
+        uint8_t *stg_rgb[2] = { nullptr, nullptr };
+        float *stg_fwd[2] = { nullptr, nullptr }, *stg_bwd[2] = { nullptr, nullptr };
     } sm;
+    // copy stream of asv_stream_feed and its events (created on first use):
+    // fed_ev[k] = slot k's upload done, used_ev[k] = slot k read by its push
+    cudaStream_t cp = nullptr;
+    cudaEvent_t fed_ev[2] = { nullptr, nullptr }, used_ev[2] = { nullptr, nullptr }, alloc_ev = nullptr;
     // connectivity enforcement scratch (asv_enforce_connectivity*), grown on demand
     void *cc = nullptr;
     size_t cc_bytes = 0;
@@ -230,6 +241,7 @@ static void ctx_free(asv_ctx *ctx, void *p)
 
 static void free_layout(asv_ctx *ctx)
 {
+    if (ctx->cp) cudaStreamSynchronize(ctx->cp);   // uploads into the staging slots end first
     if (ctx->gexec) { cudaGraphExecDestroy(ctx->gexec); ctx->gexec = nullptr; }
     for (void *p : ctx->allocs) ctx_free(ctx, p);
     ctx->allocs.clear();
@@ -614,6 +626,11 @@ asv_status asv_destroy(asv_ctx *ctx)
     ctx_free(ctx, ctx->fl);
     cudaStreamSynchronize(ctx->st);
     for (auto e : ctx->ev) cudaEventDestroy(e);
+    if (ctx->cp) {
+        cudaStreamDestroy(ctx->cp);
+        for (int k = 0; k < 2; k++) { cudaEventDestroy(ctx->fed_ev[k]); cudaEventDestroy(ctx->used_ev[k]); }
+        cudaEventDestroy(ctx->alloc_ev);
+    }
     if (ctx->own_st) cudaStreamDestroy(ctx->st);
     delete ctx;
     return ASV_OK;
@@ -1408,6 +1425,13 @@ static int stream_seeds_num(const asv_ctx *ctx, int b)
     return m.seeds100 * (Db - 10) / 100;
 }
 
+// frames block b takes from the caller: all of the first block's, then the
+// block's frames after the overlap kept on the device
+static int stream_new_frames(const asv_ctx::Stream &m, int b)
+{
+    return m.iv[2 * b + 1] - m.iv[2 * b] - (b == 0 ? 0 : 10);
+}
+
 asv_status asv_stream_begin(asv_ctx *ctx, int W, int H, int D_all, int K_video, int seeds_num_100,
                             int block_size)
 {
@@ -1466,20 +1490,92 @@ asv_status asv_stream_info_get(asv_ctx *ctx, asv_stream_info *info)
     if (m.next < m.nb) {
         info->block_start = m.iv[2 * m.next];
         info->block_end = m.iv[2 * m.next + 1];
-        info->frames_needed = info->block_end - info->block_start - (m.next == 0 ? 0 : 10);
+        info->frames_needed = stream_new_frames(m, m.next);
     }
     return ASV_OK;
 }
 
-asv_status asv_stream_push(asv_ctx *ctx, const uint8_t *rgb, const float *fwd, const float *bwd,
-                           int32_t *labels_out, int *done_frames)
+asv_status asv_stream_block(asv_ctx *ctx, int b, int *block_start, int *block_end, int *frames_needed)
+{
+    if (!ctx) return ASV_ERR_BAD_ARG;
+    const auto &m = ctx->sm;
+    if (!m.on) return fail(ctx, ASV_ERR_STATE, "no stream: call asv_stream_begin first");
+    if (b < 0 || b >= m.nb) return fail(ctx, ASV_ERR_BAD_ARG, "no such block");
+    if (block_start) *block_start = m.iv[2 * b];
+    if (block_end) *block_end = m.iv[2 * b + 1];
+    if (frames_needed) *frames_needed = stream_new_frames(m, b);
+    return ASV_OK;
+}
+
+static asv_status stream_feed(asv_ctx *ctx, bool bgr, const uint8_t *rgb, const float *fwd, const float *bwd)
+{
+    if (!ctx) return ASV_ERR_BAD_ARG;
+    auto &m = ctx->sm;
+    if (!m.on) return fail(ctx, ASV_ERR_STATE, "no stream: call asv_stream_begin first");
+    m.fed_next = std::max(m.fed_next, m.next);
+    if (m.fed_next >= m.nb) return fail(ctx, ASV_ERR_STATE, "every block of the video is fed");
+    if (m.fed_next > m.next + 1) return fail(ctx, ASV_ERR_STATE, "two blocks are fed ahead: push one first");
+    if (!rgb || (!fwd) != (!bwd)) return fail(ctx, ASV_ERR_BAD_ARG, "NULL buffer");
+    cudaSetDevice(ctx->cfg.device);
+    if (!ctx->cp) {
+        CK(cudaStreamCreateWithFlags(&ctx->cp, cudaStreamNonBlocking));
+        for (int k = 0; k < 2; k++) {
+            CK(cudaEventCreateWithFlags(&ctx->fed_ev[k], cudaEventDisableTiming));
+            CK(cudaEventCreateWithFlags(&ctx->used_ev[k], cudaEventDisableTiming));
+        }
+        CK(cudaEventCreateWithFlags(&ctx->alloc_ev, cudaEventDisableTiming));
+    }
+    const int b = m.fed_next, slot = b & 1;
+    const size_t WH = (size_t)m.W * m.H, n = (size_t)stream_new_frames(m, b) * WH;
+    if (!m.stg_rgb[slot]) {                         // both slots' staging, stream-ordered on the context
+        const size_t cap = (size_t)m.Dcap * WH;
+        for (int k = 0; k < 2; k++) {
+            asv_status s;
+            if ((s = dalloc(ctx, &m.stg_rgb[k], 3 * cap)) != ASV_OK) return s;
+            if ((s = dalloc(ctx, &m.stg_fwd[k], 2 * cap)) != ASV_OK) return s;
+            if ((s = dalloc(ctx, &m.stg_bwd[k], 2 * cap)) != ASV_OK) return s;
+        }
+        CK(cudaEventRecord(ctx->alloc_ev, ctx->st));
+        CK(cudaStreamWaitEvent(ctx->cp, ctx->alloc_ev, 0));
+    }
+    CK(cudaStreamWaitEvent(ctx->cp, ctx->used_ev[slot], 0));   // block b-2's push has read the slot
+    CK(cudaMemcpyAsync(m.stg_rgb[slot], rgb, 3 * n, cudaMemcpyHostToDevice, ctx->cp));
+    if (fwd) {
+        CK(cudaMemcpyAsync(m.stg_fwd[slot], fwd, 8 * n, cudaMemcpyHostToDevice, ctx->cp));
+        CK(cudaMemcpyAsync(m.stg_bwd[slot], bwd, 8 * n, cudaMemcpyHostToDevice, ctx->cp));
+    }
+    CK(cudaEventRecord(ctx->fed_ev[slot], ctx->cp));
+    m.fed_n[slot] = stream_new_frames(m, b);
+    m.fed_devflow[slot] = !fwd;
+    m.fed_bgr[slot] = bgr;
+    m.fed_next = b + 1;
+    return ASV_OK;
+}
+
+asv_status asv_stream_feed(asv_ctx *ctx, const uint8_t *rgb, const float *fwd, const float *bwd)
+{
+    return stream_feed(ctx, false, rgb, fwd, bwd);
+}
+
+asv_status asv_stream_feed_bgr(asv_ctx *ctx, const uint8_t *bgr, const float *fwd, const float *bwd)
+{
+    return stream_feed(ctx, true, bgr, fwd, bwd);
+}
+
+// asv_stream_push (new frames from the caller) and asv_stream_push_fed (new
+// frames fed ahead into a staging slot)
+static asv_status stream_push(asv_ctx *ctx, bool fed, const uint8_t *rgb, const float *fwd, const float *bwd,
+                              int32_t *labels_out, int *done_frames)
 {
     if (!ctx) return ASV_ERR_BAD_ARG;
     auto &m = ctx->sm;
     if (!m.on) return fail(ctx, ASV_ERR_STATE, "no stream: call asv_stream_begin first");
     if (m.next >= m.nb) return fail(ctx, ASV_ERR_STATE, "the stream is finished");
-    if (!rgb || !labels_out || (!fwd) != (!bwd)) return fail(ctx, ASV_ERR_BAD_ARG, "NULL buffer");
-    const bool device_flow = !fwd;                                  // both NULL: flow computed here
+    if (fed && m.fed_next <= m.next) return fail(ctx, ASV_ERR_STATE, "the block was not fed: asv_stream_feed first");
+    if (!fed && m.fed_next > m.next) return fail(ctx, ASV_ERR_STATE, "the block was fed: use asv_stream_push_fed");
+    if (!labels_out || (!fed && (!rgb || (!fwd) != (!bwd)))) return fail(ctx, ASV_ERR_BAD_ARG, "NULL buffer");
+    const int slot = m.next & 1;
+    const bool device_flow = fed ? m.fed_devflow[slot] : !fwd;     // no flow given: computed here
     cudaSetDevice(ctx->cfg.device);
     const int b = m.next;
     const int Db = m.iv[2 * b + 1] - m.iv[2 * b];
@@ -1496,11 +1592,32 @@ asv_status asv_stream_push(asv_ctx *ctx, const uint8_t *rgb, const float *fwd, c
         CK(cudaMemcpyAsync(d.bwd, d.bwd + src, 8 * n, cudaMemcpyDeviceToDevice, st));
     }
     const size_t nnew = (size_t)(Db - z0) * WH;
-    CK(cudaMemcpyAsync(d.rgb + 3 * z0 * WH, rgb, 3 * nnew, cudaMemcpyHostToDevice, st));
-    if (!device_flow) {
-        CK(cudaMemcpyAsync(d.fwd + z0 * WH, fwd, 8 * nnew, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(d.bwd + z0 * WH, bwd, 8 * nnew, cudaMemcpyHostToDevice, st));
+    if (fed) {                                                      // uploaded during the previous block
+        if (m.fed_n[slot] != Db - z0) return fail(ctx, ASV_ERR_STATE, "the fed frames do not match the block");
+        CK(cudaStreamWaitEvent(st, ctx->fed_ev[slot], 0));
+        if (m.fed_bgr[slot]) {                                      // cvMat2TexureInput per frame
+            asv_launch_preprocess(m.stg_rgb[slot], d.rgb + 3 * z0 * WH, m.W, m.H, Db - z0, st);
+            CK(cudaGetLastError());
+        } else {
+            CK(cudaMemcpyAsync(d.rgb + 3 * z0 * WH, m.stg_rgb[slot], 3 * nnew, cudaMemcpyDeviceToDevice, st));
+        }
+        if (!device_flow) {
+            CK(cudaMemcpyAsync(d.fwd + z0 * WH, m.stg_fwd[slot], 8 * nnew, cudaMemcpyDeviceToDevice, st));
+            CK(cudaMemcpyAsync(d.bwd + z0 * WH, m.stg_bwd[slot], 8 * nnew, cudaMemcpyDeviceToDevice, st));
+        }
+        CK(cudaEventRecord(ctx->used_ev[slot], st));
     } else {
+        CK(cudaMemcpyAsync(d.rgb + 3 * z0 * WH, rgb, 3 * nnew, cudaMemcpyHostToDevice, st));
+        if (!device_flow) {
+            CK(cudaMemcpyAsync(d.fwd + z0 * WH, fwd, 8 * nnew, cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(d.bwd + z0 * WH, bwd, 8 * nnew, cudaMemcpyHostToDevice, st));
+        }
+    }
+    asv_status es = ensure_events(ctx, 2);
+    if (es != ASV_OK) return es;
+    const size_t ev0 = ctx->ev.size() - 2;
+    if (device_flow) {
+        CK(cudaEventRecord(ctx->ev[ev0], st));
         // the block's flow from its own frames, as the streaming program does
         // per block.  Pairs within the overlap frames were computed by the
         // previous block (same two frames, same flow) and came along with the
@@ -1561,11 +1678,9 @@ asv_status asv_stream_push(asv_ctx *ctx, const uint8_t *rgb, const float *fwd, c
     ctx->jfa_blocks = jfa_blocks_for(ctx, tiles);
 
     // device time of the window's compute: from here (its frames are on the
-    // device) to the labels mapped, before they are read back
-    asv_status es = ensure_events(ctx, 2);
-    if (es != ASV_OK) return es;
-    const size_t ev0 = ctx->ev.size() - 2;
-    CK(cudaEventRecord(ctx->ev[ev0], st));
+    // device; before the flow kernels when the flow is computed here) to the
+    // labels mapped, before they are read back
+    if (!device_flow) CK(cudaEventRecord(ctx->ev[ev0], st));
     asv_launch_rgb2lab(d, st);                                   // new frames only (lab_from)
     CK(cudaMemsetAsync(d.dacc, 0, sizeof(unsigned long long) * d.total_seeds, st));
     asv_launch_density(d, st);
@@ -1612,10 +1727,22 @@ asv_status asv_stream_push(asv_ctx *ctx, const uint8_t *rgb, const float *fwd, c
     m.last_Kp = Kp;
     m.prev_Db = Db;
     m.next++;
+    m.fed_next = std::max(m.fed_next, m.next);
     ctx->have_rgb = ctx->have_flow = ctx->have_pos0 = ctx->have_M0 = ctx->have_lab = true;
     ctx->seeded = ctx->ran = true;
     if (done_frames) *done_frames = done;
     return ASV_OK;
+}
+
+asv_status asv_stream_push(asv_ctx *ctx, const uint8_t *rgb, const float *fwd, const float *bwd,
+                           int32_t *labels_out, int *done_frames)
+{
+    return stream_push(ctx, false, rgb, fwd, bwd, labels_out, done_frames);
+}
+
+asv_status asv_stream_push_fed(asv_ctx *ctx, int32_t *labels_out, int *done_frames)
+{
+    return stream_push(ctx, true, nullptr, nullptr, nullptr, labels_out, done_frames);
 }
 
 } // extern "C"

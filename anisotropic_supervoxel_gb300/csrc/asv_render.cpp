@@ -18,6 +18,7 @@
 #include <cstring>
 #include <filesystem>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace {
@@ -178,25 +179,37 @@ extern "C" int asv_render_stream_run(const char *dataset_path, const char *save_
     // seeds_num_100 = seeds_num * 100 / depth_all (streamGPU-AS/Render.cpp:156-158), blocks of 30
     if ((st = asv_stream_begin(c.c, W, H, D_all, seeds_num, 0, 30)) != ASV_OK) return asv_fail(c.c, st, "blocks");
     std::vector<int32_t> labels((size_t)W * H * D_all, -1);
-    std::vector<uint8_t> bgr, rgb;
     asv_stream_info inf;
-    for (;;) {
-        if ((st = asv_stream_info_get(c.c, &inf)) != ASV_OK) return asv_fail(c.c, st, "stream info");
-        if (inf.next_block >= inf.blocks) break;
-        // the block's new frames: imread, cvMat2TexureInput (streamGPU-AS/Render.cpp:696-702)
-        const int n = inf.frames_needed, f0 = inf.block_end - n;
-        int e = read_png_frames(files, f0, n, W, H, bgr);
-        if (e) return e;
-        rgb.resize(bgr.size());
-        const size_t fr = (size_t)W * H * 3;
-        for (int t = 0; t < n; t++)
-            if (asv_preprocess_frame(bgr.data() + fr * t, W, H, rgb.data() + fr * t) != 0) return ASV_RENDER_ERR_ARG;
+    if ((st = asv_stream_info_get(c.c, &inf)) != ASV_OK) return asv_fail(c.c, st, "stream info");
+    const int nb = inf.blocks;
+    // the block's new frames as imread gives them (streamGPU-AS/Render.cpp:
+    // 696-702), into buffer b % 2; cvMat2TexureInput runs on the device
+    std::vector<uint8_t> bgr[2];
+    auto decode = [&](int b) -> int {
+        int a = 0, e = 0, n = 0;
+        if (asv_stream_block(c.c, b, &a, &e, &n) != ASV_OK) return ASV_RENDER_ERR_GPU;
+        return read_png_frames(files, e - n, n, W, H, bgr[b % 2]);
+    };
+    int e = decode(0);
+    if (e) return e;
+    if ((st = asv_stream_feed_bgr(c.c, bgr[0].data(), nullptr, nullptr)) != ASV_OK) return asv_fail(c.c, st, "feed");
+    for (int b = 0; b < nb; b++) {
+        // block b+1 is decoded on the host threads while block b runs on the
+        // device; buffer (b+1) % 2 last held block b-1, whose push has returned
+        int e_next = 0;
+        std::thread worker([&] { if (b + 1 < nb) e_next = decode(b + 1); });
+        if ((st = asv_stream_info_get(c.c, &inf)) != ASV_OK) { worker.join(); return asv_fail(c.c, st, "stream info"); }
         int done = 0;
         // flow computed on the device per block, as the streaming program does
-        if ((st = asv_stream_push(c.c, rgb.data(), nullptr, nullptr, labels.data() + (size_t)W * H * inf.block_start,
-                                  &done)) != ASV_OK)
-            return asv_fail(c.c, st, "block_segment");
+        st = asv_stream_push_fed(c.c, labels.data() + (size_t)W * H * inf.block_start, &done);
+        worker.join();
+        if (st != ASV_OK) return asv_fail(c.c, st, "block_segment");
         say(o, "%sblock done, %lld frames\n", "", done);
+        if (b + 1 < nb) {
+            if (e_next) return e_next;
+            if ((st = asv_stream_feed_bgr(c.c, bgr[(b + 1) % 2].data(), nullptr, nullptr)) != ASV_OK)
+                return asv_fail(c.c, st, "feed");
+        }
     }
     if ((st = asv_stream_info_get(c.c, &inf)) != ASV_OK) return asv_fail(c.c, st, "stream info");
     // labels_all with label_num_all = seeds_num_placed (streamGPU-AS/Render.cpp:289-292)

@@ -317,6 +317,7 @@ class Stream(Image):
         super().__init__(**kw)
         self._ck(self.lib.asv_stream_begin(self.h, W, H, D_all, K_video, seeds_num_100, block_size))
         self.W, self.H = W, H
+        self._fed = {}       # block -> the fed arrays, alive until that block's push returns
 
     def info(self):
         i = _lib.StreamInfo()
@@ -347,6 +348,49 @@ class Stream(Image):
         done = ctypes.c_int()
         self._ck(self.lib.asv_stream_push(self.h, _ptr(rgb), _ptr(fwd), _ptr(bwd), _ptr(out),
                                           ctypes.byref(done)))
+        return inf.block_start, out[:done.value]
+
+    def block(self, b):
+        """(block_start, block_end, frames_needed) of block b"""
+        a, e, n = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self._ck(self.lib.asv_stream_block(self.h, b, ctypes.byref(a), ctypes.byref(e), ctypes.byref(n)))
+        return a.value, e.value, n.value
+
+    def feed(self, rgb, fwd=None, bwd=None, bgr=False):
+        """Queue the upload of the next unfed block's new frames (asv_stream_feed):
+        it runs on the device while the block before it computes.  bgr=True:
+        the frames as decoded (BGR, top row first), preprocessed on the device
+        (asv_stream_feed_bgr).  Returns the block's index.  The arrays must stay
+        unchanged until that block's push_fed returns (they are kept alive here
+        until then)."""
+        b = max([self.info().next_block] + [k + 1 for k in self._fed])
+        if b >= self.info().blocks:
+            raise ValueError("every block of the video is fed")
+        n = self.block(b)[2]
+        rgb = np.ascontiguousarray(rgb, np.uint8)
+        if fwd is not None:
+            fwd = np.ascontiguousarray(fwd, np.float32)
+            bwd = np.ascontiguousarray(bwd, np.float32)
+        if rgb.shape[0] != n:
+            raise ValueError(f"block {b} needs {n} new frames")
+        call = self.lib.asv_stream_feed_bgr if bgr else self.lib.asv_stream_feed
+        self._ck(call(self.h, _ptr(rgb), _ptr(fwd), _ptr(bwd)))
+        self._fed[b] = (rgb, fwd, bwd)
+        return b
+
+    def push_fed(self, out=None):
+        """asv_stream_push_fed: the next block, whose frames were fed ahead.
+        `out` and the return value as in push."""
+        inf = self.info()
+        D = inf.block_end - inf.block_start
+        if out is None:
+            out = np.empty((D, self.H, self.W), np.int32)
+        elif (out.dtype != np.int32 or not out.flags.c_contiguous or out.ndim != 3
+              or out.shape[0] < D or out.shape[1:] != (self.H, self.W)):
+            raise ValueError(f"out must be C-contiguous int32 of at least ({D}, {self.H}, {self.W})")
+        done = ctypes.c_int()
+        self._ck(self.lib.asv_stream_push_fed(self.h, _ptr(out), ctypes.byref(done)))
+        self._fed.pop(inf.next_block, None)
         return inf.block_start, out[:done.value]
 
 

@@ -93,8 +93,9 @@ typedef struct asv_stats {
     double total_ms;    /* device time of the last asv_run_lloyd */
     int launches;       /* kernels launched by the last asv_run_lloyd or asv_stream_push */
     double window_ms;   /* device time of the last asv_stream_push's compute: from its
-                           first kernel (the window's new frames already uploaded) to the
-                           window's labels mapped, before they are read back */
+                           first kernel (the window's new frames already uploaded; the
+                           optical flow included when it is computed on the device) to
+                           the window's labels mapped, before they are read back */
 } asv_stats;
 
 typedef struct asv_ctx asv_ctx;
@@ -323,6 +324,30 @@ asv_status asv_stream_info_get(asv_ctx *ctx, asv_stream_info *info);
  * W*H*done_frames int32. */
 asv_status asv_stream_push(asv_ctx *ctx, const uint8_t *rgb, const float *fwd, const float *bwd,
                            int32_t *labels_out, int *done_frames);
+
+/* Frame range and new-frame count of block b (0 <= b < blocks). */
+asv_status asv_stream_block(asv_ctx *ctx, int b, int *block_start, int *block_end, int *frames_needed);
+
+/* Uploading ahead.  No counterpart in the reference, which reads a block's
+ * frames when the block starts.  asv_stream_feed queues the host->device
+ * copy of the new frames of the next block not yet fed (same buffers and
+ * NULL-flow rule as asv_stream_push; frames_needed from asv_stream_block)
+ * on the context's copy stream and returns at once, so the copy runs while
+ * the block before it computes.  At most two blocks are fed ahead of the
+ * next push (ASV_ERR_STATE beyond).  The host buffers must stay valid and
+ * unchanged until the push of that block returns; pinned buffers make the
+ * copy asynchronous.  A fed block is processed by asv_stream_push_fed (its
+ * frames move from the staging slot into the window on the device); an
+ * asv_stream_push of a fed block, or an asv_stream_push_fed of a block not
+ * fed, fails with ASV_ERR_STATE.  The two staging slots (2 x block frames x
+ * W*H*19 bytes) are allocated at the first feed. */
+asv_status asv_stream_feed(asv_ctx *ctx, const uint8_t *rgb, const float *fwd, const float *bwd);
+/* As asv_stream_feed with the frames as cv::imread gives them (8-bit BGR,
+ * top row first): the push runs Render::cvMat2TexureInput on the device
+ * (streamGPU-AS/Render.cpp:696-702: 3x3 Gaussian blur, BGR -> RGB, vertical
+ * flip; the same arithmetic as asv_preprocess_frame). */
+asv_status asv_stream_feed_bgr(asv_ctx *ctx, const uint8_t *bgr, const float *fwd, const float *bwd);
+asv_status asv_stream_push_fed(asv_ctx *ctx, int32_t *labels_out, int *done_frames);
 
 /* ---- serving ------------------------------------------------------------- */
 

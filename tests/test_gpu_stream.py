@@ -52,6 +52,98 @@ def test_stream_reused_output_buffer(asv, orc):
     st.close()
 
 
+def _fed_frames(st, b, rgb, fwd, bwd, flow=True):
+    a, e, n = st.block(b)
+    z0 = e - a - n
+    return (rgb[a + z0:e], fwd[a + z0:e], bwd[a + z0:e]) if flow else (rgb[a + z0:e],)
+
+
+def test_stream_fed_ahead_matches_oracle(asv, orc):
+    """frames uploaded a block ahead (asv_stream_feed / asv_stream_push_fed) give
+    the oracle's labels; the call-order rules are enforced"""
+    W, H, D, s100, iters = 48, 40, 75, 200, 4
+    rgb, fwd, bwd = asv.synth_clip(W, H, D, n_ellipses=6, noise_sigma=5.0, vmax=2.0, jitter=0.3,
+                                   drift_amp=2.0, drift_period=40.0, seed=W + D)
+    st = asv.Stream(W, H, D, seeds_num_100=s100, block_size=30, lloyd_iters=iters)
+    nb = st.info().blocks
+    assert nb == 3
+    out = np.full((D, H, W), -7, np.int32)
+    with pytest.raises(asv.AsvError):
+        st.push_fed()                                    # nothing fed
+    assert st.feed(*_fed_frames(st, 0, rgb, fwd, bwd)) == 0
+    with pytest.raises(asv.AsvError):
+        st.push(*_fed_frames(st, 0, rgb, fwd, bwd))      # a fed block goes through push_fed
+    assert st.feed(*_fed_frames(st, 1, rgb, fwd, bwd)) == 1
+    with pytest.raises(asv.AsvError):
+        st.feed(*_fed_frames(st, 2, rgb, fwd, bwd))      # at most two blocks ahead
+    buf = np.full((40, H, W), -9, np.int32)
+    for b in range(nb):
+        if 1 <= b and b + 1 < nb:
+            assert st.feed(*_fed_frames(st, b + 1, rgb, fwd, bwd)) == b + 1
+        f0, lab = st.push_fed(out=buf)
+        out[f0:f0 + lab.shape[0]] = lab
+    with pytest.raises(asv.AsvError):
+        st.push_fed()                                    # the video is done
+    st.close()
+    want, info = orc.run_stream(rgb, fwd, bwd, seeds_num_100=s100, iters=iters, nthreads=8)
+    assert np.array_equal(out, want)
+
+
+def test_stream_fed_ahead_device_flow_equals_push(asv):
+    """fed without flow: the device computes each block's flow, as push does"""
+    W, H, D = 40, 32, 56
+    rgb, fwd, bwd = asv.synth_clip(W, H, D, n_ellipses=6, noise_sigma=5.0, vmax=2.0, jitter=0.3,
+                                   drift_amp=2.0, drift_period=40.0, seed=5)
+    res = []
+    for mode in ("push", "fed"):
+        st = asv.Stream(W, H, D, seeds_num_100=250, block_size=30, lloyd_iters=3)
+        nb = st.info().blocks
+        out = np.full((D, H, W), -7, np.int32)
+        if mode == "fed":
+            st.feed(*_fed_frames(st, 0, rgb, fwd, bwd, flow=False))
+        for b in range(nb):
+            if mode == "fed":
+                if b + 1 < nb:
+                    st.feed(*_fed_frames(st, b + 1, rgb, fwd, bwd, flow=False))
+                f0, lab = st.push_fed()
+            else:
+                f0, lab = st.push(*_fed_frames(st, b, rgb, fwd, bwd, flow=False))
+            out[f0:f0 + lab.shape[0]] = lab
+        st.close()
+        res.append(out)
+    assert (res[0] != -7).all()
+    assert np.array_equal(res[0], res[1])
+
+
+def test_stream_fed_bgr_equals_host_preprocessing(asv):
+    """frames fed as decoded BGR (asv_stream_feed_bgr, preprocessed on the
+    device) give the labels of the host-preprocessed frames pushed as RGB"""
+    W, H, D = 40, 32, 56
+    rgb, fwd, bwd = asv.synth_clip(W, H, D, n_ellipses=6, noise_sigma=5.0, vmax=2.0, jitter=0.3,
+                                   drift_amp=2.0, drift_period=40.0, seed=9)
+    bgr = np.ascontiguousarray(rgb[:, ::-1, :, ::-1])     # as imread would give the frames
+    pre = np.stack([asv.preprocess_frame(f) for f in bgr])
+    res = []
+    for mode in ("push", "fed_bgr"):
+        st = asv.Stream(W, H, D, seeds_num_100=250, block_size=30, lloyd_iters=3)
+        nb = st.info().blocks
+        out = np.full((D, H, W), -7, np.int32)
+        if mode == "fed_bgr":
+            st.feed(*_fed_frames(st, 0, bgr, fwd, bwd), bgr=True)
+        for b in range(nb):
+            if mode == "fed_bgr":
+                if b + 1 < nb:
+                    st.feed(*_fed_frames(st, b + 1, bgr, fwd, bwd), bgr=True)
+                f0, lab = st.push_fed()
+            else:
+                f0, lab = st.push(*_fed_frames(st, b, pre, fwd, bwd))
+            out[f0:f0 + lab.shape[0]] = lab
+        st.close()
+        res.append(out)
+    assert (res[0] != -7).all()
+    assert np.array_equal(res[0], res[1])
+
+
 def test_stream_720p_windows_match_oracle(asv, orc):
     """the 1280x720 streaming configuration (windows of 30 frames, 10 overlap,
     seeds_num_100 = 10000) over its first two windows, three Lloyd
