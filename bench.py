@@ -155,6 +155,18 @@ def profile_value(key, path=None):
     return None
 
 
+def fp32_rate(ops_per_voxel, nvox, launch_s):
+    """Executed FP32 operations of a k_jfa pass: ncu's FADD/FMUL counts per
+    voxel (two-wide instructions counted twice; the mean of the captured
+    steps 3, 2 and 1 in the committed summary) x voxels / the measured
+    average pass time."""
+    if ops_per_voxel is None or not launch_s:
+        return None
+    return {"ops_per_voxel_ncu": ops_per_voxel, "tops": ops_per_voxel * nvox / launch_s / 1e12,
+            "what": "executed FP32 operations (ncu sass counts, no FMA executes) per voxel of the "
+                    "captured passes x voxels / average gather-pass time"}
+
+
 def jfa_traffic_per_voxel():
     """DRAM bytes per voxel of one JFA pass from the committed ncu summary."""
     return profile_value("dram_bytes_per_voxel")
@@ -364,6 +376,7 @@ def run_ours(args):
                          "launch_ms": jfa_launch_s * 1e3,
                          "traffic": tpv * nvox if tpv is not None else None,
                          "issue_active_ncu": profile_value("issue_active"),
+                         "fp32": fp32_rate(profile_value("fp32_ops_per_voxel"), nvox, jfa_launch_s),
                          "jfa_share_of_loop": jfa_ms / loop_ms if loop_ms else None},
             "clocks": clk,
             "gpu_launches": int(launches * args.steps),
@@ -705,6 +718,7 @@ def run_stream_720p(args, device_flow=False):
                          "launch_of": "a k_jfa gather pass over one 1280x720x30 window (27.6 M voxels)",
                          "traffic": tpv * nvox if tpv is not None else None,
                          "issue_active_ncu": profile_value("issue_active", TRAFFIC_720P),
+                         "fp32": fp32_rate(profile_value("fp32_ops_per_voxel", TRAFFIC_720P), nvox, jfa_launch_s),
                          "jfa_share_of_loop": jfa_ms / loop_ms if loop_ms else None},
             "block_Kp_mean": statistics.mean(kps),
             "clocks": clk, "gpu_launches": int(launches),
