@@ -1527,16 +1527,19 @@ static asv_status stream_feed(asv_ctx *ctx, bool bgr, const uint8_t *rgb, const 
     }
     const int b = m.fed_next, slot = b & 1;
     const size_t WH = (size_t)m.W * m.H, n = (size_t)stream_new_frames(m, b) * WH;
-    if (!m.stg_rgb[slot]) {                         // both slots' staging, stream-ordered on the context
-        const size_t cap = (size_t)m.Dcap * WH;
+    {                                               // both slots' staging, stream-ordered on the context
+        const size_t cap = (size_t)m.Dcap * WH;     // (each buffer set only once allocated, so a failed
+        bool fresh = false;                         //  allocation leaves nothing half made for a retry)
         for (int k = 0; k < 2; k++) {
             asv_status s;
-            if ((s = dalloc(ctx, &m.stg_rgb[k], 3 * cap)) != ASV_OK) return s;
-            if ((s = dalloc(ctx, &m.stg_fwd[k], 2 * cap)) != ASV_OK) return s;
-            if ((s = dalloc(ctx, &m.stg_bwd[k], 2 * cap)) != ASV_OK) return s;
+            if (!m.stg_rgb[k]) { if ((s = dalloc(ctx, &m.stg_rgb[k], 3 * cap)) != ASV_OK) return s; fresh = true; }
+            if (!m.stg_fwd[k]) { if ((s = dalloc(ctx, &m.stg_fwd[k], 2 * cap)) != ASV_OK) return s; fresh = true; }
+            if (!m.stg_bwd[k]) { if ((s = dalloc(ctx, &m.stg_bwd[k], 2 * cap)) != ASV_OK) return s; fresh = true; }
         }
-        CK(cudaEventRecord(ctx->alloc_ev, ctx->st));
-        CK(cudaStreamWaitEvent(ctx->cp, ctx->alloc_ev, 0));
+        if (fresh) {
+            CK(cudaEventRecord(ctx->alloc_ev, ctx->st));
+            CK(cudaStreamWaitEvent(ctx->cp, ctx->alloc_ev, 0));
+        }
     }
     CK(cudaStreamWaitEvent(ctx->cp, ctx->used_ev[slot], 0));   // block b-2's push has read the slot
     CK(cudaMemcpyAsync(m.stg_rgb[slot], rgb, 3 * n, cudaMemcpyHostToDevice, ctx->cp));

@@ -144,6 +144,33 @@ def test_stream_fed_bgr_equals_host_preprocessing(asv):
     assert np.array_equal(res[0], res[1])
 
 
+def test_stream_feed_over_budget_leaves_push_usable(asv):
+    """a feed whose staging does not fit the context's HBM budget fails, again
+    on a retry, and the stream still runs through push"""
+    W, H, D = 40, 32, 56
+    rgb, fwd, bwd = asv.synth_clip(W, H, D, n_ellipses=6, noise_sigma=5.0, vmax=2.0, jitter=0.3,
+                                   drift_amp=2.0, drift_period=40.0, seed=13)
+    lo, hi = 0, 1 << 30                       # the least budget the stream's layout fits in
+    while hi - lo > 4096:
+        mid = (lo + hi) // 2
+        try:
+            asv.Stream(W, H, D, seeds_num_100=250, block_size=30, lloyd_iters=3, hbm_budget=mid).close()
+            hi = mid
+        except asv.AsvError:
+            lo = mid
+    st = asv.Stream(W, H, D, seeds_num_100=250, block_size=30, lloyd_iters=3, hbm_budget=hi)
+    for _ in range(2):
+        with pytest.raises(asv.AsvError):
+            st.feed(*_fed_frames(st, 0, rgb, fwd, bwd))
+    got = np.full((D, H, W), -7, np.int32)
+    for b in range(st.info().blocks):
+        f0, lab = st.push(*_fed_frames(st, b, rgb, fwd, bwd))
+        got[f0:f0 + lab.shape[0]] = lab
+    st.close()
+    want, _, _ = _run_stream(asv, rgb, fwd, bwd, 250, 3)
+    assert np.array_equal(got, want)
+
+
 def test_stream_720p_windows_match_oracle(asv, orc):
     """the 1280x720 streaming configuration (windows of 30 frames, 10 overlap,
     seeds_num_100 = 10000) over its first two windows, three Lloyd
