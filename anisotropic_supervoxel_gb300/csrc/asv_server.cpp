@@ -202,20 +202,31 @@ static void worker(asv_server *s, int w)
     }
 }
 
+// A session's windows run in submission order.  Each window's frames are
+// fed to the context's copy stream (asv_stream_feed), and so are those of
+// the next queued window before this one is pushed, so that upload runs
+// while this window computes.  A window whose feed is refused (e.g. the
+// staging does not fit the budget) goes through asv_stream_push instead.
 static void session_worker(asv_server *s, Session *ss)
 {
     std::unique_lock<std::mutex> lk(s->mu);
+    long long fed = -1;                        // the last request whose window is fed
     while (true) {
         s->cv_work.wait(lk, [&] { return s->stop || !ss->q.empty(); });
         if (ss->q.empty()) return;
         long long id = ss->q.front();
         ss->q.pop_front();
         Req &q = *s->reqs[id];
+        const long long nid = ss->q.empty() ? -1 : ss->q.front();
+        const Req *nq = nid >= 0 ? s->reqs[nid].get() : nullptr;   // alive until it is done
         s->running++;
         q.t_start = Clock::now();
         lk.unlock();
+        const bool fed_this = fed == id || asv_stream_feed(ss->ctx, q.r.rgb, q.r.fwd, q.r.bwd) == ASV_OK;
+        if (fed_this && nq && asv_stream_feed(ss->ctx, nq->r.rgb, nq->r.fwd, nq->r.bwd) == ASV_OK) fed = nid;
         int done = 0;
-        asv_status st = asv_stream_push(ss->ctx, q.r.rgb, q.r.fwd, q.r.bwd, q.r.labels_out, &done);
+        asv_status st = fed_this ? asv_stream_push_fed(ss->ctx, q.r.labels_out, &done)
+                                 : asv_stream_push(ss->ctx, q.r.rgb, q.r.fwd, q.r.bwd, q.r.labels_out, &done);
         lk.lock();
         q.status = st;
         q.done_frames = done;
