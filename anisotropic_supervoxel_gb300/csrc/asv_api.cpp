@@ -178,6 +178,13 @@ struct asv_ctx {
         uint8_t *stg_rgb[2] = { nullptr, nullptr };
         float *stg_fwd[2] = { nullptr, nullptr }, *stg_bwd[2] = { nullptr, nullptr };
     } sm;
+    // the streaming form's Lloyd loop as a CUDA graph, replayed by every
+    // window whose launch configuration (device pointers and totals, JFA grid,
+    // pass count) equals the one it was captured with: the per-window data
+    // (seed counts, segment descriptor) is read from device memory
+    cudaGraphExec_t sgexec = nullptr;
+    AsvDev skey{};
+    int skey_blocks = -1, skey_passes = -1, skey_iters = -1, sg_launches = 0;
     // copy stream of asv_stream_feed and its events (created on first use):
     // fed_ev[k] = slot k's upload done, used_ev[k] = slot k read by its push
     cudaStream_t cp = nullptr;
@@ -243,6 +250,7 @@ static void free_layout(asv_ctx *ctx)
 {
     if (ctx->cp) cudaStreamSynchronize(ctx->cp);   // uploads into the staging slots end first
     if (ctx->gexec) { cudaGraphExecDestroy(ctx->gexec); ctx->gexec = nullptr; }
+    if (ctx->sgexec) { cudaGraphExecDestroy(ctx->sgexec); ctx->sgexec = nullptr; ctx->skey_blocks = -1; }
     for (void *p : ctx->allocs) ctx_free(ctx, p);
     ctx->allocs.clear();
     ctx->bytes = 0;
@@ -1708,7 +1716,33 @@ static asv_status stream_push(asv_ctx *ctx, bool fed, const uint8_t *rgb, const 
     ctx->launches = 4;                                           // LAB, density (2), seed composition
     asv_launch_metric(d, 0, st);
     ctx->launches += 5;
-    enqueue_lloyd(ctx, false);
+    if (ctx->cfg.use_graph && !ctx->cfg.instrument) {
+        const bool same = ctx->sgexec && std::memcmp(&ctx->skey, &d, sizeof(AsvDev)) == 0 &&
+                          ctx->skey_blocks == ctx->jfa_blocks && ctx->skey_passes == ctx->maxpass &&
+                          ctx->skey_iters == ctx->cfg.lloyd_iters;
+        if (!same) {
+            if (ctx->sgexec) { cudaGraphExecDestroy(ctx->sgexec); ctx->sgexec = nullptr; }
+            const int before = ctx->launches;
+            cudaGraph_t g;
+            CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            enqueue_lloyd(ctx, false);
+            cudaError_t e = cudaStreamEndCapture(st, &g);
+            if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaStreamEndCapture");
+            e = cudaGraphInstantiate(&ctx->sgexec, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) { ctx->sgexec = nullptr; return cuda_fail(ctx, e, "cudaGraphInstantiate"); }
+            std::memcpy(&ctx->skey, &d, sizeof(AsvDev));
+            ctx->skey_blocks = ctx->jfa_blocks;
+            ctx->skey_passes = ctx->maxpass;
+            ctx->skey_iters = ctx->cfg.lloyd_iters;
+            ctx->sg_launches = ctx->launches - before;
+        } else {
+            ctx->launches += ctx->sg_launches;
+        }
+        CK(cudaGraphLaunch(ctx->sgexec, st));
+    } else {
+        enqueue_lloyd(ctx, false);
+    }
     const int keep = b < m.nb - 1;
     asv_launch_stream_next(d, m.s, (float)(m.bs - one_third), (float)two_third, keep, st);
     const int done = keep ? Db - one_third : Db;
