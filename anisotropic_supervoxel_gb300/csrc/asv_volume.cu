@@ -704,6 +704,7 @@ __device__ __forceinline__ void asv_jfa_run(const int32_t *__restrict__ in, int3
 
 struct AsvBitsShared {
     float4 tdat[3 * ASV_BITS_MAXT];             // the table's seed rows (as jtab)
+    unsigned acc[(ASV_BITS_MAXT + 1) * 8];      // centroid sums of the sub-tile per table entry (+ label -1)
     unsigned claim[ASV_BITS_MAXKP / 32];        // labels numbered in this sub-tile (all zero between)
     int tlab[ASV_BITS_TLCAP];                   // label of each number
     int slotz[20];                              // slice of each footprint slot
@@ -755,10 +756,26 @@ __device__ __noinline__ int asv_bits_ordered(const unsigned *__restrict__ fc, co
                 const int e = __ffs(bit) - 1;
                 const float dist = asv_jfa_dist_v(b.tdat[3 * e], b.tdat[3 * e + 1], b.tdat[3 * e + 2], vxy, vzl,
                                                   vab, ratio);
-                if (dist < mind) { mind = dist; best = b.tlab[e]; }
+                if (dist < mind) { mind = dist; best = e; }
             }
     }
-    return best;
+    return best;                                              // table entry, or -1
+}
+
+// A thread's run of voxels with one label, added to its table entry's
+// centroid sums in shared memory: count n, sum of 2z+1 and of L, a, b; the
+// column's 2x+1 and 2y+1 times n.  Exact u32 sums (a sub-tile holds at most
+// 16 x 256 voxels of coordinates below 4096).
+__device__ __forceinline__ void asv_run_flush(unsigned *__restrict__ a, unsigned n, unsigned sz, unsigned sl,
+                                              unsigned sa, unsigned sb, int x, int y)
+{
+    atomicAdd(a + 0, n * (2u * (unsigned)x + 1u));
+    atomicAdd(a + 1, n * (2u * (unsigned)y + 1u));
+    atomicAdd(a + 2, sz);
+    atomicAdd(a + 3, n);
+    atomicAdd(a + 4, sl);
+    atomicAdd(a + 5, sa);
+    atomicAdd(a + 6, sb);
 }
 
 // One sub-tile of n <= SUB chain positions from p0 in bit-set form; false
@@ -851,6 +868,8 @@ __device__ bool asv_jfa_bits_sub(const int32_t *__restrict__ in, int32_t *__rest
         return false;
     }
     for (int i = tid; i < 3 * T; i += ASV_JFA_THREADS) b.tdat[i] = __ldg(tab + 3 * b.tlab[i / 3] + i % 3);
+    if (SUMS)
+        for (int i = tid; i < (ASV_BITS_MAXT + 1) * 8; i += ASV_JFA_THREADS) b.acc[i] = 0u;
     // every footprint entry becomes its label's bit (0: no label), in place:
     // each thread converts the entries it copied
     for (int k = 0; k < nf; k++) {
@@ -881,6 +900,12 @@ __device__ bool asv_jfa_bits_sub(const int32_t *__restrict__ in, int32_t *__rest
     const unsigned m_zero = any_brk ? smask(n + 2) : 0u, m_last = any_brk ? smask(n + 3) : 0u;
     unsigned mm = smask(0), mc = smask(1);
     int im = 0;
+    // centroid sums (last pass of an iteration): the thread's current run of
+    // equal labels along its column, flushed into the sub-tile's table when
+    // the label changes and at the end; the table goes to the global sums
+    // once per sub-tile (centroids.vs:19-54; label -1 counts in slot Kp)
+    int run_e = -1;
+    unsigned run_n = 0u, run_z = 0u, run_l = 0u, run_a = 0u, run_b = 0u;
     for (int j = 0; j < n; j++) {
         const int z = b.slotz[j + 1];
         const bool chain = z + S < D;                         // the plus slice is the next centre
@@ -899,14 +924,34 @@ __device__ bool asv_jfa_bits_sub(const int32_t *__restrict__ in, int32_t *__rest
                                             ratio);
             if (da < best) { best = da; bt = ta; tie = false; } else if (da == best) tie = true;
         }
-        int label = bt >= 0 ? b.tlab[bt] : -1;
-        if (tie)
-            label = asv_bits_ordered<S>(f0 + (j + 1) * FP, f0 + im * FP, f0 + ip * FP, b, vxy, vzl, vab, ratio);
+        if (tie) bt = asv_bits_ordered<S>(f0 + (j + 1) * FP, f0 + im * FP, f0 + ip * FP, b, vxy, vzl, vab, ratio);
+        const int label = bt >= 0 ? b.tlab[bt] : -1;
         if (valid) out[z * sl + col] = label;
-        if (SUMS) asv_accumulate(sums, slot0, c, Kp, x, y, z, label, valid);
+        if (SUMS && valid) {
+            const int e = bt >= 0 ? bt : ASV_BITS_MAXT;
+            if (e != run_e) {
+                if (run_e >= 0) asv_run_flush(b.acc + 8 * run_e, run_n, run_z, run_l, run_a, run_b, x, y);
+                run_e = e;
+                run_n = run_z = run_l = run_a = run_b = 0u;
+            }
+            run_n++;
+            run_z += 2u * (unsigned)z + 1u;
+            run_l += c.x; run_a += c.y; run_b += c.z;
+        }
         if (j + 1 < n) {
             if (chain) { mm = mc; mc = mp; im = j + 1; }
             else { mm = m_zero; mc = smask(j + 2); im = n + 2; }
+        }
+    }
+    if (SUMS) {
+        if (run_e >= 0) asv_run_flush(b.acc + 8 * run_e, run_n, run_z, run_l, run_a, run_b, x, y);
+        __syncthreads();
+        for (int i = tid; i < (T + 1) * 7; i += ASV_JFA_THREADS) {
+            const int e = i / 7, k = i - e * 7;
+            const int ent = e < T ? e : ASV_BITS_MAXT;           // the -1 entry after the T labels
+            const unsigned v = b.acc[8 * ent + k];
+            if (v) atomicAdd(sums + 8ull * (slot0 + (ent < ASV_BITS_MAXT ? b.tlab[ent] : Kp)) + k,
+                             (unsigned long long)v);
         }
     }
     __syncthreads();                                          // the footprint and table are reused
