@@ -944,7 +944,19 @@ __device__ bool asv_jfa_bits_sub(const int32_t *__restrict__ in, int32_t *__rest
         }
     }
     if (SUMS) {
-        if (run_e >= 0) asv_run_flush(b.acc + 8 * run_e, run_n, run_z, run_l, run_a, run_b, x, y);
+        // the runs left at the end, grouped by entry across the warp (every
+        // lane of the block gets here; lanes without a run join with entry
+        // -1, which adds nothing), so a warp adds each entry once
+        const unsigned grp = __match_any_sync(0xffffffffu, run_e);
+        const unsigned q[7] = { run_n * (2u * (unsigned)x + 1u), run_n * (2u * (unsigned)y + 1u), run_z, run_n,
+                                run_l, run_a, run_b };
+        unsigned t[7];
+#pragma unroll
+        for (int k = 0; k < 7; k++) t[k] = __reduce_add_sync(grp, q[k]);
+        if (run_e >= 0 && lane == __ffs(grp) - 1) {
+#pragma unroll
+            for (int k = 0; k < 7; k++) atomicAdd(b.acc + 8 * run_e + k, t[k]);
+        }
         __syncthreads();
         for (int i = tid; i < (T + 1) * 7; i += ASV_JFA_THREADS) {
             const int e = i / 7, k = i - e * 7;
