@@ -699,7 +699,7 @@ __device__ __forceinline__ void asv_jfa_run(const int32_t *__restrict__ in, int3
 #define ASV_BITS_MAXKP 8192      // segment seed counts up to this use the bit-set form
 #define ASV_BITS_TLCAP 256       // claimed labels remembered for the reset
 #define ASV_BITS_NONE 255        // table number of no label
-#define ASV_BITS_AREA 62464      // shared bytes of the largest sub-tile (step 4, 16 positions)
+#define ASV_BITS_AREA 62464      // shared bytes of the largest sub-tiles (step 4, 16 positions; step 6, 12)
 #define ASV_JFA_AREA (ASV_BITS_AREA > ASV_JFA_LIST_BYTES ? ASV_BITS_AREA : ASV_JFA_LIST_BYTES)
 
 struct AsvBitsShared {
@@ -717,7 +717,7 @@ template <int S> struct AsvBitsGeo {
     static constexpr int FW = ASV_TILE_X + 2 * S;                     // footprint width and height
     static constexpr int FP = FW * FW;                                // footprint entries per slot
     // chain positions per sub-tile: deep where the footprint stays small
-    static constexpr int SUB = S <= 4 ? 16 : 8;
+    static constexpr int SUB = S <= 4 ? 16 : 12;
     static constexpr int NSLOT = SUB + 4;
     static constexpr int NCOL = (FP + ASV_JFA_THREADS - 1) / ASV_JFA_THREADS;
     static constexpr int FLAB_BYTES = NSLOT * FP * 4;
