@@ -586,9 +586,10 @@ __device__ __forceinline__ int32_t asv_jfa_eval(const asv_list_t *__restrict__ A
     return best;
 }
 
-// Centroid sums of one voxel, fused into the last JFA pass of a Lloyd
-// iteration (centroids.vs:19-54; a label outside [0, Kp) counts in the -1
-// slot, so no slot beyond the segment's is written): the lanes of the warp are grouped by
+// Centroid sums of one voxel in the list form, fused into the last JFA pass
+// of a Lloyd iteration (the bit-set form sums runs of equal labels instead,
+// asv_run_flush) (centroids.vs:19-54; a label outside [0, Kp) counts in the
+// -1 slot, so no slot beyond the segment's is written): the lanes of the warp are grouped by
 // destination slot, reduced in the warp, and one u64 atomic per group and
 // component is issued.  Every lane of the warp makes this call for every
 // voxel of the tile (a lane whose column lies outside the segment passes
