@@ -700,12 +700,14 @@ __device__ __forceinline__ void asv_jfa_run(const int32_t *__restrict__ in, int3
 #define ASV_BITS_MAXKP 8192      // segment seed counts up to this use the bit-set form
 #define ASV_BITS_TLCAP 256       // claimed labels remembered for the reset
 #define ASV_BITS_NONE 255        // table number of no label
+#define ASV_ACC_ROW 7            // words per entry of the sub-tile's centroid-sum table (odd: the
+                                 // entries' rows start in different shared-memory banks)
 #define ASV_BITS_AREA 62464      // shared bytes of the largest sub-tiles (step 4, 16 positions; step 6, 12)
 #define ASV_JFA_AREA (ASV_BITS_AREA > ASV_JFA_LIST_BYTES ? ASV_BITS_AREA : ASV_JFA_LIST_BYTES)
 
 struct AsvBitsShared {
     float4 tdat[3 * ASV_BITS_MAXT];             // the table's seed rows (as jtab)
-    unsigned acc[(ASV_BITS_MAXT + 1) * 8];      // centroid sums of the sub-tile per table entry (+ label -1)
+    unsigned acc[(ASV_BITS_MAXT + 1) * ASV_ACC_ROW];   // centroid sums of the sub-tile per table entry (+ label -1)
     unsigned claim[ASV_BITS_MAXKP / 32];        // labels numbered in this sub-tile (all zero between)
     int tlab[ASV_BITS_TLCAP];                   // label of each number
     int slotz[20];                              // slice of each footprint slot
@@ -870,7 +872,7 @@ __device__ bool asv_jfa_bits_sub(const int32_t *__restrict__ in, int32_t *__rest
     }
     for (int i = tid; i < 3 * T; i += ASV_JFA_THREADS) b.tdat[i] = __ldg(tab + 3 * b.tlab[i / 3] + i % 3);
     if (SUMS)
-        for (int i = tid; i < (ASV_BITS_MAXT + 1) * 8; i += ASV_JFA_THREADS) b.acc[i] = 0u;
+        for (int i = tid; i < (ASV_BITS_MAXT + 1) * ASV_ACC_ROW; i += ASV_JFA_THREADS) b.acc[i] = 0u;
     // every footprint entry becomes its label's bit (0: no label), in place:
     // each thread converts the entries it copied
     for (int k = 0; k < nf; k++) {
@@ -931,7 +933,7 @@ __device__ bool asv_jfa_bits_sub(const int32_t *__restrict__ in, int32_t *__rest
         if (SUMS && valid) {
             const int e = bt >= 0 ? bt : ASV_BITS_MAXT;
             if (e != run_e) {
-                if (run_e >= 0) asv_run_flush(b.acc + 8 * run_e, run_n, run_z, run_l, run_a, run_b, x, y);
+                if (run_e >= 0) asv_run_flush(b.acc + ASV_ACC_ROW * run_e, run_n, run_z, run_l, run_a, run_b, x, y);
                 run_e = e;
                 run_n = run_z = run_l = run_a = run_b = 0u;
             }
@@ -956,13 +958,13 @@ __device__ bool asv_jfa_bits_sub(const int32_t *__restrict__ in, int32_t *__rest
         for (int k = 0; k < 7; k++) t[k] = __reduce_add_sync(grp, q[k]);
         if (run_e >= 0 && lane == __ffs(grp) - 1) {
 #pragma unroll
-            for (int k = 0; k < 7; k++) atomicAdd(b.acc + 8 * run_e + k, t[k]);
+            for (int k = 0; k < 7; k++) atomicAdd(b.acc + ASV_ACC_ROW * run_e + k, t[k]);
         }
         __syncthreads();
         for (int i = tid; i < (T + 1) * 7; i += ASV_JFA_THREADS) {
             const int e = i / 7, k = i - e * 7;
             const int ent = e < T ? e : ASV_BITS_MAXT;           // the -1 entry after the T labels
-            const unsigned v = b.acc[8 * ent + k];
+            const unsigned v = b.acc[ASV_ACC_ROW * ent + k];
             if (v) atomicAdd(sums + 8ull * (slot0 + (ent < ASV_BITS_MAXT ? b.tlab[ent] : Kp)) + k,
                              (unsigned long long)v);
         }
