@@ -177,7 +177,17 @@ struct asv_ctx {
         bool fed_bgr[2] = { false, false };        // fed as decoded BGR: preprocessed on the device
         uint8_t *stg_rgb[2] = { nullptr, nullptr };
         float *stg_fwd[2] = { nullptr, nullptr }, *stg_bwd[2] = { nullptr, nullptr };
+        // pinned host staging of a block's small copies (in the context's
+        // pinned block hpin), so that none of them is a synchronous copy
+        // from pageable memory: prefixes, the segment descriptor before and
+        // after the seed count is known, counters, post record, cells, grid
+        int *h_pref = nullptr, *h_ctr = nullptr, *h_post = nullptr, *h_ctr2 = nullptr, *h_cells = nullptr;
+        SegDesc *h_sdA = nullptr, *h_sdB = nullptr;
+        float4 *h_grid = nullptr;
+        size_t h_cells_cap = 0;
     } sm;
+    void *hpin = nullptr;                     // pinned host block of the streaming form
+    size_t hpin_bytes = 0;
     // the streaming form's Lloyd loop as a CUDA graph, replayed by every
     // window whose launch configuration (device pointers and totals, JFA grid,
     // pass count) equals the one it was captured with: the per-window data
@@ -634,6 +644,7 @@ asv_status asv_destroy(asv_ctx *ctx)
     ctx_free(ctx, ctx->fl);
     cudaStreamSynchronize(ctx->st);
     for (auto e : ctx->ev) cudaEventDestroy(e);
+    if (ctx->hpin) cudaFreeHost(ctx->hpin);
     if (ctx->cp) {
         cudaStreamDestroy(ctx->cp);
         for (int k = 0; k < 2; k++) { cudaEventDestroy(ctx->fed_ev[k]); cudaEventDestroy(ctx->used_ev[k]); }
@@ -1471,6 +1482,38 @@ asv_status asv_stream_begin(asv_ctx *ctx, int W, int H, int D_all, int K_video, 
     cap.W = W; cap.H = H; cap.D = m.Dcap; cap.Kp = m.Kcap; cap.npass = 1;
     cap.g.wNum = wmax; cap.g.hNum = hmax; cap.g.dNum = dmax; cap.g.Kp = m.Kcap;
     cap.cells.assign((size_t)W + H + m.Dcap + 2 * wmax, -1);
+    {                                              // the pinned host staging of every block's small copies
+        size_t off = 0;
+        auto take = [&](size_t b) { const size_t o = off; off += (b + 255) & ~(size_t)255; return o; };
+        const size_t o_pref = take(6 * sizeof(int)), o_sda = take(sizeof(SegDesc)), o_sdb = take(sizeof(SegDesc)),
+                     o_ctr = take(sizeof(int) * STREAM_CTR_WORDS), o_post = take(sizeof(int) * ASV_POST_WORDS),
+                     o_ctr2 = take(sizeof(int) * STREAM_CTR_WORDS), o_cells = take(sizeof(int) * cap.cells.size()),
+                     o_grid = take(sizeof(float4) * (size_t)m.Kcap);
+        if (ctx->hpin_bytes < off) {
+            if (ctx->hpin) {
+                cudaStreamSynchronize(ctx->st);
+                cudaFreeHost(ctx->hpin);
+                ctx->hpin = nullptr;
+                ctx->hpin_bytes = 0;
+            }
+            if (cudaHostAlloc(&ctx->hpin, off, cudaHostAllocDefault) != cudaSuccess) {
+                cudaGetLastError();
+                ctx->hpin = nullptr;
+                return fail(ctx, ASV_ERR_OOM, "cudaHostAlloc: stream staging");
+            }
+            ctx->hpin_bytes = off;
+        }
+        char *hb = (char *)ctx->hpin;
+        m.h_pref = (int *)(hb + o_pref);
+        m.h_sdA = (SegDesc *)(hb + o_sda);
+        m.h_sdB = (SegDesc *)(hb + o_sdb);
+        m.h_ctr = (int *)(hb + o_ctr);
+        m.h_post = (int *)(hb + o_post);
+        m.h_ctr2 = (int *)(hb + o_ctr2);
+        m.h_cells = (int *)(hb + o_cells);
+        m.h_grid = (float4 *)(hb + o_grid);
+        m.h_cells_cap = cap.cells.size();
+    }
     cap.grid.assign((size_t)4 * m.Kcap, 0.f);
     ctx->seg.assign(1, cap);
     asv_status s = asv_build_layout(ctx);
@@ -1675,16 +1718,20 @@ static asv_status stream_push(asv_ctx *ctx, bool fed, const uint8_t *rgb, const 
     const int chunks = (int)((sd.nvox + ASV_CHUNK - 1) / ASV_CHUNK);
     d.total_tiles = tiles;
     d.total_chunks = chunks;
-    int tp[2] = { 0, tiles }, cp[2] = { 0, chunks }, sp[2] = { 0, seed_cap };
-    CK(cudaMemcpyAsync((void *)d.tile_prefix, tp, sizeof(tp), cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync((void *)d.chunk_prefix, cp, sizeof(cp), cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync((void *)d.seed_prefix, sp, sizeof(sp), cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync((void *)d.segs, &sd, sizeof(SegDesc), cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(d.cells, h.cells.data(), sizeof(int) * h.cells.size(), cudaMemcpyHostToDevice, st));
-    std::vector<float4> grid((size_t)Kn);
+    // (the pinned staging is free again: the previous block ended with a synchronize)
+    if (h.cells.size() > m.h_cells_cap || Kn > m.Kcap) return fail(ctx, ASV_ERR_STATE, "block larger than its layout");
+    int *pref = m.h_pref;
+    pref[0] = 0; pref[1] = tiles; pref[2] = 0; pref[3] = chunks; pref[4] = 0; pref[5] = seed_cap;
+    CK(cudaMemcpyAsync((void *)d.tile_prefix, pref, 2 * sizeof(int), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync((void *)d.chunk_prefix, pref + 2, 2 * sizeof(int), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync((void *)d.seed_prefix, pref + 4, 2 * sizeof(int), cudaMemcpyHostToDevice, st));
+    *m.h_sdA = sd;
+    CK(cudaMemcpyAsync((void *)d.segs, m.h_sdA, sizeof(SegDesc), cudaMemcpyHostToDevice, st));
+    std::memcpy(m.h_cells, h.cells.data(), sizeof(int) * h.cells.size());
+    CK(cudaMemcpyAsync(d.cells, m.h_cells, sizeof(int) * h.cells.size(), cudaMemcpyHostToDevice, st));
     for (int k = 0; k < Kn; k++)
-        grid[k] = make_float4(h.grid[4 * k], h.grid[4 * k + 1], h.grid[4 * k + 2], h.grid[4 * k + 3]);
-    CK(cudaMemcpyAsync(d.grid, grid.data(), sizeof(float4) * Kn, cudaMemcpyHostToDevice, st));
+        m.h_grid[k] = make_float4(h.grid[4 * k], h.grid[4 * k + 1], h.grid[4 * k + 2], h.grid[4 * k + 3]);
+    CK(cudaMemcpyAsync(d.grid, m.h_grid, sizeof(float4) * Kn, cudaMemcpyHostToDevice, st));
     ctx->maxpass = h.npass;
     ctx->jfa_blocks = jfa_blocks_for(ctx, tiles);
 
@@ -1698,15 +1745,15 @@ static asv_status stream_push(asv_ctx *ctx, bool fed, const uint8_t *rgb, const 
     asv_launch_density_adjust(d, st);
     asv_launch_stream_compose(d, m.s, Kn, m.Kcap, st);          // kept seeds first, then the new ones
     CK(cudaGetLastError());
-    int ctr[STREAM_CTR_WORDS], post[ASV_POST_WORDS];
-    CK(cudaMemcpyAsync(ctr, m.s.ctr, sizeof(ctr), cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(post, d.post, sizeof(post), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(m.h_ctr, m.s.ctr, sizeof(int) * STREAM_CTR_WORDS, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(m.h_post, d.post, sizeof(int) * ASV_POST_WORDS, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    if (post[POST_VALID] != Kn) return fail(ctx, ASV_ERR_CUDA, "density placement produced fewer seeds than the grid");
-    if (ctr[STREAM_KP] < 0) return fail(ctx, ASV_ERR_OVER_BUDGET, "kept + new seeds exceed the stream's seed capacity");
-    const int Kp = ctr[STREAM_KP];
+    if (m.h_post[POST_VALID] != Kn) return fail(ctx, ASV_ERR_CUDA, "density placement produced fewer seeds than the grid");
+    if (m.h_ctr[STREAM_KP] < 0) return fail(ctx, ASV_ERR_OVER_BUDGET, "kept + new seeds exceed the stream's seed capacity");
+    const int Kp = m.h_ctr[STREAM_KP];
     sd.Kp = Kp;
-    CK(cudaMemcpyAsync((void *)d.segs, &sd, sizeof(SegDesc), cudaMemcpyHostToDevice, st));
+    *m.h_sdB = sd;
+    CK(cudaMemcpyAsync((void *)d.segs, m.h_sdB, sizeof(SegDesc), cudaMemcpyHostToDevice, st));
     h.Kp = Kp;
     ctx->seg[0] = h;
     ctx->seg[0].vox_off = 0;
@@ -1751,7 +1798,7 @@ static asv_status stream_push(asv_ctx *ctx, bool fed, const uint8_t *rgb, const 
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev[ev0 + 1], st));
     CK(cudaMemcpyAsync(labels_out, m.s.lab_out, sizeof(int32_t) * WH * done, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(ctr, m.s.ctr, sizeof(ctr), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(m.h_ctr2, m.s.ctr, sizeof(int) * STREAM_CTR_WORDS, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     float wms = 0.f;
     CK(cudaEventElapsedTime(&wms, ctx->ev[ev0], ctx->ev[ev0 + 1]));
@@ -1759,8 +1806,8 @@ static asv_status stream_push(asv_ctx *ctx, bool fed, const uint8_t *rgb, const 
     ctx->stats.launches = ctx->launches;
     std::swap(m.s.kept_pos, m.s.kept_next);
     std::swap(m.s.gmap_prev, m.s.gmap_cur);
-    m.placed = ctr[STREAM_PLACED];
-    m.kept = ctr[STREAM_KEPT];
+    m.placed = m.h_ctr2[STREAM_PLACED];
+    m.kept = m.h_ctr2[STREAM_KEPT];
     m.last_Kp = Kp;
     m.prev_Db = Db;
     m.next++;
