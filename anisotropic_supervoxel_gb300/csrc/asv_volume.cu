@@ -991,7 +991,9 @@ __device__ __forceinline__ void asv_jfa_tile(const int32_t *__restrict__ in, int
     // go through one inlined copy of the list form
     unsigned fail = 1u;
     int sub = n;
-    if (step <= ASV_BITS_MAXS && Kp <= ASV_BITS_MAXKP && n <= 32 * 4) {   // <= 32 sub-tiles of >= 4
+    // <= 32 sub-tiles of >= 4; with tiles of 4 positions the footprint slots
+    // outnumber the positions from step 3 on, where the list form is faster
+    if (step <= ASV_BITS_MAXS && Kp <= ASV_BITS_MAXKP && n <= 32 * 4 && (zrun >= 8 || step <= 2)) {
         fail = 0u;
 #define ASV_BITS_CASE(S_)                                                                                    \
     case S_:                                                                                                 \

@@ -112,7 +112,8 @@ def _blocky_labels(rng, shape, kp, block, minus=0.02):
 @pytest.mark.parametrize("step", [1, 2, 3, 4, 5, 6, 8])
 def test_jfa_single_pass_bitset_and_ties(asv, orc, step, zrun):
     """Labels constant on small cubes keep a sub-tile's footprint under 32
-    labels, so the pass takes the bit-set form (steps <= 6); seeds come in
+    labels, so the pass takes the bit-set form (steps <= 6; with tiles of 4
+    positions only steps 1-2, the list form above); seeds come in
     identical pairs (same position, colour and metric), so pairs of labels
     tie at the least distance (thousands of voxels per case) and the
     shader's candidate order decides.  A third of the volume holds random
