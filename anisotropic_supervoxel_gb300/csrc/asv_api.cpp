@@ -179,10 +179,10 @@ struct asv_ctx {
         float *stg_fwd[2] = { nullptr, nullptr }, *stg_bwd[2] = { nullptr, nullptr };
         // pinned host staging of a block's small copies (in the context's
         // pinned block hpin), so that none of them is a synchronous copy
-        // from pageable memory: prefixes, the segment descriptor before and
-        // after the seed count is known, counters, post record, cells, grid
-        int *h_pref = nullptr, *h_ctr = nullptr, *h_post = nullptr, *h_ctr2 = nullptr, *h_cells = nullptr;
-        SegDesc *h_sdA = nullptr, *h_sdB = nullptr;
+        // from pageable memory: prefixes, the segment descriptor, the
+        // counters after the seed composition and at the end, cells, grid
+        int *h_pref = nullptr, *h_ctr = nullptr, *h_ctr2 = nullptr, *h_cells = nullptr;
+        SegDesc *h_sdA = nullptr;
         float4 *h_grid = nullptr;
         size_t h_cells_cap = 0;
     } sm;
@@ -1485,8 +1485,8 @@ asv_status asv_stream_begin(asv_ctx *ctx, int W, int H, int D_all, int K_video, 
     {                                              // the pinned host staging of every block's small copies
         size_t off = 0;
         auto take = [&](size_t b) { const size_t o = off; off += (b + 255) & ~(size_t)255; return o; };
-        const size_t o_pref = take(6 * sizeof(int)), o_sda = take(sizeof(SegDesc)), o_sdb = take(sizeof(SegDesc)),
-                     o_ctr = take(sizeof(int) * STREAM_CTR_WORDS), o_post = take(sizeof(int) * ASV_POST_WORDS),
+        const size_t o_pref = take(6 * sizeof(int)), o_sda = take(sizeof(SegDesc)),
+                     o_ctr = take(sizeof(int) * STREAM_CTR_WORDS),
                      o_ctr2 = take(sizeof(int) * STREAM_CTR_WORDS), o_cells = take(sizeof(int) * cap.cells.size()),
                      o_grid = take(sizeof(float4) * (size_t)m.Kcap);
         if (ctx->hpin_bytes < off) {
@@ -1506,9 +1506,7 @@ asv_status asv_stream_begin(asv_ctx *ctx, int W, int H, int D_all, int K_video, 
         char *hb = (char *)ctx->hpin;
         m.h_pref = (int *)(hb + o_pref);
         m.h_sdA = (SegDesc *)(hb + o_sda);
-        m.h_sdB = (SegDesc *)(hb + o_sdb);
         m.h_ctr = (int *)(hb + o_ctr);
-        m.h_post = (int *)(hb + o_post);
         m.h_ctr2 = (int *)(hb + o_ctr2);
         m.h_cells = (int *)(hb + o_cells);
         m.h_grid = (float4 *)(hb + o_grid);
@@ -1745,16 +1743,10 @@ static asv_status stream_push(asv_ctx *ctx, bool fed, const uint8_t *rgb, const 
     asv_launch_density_adjust(d, st);
     asv_launch_stream_compose(d, m.s, Kn, m.Kcap, st);          // kept seeds first, then the new ones
     CK(cudaGetLastError());
+    // the composed seed count went to the segment descriptor on the device
+    // (k_stream_compose), so the rest of the block is enqueued without a
+    // host round trip; the counters of this point are read at the end
     CK(cudaMemcpyAsync(m.h_ctr, m.s.ctr, sizeof(int) * STREAM_CTR_WORDS, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(m.h_post, d.post, sizeof(int) * ASV_POST_WORDS, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    if (m.h_post[POST_VALID] != Kn) return fail(ctx, ASV_ERR_CUDA, "density placement produced fewer seeds than the grid");
-    if (m.h_ctr[STREAM_KP] < 0) return fail(ctx, ASV_ERR_OVER_BUDGET, "kept + new seeds exceed the stream's seed capacity");
-    const int Kp = m.h_ctr[STREAM_KP];
-    sd.Kp = Kp;
-    *m.h_sdB = sd;
-    CK(cudaMemcpyAsync((void *)d.segs, m.h_sdB, sizeof(SegDesc), cudaMemcpyHostToDevice, st));
-    h.Kp = Kp;
     ctx->seg[0] = h;
     ctx->seg[0].vox_off = 0;
     ctx->seg[0].seed_off = 0;
@@ -1800,6 +1792,10 @@ static asv_status stream_push(asv_ctx *ctx, bool fed, const uint8_t *rgb, const 
     CK(cudaMemcpyAsync(labels_out, m.s.lab_out, sizeof(int32_t) * WH * done, cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(m.h_ctr2, m.s.ctr, sizeof(int) * STREAM_CTR_WORDS, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    if (m.h_ctr[STREAM_KP] == -2) return fail(ctx, ASV_ERR_CUDA, "density placement produced fewer seeds than the grid");
+    if (m.h_ctr[STREAM_KP] < 0) return fail(ctx, ASV_ERR_OVER_BUDGET, "kept + new seeds exceed the stream's seed capacity");
+    const int Kp = m.h_ctr[STREAM_KP];
+    ctx->seg[0].Kp = Kp;
     float wms = 0.f;
     CK(cudaEventElapsedTime(&wms, ctx->ev[ev0], ctx->ev[ev0 + 1]));
     ctx->stats.window_ms = wms;

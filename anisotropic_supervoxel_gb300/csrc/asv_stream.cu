@@ -15,8 +15,15 @@
 __global__ void __launch_bounds__(1024) k_stream_compose(AsvDev d, StreamDev s, int Kn, int Kcap)
 {
     const int kept = s.ctr[STREAM_KEPT], placed = s.ctr[STREAM_PLACED];
-    if (kept + Kn > Kcap) {
-        if (threadIdx.x == 0) s.ctr[STREAM_KP] = -1;   // over capacity: the host reports it
+    SegDesc *seg = const_cast<SegDesc *>(d.segs);           // the block's seed count is set here, on the device
+    const bool short_grid = d.post[POST_VALID] != Kn;
+    if (short_grid || kept + Kn > Kcap) {
+        // fewer placed seeds than the grid, or over capacity: the block runs
+        // with no seeds and leaves the stream's state alone; the host reports it
+        if (threadIdx.x == 0) {
+            s.ctr[STREAM_KP] = short_grid ? -2 : -1;
+            seg[0].Kp = 0;
+        }
         return;
     }
     float4 *tmp = d.grid;
@@ -32,7 +39,10 @@ __global__ void __launch_bounds__(1024) k_stream_compose(AsvDev d, StreamDev s, 
         d.pos0[kept + i] = make_float4(p.x, p.y, p.z, (float)(kept + i));
         s.gmap_cur[kept + i] = placed + i;
     }
-    if (threadIdx.x == 0) s.ctr[STREAM_KP] = kept + Kn;
+    if (threadIdx.x == 0) {
+        s.ctr[STREAM_KP] = kept + Kn;
+        seg[0].Kp = kept + Kn;
+    }
 }
 
 // After a block: final centroids of the alive seeds
@@ -42,6 +52,7 @@ __global__ void __launch_bounds__(1024) k_stream_compose(AsvDev d, StreamDev s, 
 __global__ void __launch_bounds__(1024) k_stream_next(AsvDev d, StreamDev s, float z_keep,
                                                       float z_shift, int keep)
 {
+    if (s.ctr[STREAM_KP] < 0) return;                        // a refused block: the state stays
     const SegDesc &S = d.segs[0];
     const int Kp = S.Kp;
     const unsigned long long *sums = d.sums + 8ull * S.seed_off;
@@ -106,7 +117,7 @@ __global__ void __launch_bounds__(256) k_stream_map(AsvDev d, StreamDev s, long 
     const SegDesc &S = d.segs[0];
     const int32_t *post = (S.final_buf ? d.labA : d.labB) + S.vox_off;
     long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= n) return;
+    if (v >= n || s.ctr[STREAM_KP] < 0) return;
     int l = post[v];
     s.lab_out[v] = (l >= 0 && l < S.Kp) ? s.gmap_cur[l] : 0;
 }
