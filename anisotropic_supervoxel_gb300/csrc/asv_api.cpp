@@ -1638,10 +1638,10 @@ static asv_status stream_push(asv_ctx *ctx, bool fed, const uint8_t *rgb, const 
     cudaStream_t st = ctx->st;
     if (b > 0) {                                                    // Render.cpp:405-412, :545-556
         size_t src = (size_t)(m.prev_Db - 10) * WH, n = 10 * WH;
-        CK(cudaMemcpyAsync(d.rgb, d.rgb + 3 * src, 3 * n, cudaMemcpyDeviceToDevice, st));
-        CK(cudaMemcpyAsync(d.lab, d.lab + src, 4 * n, cudaMemcpyDeviceToDevice, st));
-        CK(cudaMemcpyAsync(d.fwd, d.fwd + src, 8 * n, cudaMemcpyDeviceToDevice, st));
-        CK(cudaMemcpyAsync(d.bwd, d.bwd + src, 8 * n, cudaMemcpyDeviceToDevice, st));
+        CK(asv_copy_d2d(d.rgb, d.rgb + 3 * src, 3 * n, st));
+        CK(asv_copy_d2d(d.lab, d.lab + src, 4 * n, st));
+        CK(asv_copy_d2d(d.fwd, d.fwd + src, 8 * n, st));
+        CK(asv_copy_d2d(d.bwd, d.bwd + src, 8 * n, st));
     }
     const size_t nnew = (size_t)(Db - z0) * WH;
     if (fed) {                                                      // uploaded during the previous block
@@ -1651,11 +1651,11 @@ static asv_status stream_push(asv_ctx *ctx, bool fed, const uint8_t *rgb, const 
             asv_launch_preprocess(m.stg_rgb[slot], d.rgb + 3 * z0 * WH, m.W, m.H, Db - z0, st);
             CK(cudaGetLastError());
         } else {
-            CK(cudaMemcpyAsync(d.rgb + 3 * z0 * WH, m.stg_rgb[slot], 3 * nnew, cudaMemcpyDeviceToDevice, st));
+            CK(asv_copy_d2d(d.rgb + 3 * z0 * WH, m.stg_rgb[slot], 3 * nnew, st));
         }
         if (!device_flow) {
-            CK(cudaMemcpyAsync(d.fwd + z0 * WH, m.stg_fwd[slot], 8 * nnew, cudaMemcpyDeviceToDevice, st));
-            CK(cudaMemcpyAsync(d.bwd + z0 * WH, m.stg_bwd[slot], 8 * nnew, cudaMemcpyDeviceToDevice, st));
+            CK(asv_copy_d2d(d.fwd + z0 * WH, m.stg_fwd[slot], 8 * nnew, st));
+            CK(asv_copy_d2d(d.bwd + z0 * WH, m.stg_bwd[slot], 8 * nnew, st));
         }
         CK(cudaEventRecord(ctx->used_ev[slot], st));
     } else {

@@ -137,3 +137,31 @@ void asv_launch_stream_map(const AsvDev &d, const StreamDev &s, long long n, cud
 {
     k_stream_map<<<(int)((n + 255) / 256), 256, 0, st>>>(d, s, n);
 }
+
+// device-to-device copy of 16-byte words on the SMs
+__global__ void __launch_bounds__(256) k_copy16(const uint4 *__restrict__ src, uint4 *__restrict__ dst, size_t n)
+{
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+
+// A block's device-to-device copies (the overlap shift, the staging of fed
+// frames) as a kernel when both ends and the size are 16-byte aligned, so
+// they do not queue on a copy engine behind the next block's upload from
+// the host; a cudaMemcpyAsync otherwise.
+cudaError_t asv_copy_d2d(void *dst, const void *src, size_t bytes, cudaStream_t st)
+{
+    if (!bytes) return cudaSuccess;
+    const uintptr_t a = (uintptr_t)dst, b = (uintptr_t)src;
+    const bool apart = a + bytes <= b || b + bytes <= a;
+    if (apart && ((a | b | bytes) & 15u) == 0) {
+        const size_t n = bytes / 16;
+        int sms = 0, dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const size_t want = (n + 255) / 256, cap = (size_t)(sms > 0 ? sms : 1) * 8;
+        k_copy16<<<(unsigned)(want < cap ? want : cap), 256, 0, st>>>((const uint4 *)src, (uint4 *)dst, n);
+        return cudaGetLastError();
+    }
+    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, st);
+}

@@ -19,3 +19,4 @@ void asv_launch_stream_compose(const AsvDev &d, const StreamDev &s, int Kn, int 
 void asv_launch_stream_next(const AsvDev &d, const StreamDev &s, float z_keep, float z_shift, int keep,
                             cudaStream_t st);
 void asv_launch_stream_map(const AsvDev &d, const StreamDev &s, long long n, cudaStream_t st);
+cudaError_t asv_copy_d2d(void *dst, const void *src, size_t bytes, cudaStream_t st);
