@@ -146,6 +146,8 @@ SIGNATURES = {
     "asv_stream_feed": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "asv_stream_feed_bgr": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "asv_stream_push_fed": (c_int, [c_void_p, c_void_p, P(c_int)]),
+    "asv_stream_push_fed_async": (c_int, [c_void_p, c_void_p]),
+    "asv_stream_wait": (c_int, [c_void_p, P(c_int), P(c_int)]),
     # include/asv_host.h
     "asv_synth_clip": (c_int, [P(SynthParams), c_void_p, c_void_p, c_void_p]),
     "asv_synth_truth": (c_int, [P(SynthParams), c_void_p]),

@@ -181,11 +181,20 @@ struct asv_ctx {
         // pinned block hpin), so that none of them is a synchronous copy
         // from pageable memory: prefixes, the segment descriptor, the
         // counters after the seed composition and at the end, cells, grid
-        int *h_pref = nullptr, *h_ctr = nullptr, *h_ctr2 = nullptr, *h_cells = nullptr;
-        SegDesc *h_sdA = nullptr;
-        float4 *h_grid = nullptr;
+        // (one set per block parity: two blocks can be in flight)
+        int *h_pref[2] = {}, *h_ctr[2] = {}, *h_ctr2[2] = {}, *h_cells[2] = {};
+        SegDesc *h_sdA[2] = {};
+        float4 *h_grid[2] = {};
         size_t h_cells_cap = 0;
+        // blocks enqueued and not yet finished (asv_stream_push_fed_async /
+        // asv_stream_wait), oldest first
+        struct Flight { int block = -1, done = 0, launches = 0; };
+        Flight flight[2];
+        int nflight = 0;
+        bool failed = false;                       // a block was refused: the stream is over
     } sm;
+    // per block parity: device time start, end, and everything read back
+    cudaEvent_t sev[6] = {};
     void *hpin = nullptr;                     // pinned host block of the streaming form
     size_t hpin_bytes = 0;
     // the streaming form's Lloyd loop as a CUDA graph, replayed by every
@@ -645,6 +654,7 @@ asv_status asv_destroy(asv_ctx *ctx)
     cudaStreamSynchronize(ctx->st);
     for (auto e : ctx->ev) cudaEventDestroy(e);
     if (ctx->hpin) cudaFreeHost(ctx->hpin);
+    for (auto e : ctx->sev) if (e) cudaEventDestroy(e);
     if (ctx->cp) {
         cudaStreamDestroy(ctx->cp);
         for (int k = 0; k < 2; k++) { cudaEventDestroy(ctx->fed_ev[k]); cudaEventDestroy(ctx->used_ev[k]); }
@@ -1485,10 +1495,15 @@ asv_status asv_stream_begin(asv_ctx *ctx, int W, int H, int D_all, int K_video, 
     {                                              // the pinned host staging of every block's small copies
         size_t off = 0;
         auto take = [&](size_t b) { const size_t o = off; off += (b + 255) & ~(size_t)255; return o; };
-        const size_t o_pref = take(6 * sizeof(int)), o_sda = take(sizeof(SegDesc)),
-                     o_ctr = take(sizeof(int) * STREAM_CTR_WORDS),
-                     o_ctr2 = take(sizeof(int) * STREAM_CTR_WORDS), o_cells = take(sizeof(int) * cap.cells.size()),
-                     o_grid = take(sizeof(float4) * (size_t)m.Kcap);
+        size_t o_pref[2], o_sda[2], o_ctr[2], o_ctr2[2], o_cells[2], o_grid[2];
+        for (int q = 0; q < 2; q++) {
+            o_pref[q] = take(6 * sizeof(int));
+            o_sda[q] = take(sizeof(SegDesc));
+            o_ctr[q] = take(sizeof(int) * STREAM_CTR_WORDS);
+            o_ctr2[q] = take(sizeof(int) * STREAM_CTR_WORDS);
+            o_cells[q] = take(sizeof(int) * cap.cells.size());
+            o_grid[q] = take(sizeof(float4) * (size_t)m.Kcap);
+        }
         if (ctx->hpin_bytes < off) {
             if (ctx->hpin) {
                 cudaStreamSynchronize(ctx->st);
@@ -1504,13 +1519,21 @@ asv_status asv_stream_begin(asv_ctx *ctx, int W, int H, int D_all, int K_video, 
             ctx->hpin_bytes = off;
         }
         char *hb = (char *)ctx->hpin;
-        m.h_pref = (int *)(hb + o_pref);
-        m.h_sdA = (SegDesc *)(hb + o_sda);
-        m.h_ctr = (int *)(hb + o_ctr);
-        m.h_ctr2 = (int *)(hb + o_ctr2);
-        m.h_cells = (int *)(hb + o_cells);
-        m.h_grid = (float4 *)(hb + o_grid);
+        for (int q = 0; q < 2; q++) {
+            m.h_pref[q] = (int *)(hb + o_pref[q]);
+            m.h_sdA[q] = (SegDesc *)(hb + o_sda[q]);
+            m.h_ctr[q] = (int *)(hb + o_ctr[q]);
+            m.h_ctr2[q] = (int *)(hb + o_ctr2[q]);
+            m.h_cells[q] = (int *)(hb + o_cells[q]);
+            m.h_grid[q] = (float4 *)(hb + o_grid[q]);
+        }
         m.h_cells_cap = cap.cells.size();
+        for (auto &e : ctx->sev)
+            if (!e && cudaEventCreate(&e) != cudaSuccess) {
+                cudaGetLastError();
+                e = nullptr;
+                return fail(ctx, ASV_ERR_CUDA, "cudaEventCreate: stream events");
+            }
     }
     cap.grid.assign((size_t)4 * m.Kcap, 0.f);
     ctx->seg.assign(1, cap);
@@ -1614,19 +1637,24 @@ asv_status asv_stream_feed_bgr(asv_ctx *ctx, const uint8_t *bgr, const float *fw
     return stream_feed(ctx, true, bgr, fwd, bwd);
 }
 
-// asv_stream_push (new frames from the caller) and asv_stream_push_fed (new
-// frames fed ahead into a staging slot)
-static asv_status stream_push(asv_ctx *ctx, bool fed, const uint8_t *rgb, const float *fwd, const float *bwd,
-                              int32_t *labels_out, int *done_frames)
+// Enqueues the next block on the context's stream: new frames from the
+// caller (asv_stream_push) or fed ahead into a staging slot
+// (asv_stream_push_fed); stream_finish waits for it.  Everything the block
+// reads back goes to the pinned set of its parity, so two blocks can be in
+// flight.
+static asv_status stream_enqueue(asv_ctx *ctx, bool fed, const uint8_t *rgb, const float *fwd, const float *bwd,
+                                 int32_t *labels_out)
 {
     if (!ctx) return ASV_ERR_BAD_ARG;
     auto &m = ctx->sm;
     if (!m.on) return fail(ctx, ASV_ERR_STATE, "no stream: call asv_stream_begin first");
+    if (m.failed) return fail(ctx, ASV_ERR_STATE, "a block of the stream was refused");
     if (m.next >= m.nb) return fail(ctx, ASV_ERR_STATE, "the stream is finished");
+    if (m.nflight >= 2) return fail(ctx, ASV_ERR_STATE, "two blocks in flight: asv_stream_wait first");
     if (fed && m.fed_next <= m.next) return fail(ctx, ASV_ERR_STATE, "the block was not fed: asv_stream_feed first");
     if (!fed && m.fed_next > m.next) return fail(ctx, ASV_ERR_STATE, "the block was fed: use asv_stream_push_fed");
     if (!labels_out || (!fed && (!rgb || (!fwd) != (!bwd)))) return fail(ctx, ASV_ERR_BAD_ARG, "NULL buffer");
-    const int slot = m.next & 1;
+    const int slot = m.next & 1, par = slot;                        // staging slot and pinned set
     const bool device_flow = fed ? m.fed_devflow[slot] : !fwd;     // no flow given: computed here
     cudaSetDevice(ctx->cfg.device);
     const int b = m.next;
@@ -1665,11 +1693,9 @@ static asv_status stream_push(asv_ctx *ctx, bool fed, const uint8_t *rgb, const 
             CK(cudaMemcpyAsync(d.bwd + z0 * WH, bwd, 8 * nnew, cudaMemcpyHostToDevice, st));
         }
     }
-    asv_status es = ensure_events(ctx, 2);
-    if (es != ASV_OK) return es;
-    const size_t ev0 = ctx->ev.size() - 2;
+    cudaEvent_t ev_start = ctx->sev[3 * par], ev_end = ctx->sev[3 * par + 1], ev_read = ctx->sev[3 * par + 2];
     if (device_flow) {
-        CK(cudaEventRecord(ctx->ev[ev0], st));
+        CK(cudaEventRecord(ev_start, st));
         // the block's flow from its own frames, as the streaming program does
         // per block.  Pairs within the overlap frames were computed by the
         // previous block (same two frames, same flow) and came along with the
@@ -1716,27 +1742,28 @@ static asv_status stream_push(asv_ctx *ctx, bool fed, const uint8_t *rgb, const 
     const int chunks = (int)((sd.nvox + ASV_CHUNK - 1) / ASV_CHUNK);
     d.total_tiles = tiles;
     d.total_chunks = chunks;
-    // (the pinned staging is free again: the previous block ended with a synchronize)
+    // (the pinned set of this parity is free again: its previous block was finished)
     if (h.cells.size() > m.h_cells_cap || Kn > m.Kcap) return fail(ctx, ASV_ERR_STATE, "block larger than its layout");
-    int *pref = m.h_pref;
+    int *pref = m.h_pref[par];
     pref[0] = 0; pref[1] = tiles; pref[2] = 0; pref[3] = chunks; pref[4] = 0; pref[5] = seed_cap;
     CK(cudaMemcpyAsync((void *)d.tile_prefix, pref, 2 * sizeof(int), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync((void *)d.chunk_prefix, pref + 2, 2 * sizeof(int), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync((void *)d.seed_prefix, pref + 4, 2 * sizeof(int), cudaMemcpyHostToDevice, st));
-    *m.h_sdA = sd;
-    CK(cudaMemcpyAsync((void *)d.segs, m.h_sdA, sizeof(SegDesc), cudaMemcpyHostToDevice, st));
-    std::memcpy(m.h_cells, h.cells.data(), sizeof(int) * h.cells.size());
-    CK(cudaMemcpyAsync(d.cells, m.h_cells, sizeof(int) * h.cells.size(), cudaMemcpyHostToDevice, st));
+    *m.h_sdA[par] = sd;
+    CK(cudaMemcpyAsync((void *)d.segs, m.h_sdA[par], sizeof(SegDesc), cudaMemcpyHostToDevice, st));
+    std::memcpy(m.h_cells[par], h.cells.data(), sizeof(int) * h.cells.size());
+    CK(cudaMemcpyAsync(d.cells, m.h_cells[par], sizeof(int) * h.cells.size(), cudaMemcpyHostToDevice, st));
+    float4 *grid4 = m.h_grid[par];
     for (int k = 0; k < Kn; k++)
-        m.h_grid[k] = make_float4(h.grid[4 * k], h.grid[4 * k + 1], h.grid[4 * k + 2], h.grid[4 * k + 3]);
-    CK(cudaMemcpyAsync(d.grid, m.h_grid, sizeof(float4) * Kn, cudaMemcpyHostToDevice, st));
+        grid4[k] = make_float4(h.grid[4 * k], h.grid[4 * k + 1], h.grid[4 * k + 2], h.grid[4 * k + 3]);
+    CK(cudaMemcpyAsync(d.grid, grid4, sizeof(float4) * Kn, cudaMemcpyHostToDevice, st));
     ctx->maxpass = h.npass;
     ctx->jfa_blocks = jfa_blocks_for(ctx, tiles);
 
     // device time of the window's compute: from here (its frames are on the
     // device; before the flow kernels when the flow is computed here) to the
     // labels mapped, before they are read back
-    if (!device_flow) CK(cudaEventRecord(ctx->ev[ev0], st));
+    if (!device_flow) CK(cudaEventRecord(ev_start, st));
     asv_launch_rgb2lab(d, st);                                   // new frames only (lab_from)
     CK(cudaMemsetAsync(d.dacc, 0, sizeof(unsigned long long) * d.total_seeds, st));
     asv_launch_density(d, st);
@@ -1746,7 +1773,7 @@ static asv_status stream_push(asv_ctx *ctx, bool fed, const uint8_t *rgb, const 
     // the composed seed count went to the segment descriptor on the device
     // (k_stream_compose), so the rest of the block is enqueued without a
     // host round trip; the counters of this point are read at the end
-    CK(cudaMemcpyAsync(m.h_ctr, m.s.ctr, sizeof(int) * STREAM_CTR_WORDS, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(m.h_ctr[par], m.s.ctr, sizeof(int) * STREAM_CTR_WORDS, cudaMemcpyDeviceToHost, st));
     ctx->seg[0] = h;
     ctx->seg[0].vox_off = 0;
     ctx->seg[0].seed_off = 0;
@@ -1788,30 +1815,66 @@ static asv_status stream_push(asv_ctx *ctx, bool fed, const uint8_t *rgb, const 
     asv_launch_stream_map(d, m.s, (long long)WH * done, st);
     ctx->launches += 2;
     CK(cudaGetLastError());
-    CK(cudaEventRecord(ctx->ev[ev0 + 1], st));
+    CK(cudaEventRecord(ev_end, st));
     CK(cudaMemcpyAsync(labels_out, m.s.lab_out, sizeof(int32_t) * WH * done, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(m.h_ctr2, m.s.ctr, sizeof(int) * STREAM_CTR_WORDS, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    if (m.h_ctr[STREAM_KP] == -2) return fail(ctx, ASV_ERR_CUDA, "density placement produced fewer seeds than the grid");
-    if (m.h_ctr[STREAM_KP] < 0) return fail(ctx, ASV_ERR_OVER_BUDGET, "kept + new seeds exceed the stream's seed capacity");
-    const int Kp = m.h_ctr[STREAM_KP];
-    ctx->seg[0].Kp = Kp;
-    float wms = 0.f;
-    CK(cudaEventElapsedTime(&wms, ctx->ev[ev0], ctx->ev[ev0 + 1]));
-    ctx->stats.window_ms = wms;
-    ctx->stats.launches = ctx->launches;
+    CK(cudaMemcpyAsync(m.h_ctr2[par], m.s.ctr, sizeof(int) * STREAM_CTR_WORDS, cudaMemcpyDeviceToHost, st));
+    CK(cudaEventRecord(ev_read, st));
+    // the next block's device buffers and frame positions (its kernels run
+    // after these in stream order)
     std::swap(m.s.kept_pos, m.s.kept_next);
     std::swap(m.s.gmap_prev, m.s.gmap_cur);
-    m.placed = m.h_ctr2[STREAM_PLACED];
-    m.kept = m.h_ctr2[STREAM_KEPT];
-    m.last_Kp = Kp;
     m.prev_Db = Db;
     m.next++;
     m.fed_next = std::max(m.fed_next, m.next);
     ctx->have_rgb = ctx->have_flow = ctx->have_pos0 = ctx->have_M0 = ctx->have_lab = true;
     ctx->seeded = ctx->ran = true;
-    if (done_frames) *done_frames = done;
+    auto &f = m.flight[m.nflight++];
+    f.block = b;
+    f.done = done;
+    f.launches = ctx->launches;
     return ASV_OK;
+}
+
+// Waits for the oldest block in flight and takes in what it read back.
+static asv_status stream_finish(asv_ctx *ctx, int *block, int *done_frames)
+{
+    if (!ctx) return ASV_ERR_BAD_ARG;
+    auto &m = ctx->sm;
+    if (!m.on || m.nflight == 0) return fail(ctx, ASV_ERR_STATE, "no block in flight");
+    const asv_ctx::Stream::Flight f = m.flight[0];
+    m.flight[0] = m.flight[1];
+    m.nflight--;
+    const int par = f.block & 1;
+    cudaSetDevice(ctx->cfg.device);
+    CK(cudaEventSynchronize(ctx->sev[3 * par + 2]));
+    const int kp = m.h_ctr[par][STREAM_KP];
+    if (kp < 0) {
+        m.failed = true;
+        return fail(ctx, kp == -2 ? ASV_ERR_CUDA : ASV_ERR_OVER_BUDGET,
+                    kp == -2 ? "density placement produced fewer seeds than the grid"
+                             : "kept + new seeds exceed the stream's seed capacity");
+    }
+    float wms = 0.f;
+    CK(cudaEventElapsedTime(&wms, ctx->sev[3 * par], ctx->sev[3 * par + 1]));
+    ctx->stats.window_ms = wms;
+    ctx->stats.launches = f.launches;
+    if (m.nflight == 0) ctx->seg[0].Kp = kp;                   // the host record is the last block's
+    m.placed = m.h_ctr2[par][STREAM_PLACED];
+    m.kept = m.h_ctr2[par][STREAM_KEPT];
+    m.last_Kp = kp;
+    if (block) *block = f.block;
+    if (done_frames) *done_frames = f.done;
+    return ASV_OK;
+}
+
+static asv_status stream_push(asv_ctx *ctx, bool fed, const uint8_t *rgb, const float *fwd, const float *bwd,
+                              int32_t *labels_out, int *done_frames)
+{
+    if (ctx && ctx->sm.nflight > 0)
+        return fail(ctx, ASV_ERR_STATE, "blocks in flight: asv_stream_wait for them first");
+    const asv_status s = stream_enqueue(ctx, fed, rgb, fwd, bwd, labels_out);
+    if (s != ASV_OK) return s;
+    return stream_finish(ctx, nullptr, done_frames);
 }
 
 asv_status asv_stream_push(asv_ctx *ctx, const uint8_t *rgb, const float *fwd, const float *bwd,
@@ -1823,6 +1886,16 @@ asv_status asv_stream_push(asv_ctx *ctx, const uint8_t *rgb, const float *fwd, c
 asv_status asv_stream_push_fed(asv_ctx *ctx, int32_t *labels_out, int *done_frames)
 {
     return stream_push(ctx, true, nullptr, nullptr, nullptr, labels_out, done_frames);
+}
+
+asv_status asv_stream_push_fed_async(asv_ctx *ctx, int32_t *labels_out)
+{
+    return stream_enqueue(ctx, true, nullptr, nullptr, nullptr, labels_out);
+}
+
+asv_status asv_stream_wait(asv_ctx *ctx, int *block, int *done_frames)
+{
+    return stream_finish(ctx, block, done_frames);
 }
 
 } // extern "C"

@@ -6,6 +6,7 @@ plain per-clip pipeline of `Render::run` (GPU-AS/Render.cpp:100-350) with
 host buffers in and labels out.  Everything runs on the CUDA path of
 libasv.so; there is no CPU fallback.
 """
+import collections
 import ctypes
 import os
 
@@ -318,6 +319,7 @@ class Stream(Image):
         self._ck(self.lib.asv_stream_begin(self.h, W, H, D_all, K_video, seeds_num_100, block_size))
         self.W, self.H = W, H
         self._fed = {}       # block -> the fed arrays, alive until that block's push returns
+        self._inflight = collections.deque()   # (block, first frame, labels out) of enqueued blocks
 
     def info(self):
         i = _lib.StreamInfo()
@@ -392,6 +394,30 @@ class Stream(Image):
         self._ck(self.lib.asv_stream_push_fed(self.h, _ptr(out), ctypes.byref(done)))
         self._fed.pop(inf.next_block, None)
         return inf.block_start, out[:done.value]
+
+    def push_fed_async(self, out):
+        """asv_stream_push_fed_async: enqueue the next (fed) block and return;
+        `wait` gives its labels, in `out` (kept here until then).  Returns the
+        block's index."""
+        inf = self.info()
+        D = inf.block_end - inf.block_start
+        if (out.dtype != np.int32 or not out.flags.c_contiguous or out.ndim != 3
+                or out.shape[0] < D or out.shape[1:] != (self.H, self.W)):
+            raise ValueError(f"out must be C-contiguous int32 of at least ({D}, {self.H}, {self.W})")
+        self._ck(self.lib.asv_stream_push_fed_async(self.h, _ptr(out)))
+        self._inflight.append((inf.next_block, inf.block_start, out))
+        return inf.next_block
+
+    def wait(self):
+        """asv_stream_wait: the oldest block in flight, as
+        (first frame index, labels [done,H,W] int32, a view of its `out`)."""
+        blk, done = ctypes.c_int(), ctypes.c_int()
+        try:
+            self._ck(self.lib.asv_stream_wait(self.h, ctypes.byref(blk), ctypes.byref(done)))
+        finally:
+            b, f0, out = self._inflight.popleft() if self._inflight else (None, 0, None)
+            self._fed.pop(b, None)
+        return f0, out[:done.value]
 
 
 class Server:

@@ -641,7 +641,56 @@ def run_stream_720p(args, device_flow=False):
     clk = clocks.stop()
     st.close()
     value, dev_s = replicas_value(vox_it / 1e6, sum(dev_ms) / 1e3, f"cuda:{local}")
-    e2e_val, e2e_s = replicas_value(vox_it / 1e6, t_region, f"cuda:{local}")
+    e2e_sync, _ = replicas_value(vox_it / 1e6, t_region, f"cuda:{local}")
+
+    # e2e, pipelined: the same video from its start on a new streaming
+    # context; every timed step copies its window's new frames into a pinned
+    # set, feeds them (copy stream), enqueues the window
+    # (asv_stream_push_fed_async) and waits for the window before it
+    # (asv_stream_wait: its labels in host memory), so the host's work for
+    # one window overlaps the device's work on the other.  The frames are
+    # generated before the timed region (generation takes longer than a
+    # window).  K_e2e windows, at most 12 (5 GB of frames held).
+    k_e2e = min(args.steps, 12)
+    w2 = 2                                                 # warm-up windows of this phase
+    st2 = new_stream()
+    pre = []
+    for b in range(w2 + k_e2e + 1):
+        _, e, n = st2.block(b)
+        pre.append(workloads.stream_frames(w, e - n, n))
+    labs = [_pinned(np.zeros((bs + bs // 3, H, W), np.int32)) for _ in range(2)]
+
+    def put(b):
+        """window b's frames into pinned set b % 2"""
+        n = pre[b][0].shape[0]
+        p = pins[b % 2]
+        for key, arr in zip(("rgb", "fwd", "bwd"), pre[b]):
+            p[key][:n] = arr
+        return (p["rgb"][:n],) if device_flow else (p["rgb"][:n], p["fwd"][:n], p["bwd"][:n])
+
+    st2.feed(*put(0))
+    for b in range(w2):
+        st2.feed(*put(b + 1))
+        st2.push_fed(out=labs[b % 2])
+    torch.cuda.synchronize()
+    barrier()
+    t_p0 = time.perf_counter()
+    st2.push_fed_async(labs[w2 % 2])
+    vox_p = 0
+    for j in range(k_e2e):
+        b = w2 + j
+        if j + 1 < k_e2e:
+            st2.feed(*put(b + 1))                           # set (b+1) % 2: its window b-1 has finished
+            st2.push_fed_async(labs[(b + 1) % 2])
+        f0, lab = st2.wait()
+        blk = st2.block(b)
+        vox_p += W * H * (blk[1] - blk[0]) * I
+    torch.cuda.synchronize()
+    barrier()
+    t_p = time.perf_counter() - t_p0
+    st2.close()
+    del pre
+    e2e_val, e2e_s = replicas_value(vox_p / 1e6, t_p, f"cuda:{local}")
 
     # k_jfa per launch at this size: the Lloyd loop of the video's first 30
     # frames (2000 seeds, stream variant) with a CUDA event around every pass
@@ -711,7 +760,11 @@ def run_stream_720p(args, device_flow=False):
                                    "window's compute, its labels down into a pinned buffer); device_*: its "
                                    "compute alone", "target_p99": 33.0},
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(h2d / args.steps),
-                    "d2h_bytes_per_step": int(d2h / args.steps)},
+                    "d2h_bytes_per_step": int(d2h / args.steps), "windows": k_e2e,
+                    "what": "pipelined windows through asv_stream_feed + asv_stream_push_fed_async + "
+                            "asv_stream_wait (per window: new frames copied into pinned memory and up, "
+                            "compute, labels down), wall time of the whole run",
+                    "sync": e2e_sync},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind, "kernel": "k_jfa",
                          "bytes_per_launch": JFA_BYTES_PER_VOXEL * nvox, "launch_ms": jfa_launch_s * 1e3,

@@ -349,6 +349,18 @@ asv_status asv_stream_feed(asv_ctx *ctx, const uint8_t *rgb, const float *fwd, c
 asv_status asv_stream_feed_bgr(asv_ctx *ctx, const uint8_t *bgr, const float *fwd, const float *bwd);
 asv_status asv_stream_push_fed(asv_ctx *ctx, int32_t *labels_out, int *done_frames);
 
+/* Pipelined form of asv_stream_push_fed: enqueues the next (fed) block and
+ * returns at once, so the host can feed and enqueue the block after it while
+ * this one runs; asv_stream_wait waits for the oldest block in flight and
+ * gives its index and finished frame count (its labels are then in the
+ * labels_out given at its enqueue, which must stay untouched until then).
+ * At most two blocks are in flight (ASV_ERR_STATE beyond); the synchronous
+ * asv_stream_push / asv_stream_push_fed need none in flight.  A block that
+ * is refused (seed capacity) is reported by its wait, and the stream then
+ * takes no further block.  No counterpart in the reference. */
+asv_status asv_stream_push_fed_async(asv_ctx *ctx, int32_t *labels_out);
+asv_status asv_stream_wait(asv_ctx *ctx, int *block, int *done_frames);
+
 /* ---- serving ------------------------------------------------------------- */
 
 /* No counterpart in the reference (a desktop program that segments one clip

@@ -89,6 +89,37 @@ def test_stream_fed_ahead_matches_oracle(asv, orc):
     assert np.array_equal(out, want)
 
 
+def test_stream_pipelined_matches_oracle(asv, orc):
+    """two blocks in flight (asv_stream_push_fed_async / asv_stream_wait) give
+    the oracle's labels; the in-flight rules are enforced"""
+    W, H, D, s100, iters = 48, 40, 75, 200, 4
+    rgb, fwd, bwd = asv.synth_clip(W, H, D, n_ellipses=6, noise_sigma=5.0, vmax=2.0, jitter=0.3,
+                                   drift_amp=2.0, drift_period=40.0, seed=W + D)
+    st = asv.Stream(W, H, D, seeds_num_100=s100, block_size=30, lloyd_iters=iters)
+    assert st.info().blocks == 3
+    bufs = [np.full((40, H, W), -9, np.int32) for _ in range(2)]
+    out = np.full((D, H, W), -7, np.int32)
+    st.feed(*_fed_frames(st, 0, rgb, fwd, bwd))
+    assert st.push_fed_async(bufs[0]) == 0
+    st.feed(*_fed_frames(st, 1, rgb, fwd, bwd))
+    assert st.push_fed_async(bufs[1]) == 1                   # two blocks in flight
+    st.feed(*_fed_frames(st, 2, rgb, fwd, bwd))
+    with pytest.raises(asv.AsvError):
+        st.push_fed_async(np.zeros((40, H, W), np.int32))    # a third: wait first
+    with pytest.raises(asv.AsvError):
+        st.push_fed()                                        # synchronous push with blocks in flight
+    for b in range(3):
+        f0, lab = st.wait()
+        out[f0:f0 + lab.shape[0]] = lab
+        if b == 0:
+            assert st.push_fed_async(bufs[0]) == 2           # block 0's buffer is free again
+    with pytest.raises(asv.AsvError):
+        st.wait()                                            # nothing in flight
+    st.close()
+    want, info = orc.run_stream(rgb, fwd, bwd, seeds_num_100=s100, iters=iters, nthreads=8)
+    assert np.array_equal(out, want)
+
+
 def test_stream_fed_ahead_device_flow_equals_push(asv):
     """fed without flow: the device computes each block's flow, as push does"""
     W, H, D = 40, 32, 56
