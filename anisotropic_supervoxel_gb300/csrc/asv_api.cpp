@@ -1469,6 +1469,7 @@ asv_status asv_stream_begin(asv_ctx *ctx, int W, int H, int D_all, int K_video, 
     if (W < 1 || H < 1 || D_all < 2 || block_size < 6 || (K_video < 1 && seeds_num_100 < 1))
         return fail(ctx, ASV_ERR_BAD_ARG, "need W,H >= 1, D_all >= 2, block_size >= 6 and seeds");
     cudaSetDevice(ctx->cfg.device);
+    if (ctx->sm.nflight) cudaStreamSynchronize(ctx->st);   // blocks in flight finish their copies first
     free_layout(ctx);
     ctx->cfg.variant = ASV_VARIANT_STREAM;          // compactness 6, no angle filter
     auto &m = ctx->sm;

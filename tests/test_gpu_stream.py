@@ -120,6 +120,24 @@ def test_stream_pipelined_matches_oracle(asv, orc):
     assert np.array_equal(out, want)
 
 
+def test_stream_close_with_blocks_in_flight(asv):
+    """closing a stream with two blocks enqueued and not waited for is clean,
+    and a new stream on the device works after it"""
+    W, H, D = 40, 32, 56
+    rgb, fwd, bwd = asv.synth_clip(W, H, D, n_ellipses=6, noise_sigma=5.0, vmax=2.0, jitter=0.3,
+                                   drift_amp=2.0, drift_period=40.0, seed=21)
+    bufs = [np.full((40, H, W), -9, np.int32) for _ in range(2)]
+    st = asv.Stream(W, H, D, seeds_num_100=250, block_size=30, lloyd_iters=3)
+    for b in range(2):
+        st.feed(*_fed_frames(st, b, rgb, fwd, bwd))
+        st.push_fed_async(bufs[b])
+    st.close()                                               # waits for the device, drops the blocks
+    assert (bufs[0] != -9).any()                             # the first block's labels did arrive
+    got, nb, _ = _run_stream(asv, rgb, fwd, bwd, 250, 3)
+    want, _, _ = _run_stream(asv, rgb, fwd, bwd, 250, 3, reuse_out=True)
+    assert nb == 2 and np.array_equal(got, want)
+
+
 def test_stream_fed_ahead_device_flow_equals_push(asv):
     """fed without flow: the device computes each block's flow, as push does"""
     W, H, D = 40, 32, 56
